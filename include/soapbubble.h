@@ -1,0 +1,167 @@
+/*
+ * soapbubble_gb300 -- C ABI of the GB300 soap-bubble time step.
+ *
+ * The reference (RiverIntheSky/SoapBubble) has no plugin or FFI layer: its
+ * step is reached through the C++ classes Bubble (include/bubble.cuh:36-89,
+ * constructor + run()), Solver (include/solver.cuh:15-150, stepForward() at
+ * kernel/solver.cu:260-292) and Quantity (include/quantity.cuh:5-96, host
+ * buffers indexed [theta][phi]).  These entry points replace that surface;
+ * each declaration names the reference interface it stands in for.
+ *
+ * Conventions
+ *   - Every function returns an sb_status (0 = success); sb_last_error()
+ *     gives a message for the calling thread.  Nothing calls exit().
+ *   - Host arrays are row-major [theta][phi] with row stride nPhi, exactly the
+ *     reference's host buffers (kernel/quantity.cu:94-97): centred fields and
+ *     u_phi have nTheta rows, u_theta has nTheta-1 rows.
+ *   - Each handle owns its device memory and its CUDA stream.  Calls on
+ *     different handles may run from different threads; calls on one handle
+ *     must not overlap.
+ */
+#ifndef SOAPBUBBLE_GB300_H
+#define SOAPBUBBLE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SB_OK = 0,
+    SB_ERR_INVALID = 1,      /* bad argument or configuration */
+    SB_ERR_CUDA = 2,         /* CUDA runtime error */
+    SB_ERR_OOM = 3,          /* device allocation failed */
+    SB_ERR_NOT_CONVERGED = 4,/* implicit solve missed its tolerance */
+    SB_ERR_BROKEN = 5,       /* film broken (no thickness left) */
+    SB_ERR_IO = 6            /* file output failed */
+} sb_status;
+
+/* The 17 keys of the reference's config.txt (kernel/main.cu:20-36) plus
+ * solver and storage options.  Bubble::Bubble (kernel/bubble.cu:2568-2603)
+ * derives the nondimensional coefficients from these. */
+typedef struct {
+    double radius;        /* m */
+    double H;             /* mean half film thickness, m */
+    double U;             /* characteristic velocity; the reference forces 1 */
+    double c_m;           /* bulk concentration (unused by the step) */
+    double Gamma_m;       /* surface mean concentration, mol m^-2 */
+    double T;             /* temperature, K */
+    double Ds;            /* soap diffusivity (unused by the step) */
+    double rm;            /* Lennard-Jones distance (van der Waals is off) */
+    int nTheta;           /* numberOfGridsInTheta; nPhi = 2 nTheta, a power of two */
+    double dt;            /* timePerStep, s */
+    double DT;            /* timePerFrame, s */
+    int frames;           /* frameNumbers */
+    double blendCoeff;    /* BIMOCQ blend */
+    int device;           /* CUDA device ordinal */
+    /* extensions (zero selects the default) */
+    double gs_scale;      /* multiplies the nondimensional gravity (0 -> 1) */
+    double M_scale;       /* multiplies the Marangoni coefficient M (0 -> 1) */
+    int solver_mode;      /* 0: mixed precision (FP64 dots + refinement), 1: plain FP32 */
+    double solver_tol;    /* relative residual target (0 -> 1e-6) */
+    int solver_max_iter;  /* (0 -> 1000) */
+    int force_reinit;     /* 0: decide by distortion > 4; 1: never; 2: every step */
+} sb_params;
+
+/* Diagnostics of the most recent step (the reference prints these:
+ * kernel/solver.cu:282, kernel/bubble.cu:1495-1497, solver.cu:592). */
+typedef struct {
+    double distortion;        /* max BIMOCQ distortion, grid units */
+    int reinit;               /* maps re-initialised in the last step */
+    int solver_iters;
+    double solver_rel_resid;  /* ||b - A x|| / ||b|| of the returned gamma */
+    int solver_converged;
+    int broken_cells;         /* identity rows of the implicit system */
+    long long steps;          /* steps taken by this handle */
+    long long reinits;        /* re-initialisations so far */
+    double mass_eta;          /* sum eta sin(theta) (after sb_update_mass) */
+    double mass_gamma;        /* sum gamma sin(theta) */
+} sb_stats;
+
+typedef struct sb_bubble sb_bubble;
+
+/* Field selectors for sb_upload_field / sb_download_field. */
+typedef enum {
+    SB_ETA = 0, SB_GAMMA, SB_UTHETA, SB_UPHI,
+    SB_ETA_INIT, SB_ETA_DELTA, SB_ETA_INIT_LAST, SB_ETA_DELTA_LAST,
+    SB_GAMMA_INIT, SB_GAMMA_DELTA, SB_GAMMA_INIT_LAST, SB_GAMMA_DELTA_LAST,
+    SB_FWD_T, SB_FWD_P, SB_BWD_T, SB_BWD_P, SB_BWDPREV_T, SB_BWDPREV_P,
+    SB_UAIR_INIT, SB_VAIR_INIT, SB_UAIR, SB_VAIR,
+    SB_FIELD_COUNT
+} sb_field;
+
+/* Fill p with the reference's defaults (config.txt, include/bubble.cuh:78-84). */
+void sb_default_params(sb_params* p);
+
+/* Replaces Solver::Solver (kernel/solver.cu:63-160) and the constant upload of
+ * Bubble::run (kernel/bubble.cu:2609-2638): allocates every device buffer of
+ * one bubble, initialises eta = 0.5, gamma = 1, u = 0, identity maps
+ * (kernel/initializer.cu:22-50, solver.cu:102-106, 145-160). */
+int sb_create(const sb_params* p, sb_bubble** out);
+
+/* Replaces Solver::~Solver (kernel/solver.cu:163-215). */
+int sb_destroy(sb_bubble* b);
+
+/* Replaces initThicknessfromPic / initAirflowfromPic / initWithConst
+ * (kernel/initializer.cu:22-135): uploads the initial state from host FP64
+ * arrays in the reference layout.  Any pointer may be NULL (field kept).
+ * Resets the BIMOCQ buffers (init = initLast = field, delta = deltaLast = 0)
+ * and the characteristic maps to identity. */
+int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma,
+                     const double* u_theta, const double* u_phi,
+                     const double* uair_init, const double* vair_init);
+
+/* Replaces Quantity::copyToGPU for any single buffer (kernel/quantity.cu:3-11),
+ * including BIMOCQ buffers and maps (absolute grid coordinates theta/h,
+ * phi/h as the reference's forward_t/forward_p).  n = element count. */
+int sb_upload_field(sb_bubble* b, sb_field which, const double* src, size_t n);
+
+/* Replaces Quantity::copyBackToCPU / Solver::copyToCPU (kernel/quantity.cu:14-18,
+ * solver.cu:243-249) for any buffer; maps come back in absolute coordinates. */
+int sb_download_field(sb_bubble* b, sb_field which, double* dst, size_t n);
+
+/* Element count of a field. */
+size_t sb_field_size(const sb_bubble* b, sb_field which);
+
+/* Replaces Solver::stepForward(dt) (kernel/solver.cu:252-292) called
+ * n_steps times with currentTimeGlobal = t_frame (s) and the dimensional
+ * step dt (s) -- Bubble::run keeps t at the frame start for every step of a
+ * frame (kernel/bubble.cu:2661-2678).  Asynchronous on the handle's stream
+ * unless an error must be reported. */
+int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt);
+
+/* Wait for the handle's queued work; returns SB_ERR_NOT_CONVERGED if the
+ * last solve missed its tolerance. */
+int sb_synchronize(sb_bubble* b);
+
+/* Statistics of the last step (synchronises). */
+int sb_get_stats(sb_bubble* b, sb_stats* out);
+
+/* Computes the mass integrals into the stats (synchronises). */
+int sb_update_mass(sb_bubble* b);
+
+/* Replaces Solver::write_thickness_img (kernel/solver.cu:541-593): writes a
+ * 3-channel (B, G, R equal) HALF EXR of eta * H * 2e5 to path and sets
+ * *broken when no cell has eta > 0. */
+int sb_write_thickness_exr(sb_bubble* b, const char* path, int* broken);
+
+/* Replaces Bubble::run (kernel/bubble.cu:2607-2704): the frame loop with
+ * full steps, a fractional last step per frame, and frame%04d.exr output
+ * into out_dir (NULL: no output).  frames <= 0 uses p->frames. */
+int sb_run(sb_bubble* b, const char* out_dir, int frames);
+
+/* Device bytes held by one bubble of this configuration (for admission). */
+size_t sb_bytes_required(const sb_params* p);
+
+/* CUDA stream of the handle (cudaStream_t), for callers that order their
+ * own work after the step. */
+void* sb_stream(sb_bubble* b);
+
+/* Message for the last failing call on this thread. */
+const char* sb_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOAPBUBBLE_GB300_H */

@@ -1,0 +1,175 @@
+"""Python mirror of the reference's Bubble / Solver / Quantity surface.
+
+`GpuBubble` owns one sb_bubble handle (C ABI, include/soapbubble.h) and moves
+fields in the reference's host layout (row-major [theta][phi] float64,
+u_theta with nTheta-1 rows; maps as absolute grid coordinates).  `Bubble`
+keeps the reference constructor (include/bubble.cuh:78-84) and run()
+(kernel/bubble.cu:2607-2704).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import SbParams, SbStats, check, lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def default_params() -> SbParams:
+    p = SbParams()
+    lib().sb_default_params(C.byref(p))
+    return p
+
+
+def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
+                Gamma_m: float = 1e-6, T: float = 298.15, blendCoeff: float = 0.5,
+                DT: Optional[float] = None, frames: int = 1, solver_mode: int = 0,
+                solver_tol: float = 1e-6, solver_max_iter: int = 1000, force_reinit: int = 0,
+                gs_scale: float = 0.0, M_scale: float = 0.0, device: int = 0) -> SbParams:
+    p = default_params()
+    p.nTheta, p.dt, p.radius, p.H, p.Gamma_m, p.T = nTheta, dt, radius, H, Gamma_m, T
+    p.blendCoeff = blendCoeff
+    p.DT = DT if DT is not None else 10 * dt
+    p.frames = frames
+    p.solver_mode, p.solver_tol, p.solver_max_iter = solver_mode, solver_tol, solver_max_iter
+    p.force_reinit, p.gs_scale, p.M_scale, p.device = force_reinit, gs_scale, M_scale, device
+    return p
+
+
+class GpuBubble:
+    """One bubble resident on the GPU (Solver + Quantity of the reference)."""
+
+    def __init__(self, params: SbParams):
+        self.params = params
+        h = C.c_void_p()
+        check(lib().sb_create(C.byref(params), C.byref(h)), "sb_create")
+        self.h = h
+        self.nTheta = params.nTheta
+        self.nPhi = 2 * params.nTheta
+
+    def close(self) -> None:
+        if self.h:
+            lib().sb_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- fields -------------------------------------------------------------
+    def shape(self, name: str):
+        n = lib().sb_field_size(self.h, _lib.FIELD_ID[name])
+        if name in ("u_theta", "vair_init"):
+            return (self.nTheta - 1, self.nPhi)
+        if name in ("uair", "vair"):
+            return (n,)
+        return (self.nTheta, self.nPhi)
+
+    def upload_fields(self, eta=None, gamma=None, u_theta=None, u_phi=None,
+                      uair_init=None, vair_init=None) -> None:
+        arrs = []
+
+        def conv(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            arrs.append(a)
+            return _dp(a)
+
+        args = [conv(a) for a in (eta, gamma, u_theta, u_phi, uair_init, vair_init)]
+        check(lib().sb_upload_fields(self.h, *args), "sb_upload_fields")
+
+    def upload(self, name: str, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        check(lib().sb_upload_field(self.h, _lib.FIELD_ID[name], _dp(a), a.size), "sb_upload_field")
+
+    def download(self, name: str) -> np.ndarray:
+        n = lib().sb_field_size(self.h, _lib.FIELD_ID[name])
+        out = np.empty(n, dtype=np.float64)
+        check(lib().sb_download_field(self.h, _lib.FIELD_ID[name], _dp(out), n), "sb_download_field")
+        return out.reshape(self.shape(name))
+
+    # -- stepping -----------------------------------------------------------
+    def step(self, n: int = 1, t: float = 0.0, dt: Optional[float] = None) -> None:
+        check(lib().sb_step(self.h, n, t, self.params.dt if dt is None else dt), "sb_step")
+
+    def synchronize(self) -> None:
+        check(lib().sb_synchronize(self.h), "sb_synchronize")
+
+    def stats(self, mass: bool = False) -> SbStats:
+        if mass:
+            check(lib().sb_update_mass(self.h), "sb_update_mass")
+        s = SbStats()
+        check(lib().sb_get_stats(self.h, C.byref(s)), "sb_get_stats")
+        return s
+
+    def write_thickness_exr(self, path: str) -> bool:
+        broken = C.c_int(0)
+        check(lib().sb_write_thickness_exr(self.h, path.encode(), C.byref(broken)),
+              "sb_write_thickness_exr")
+        return bool(broken.value)
+
+    def run(self, out_dir: Optional[str], frames: int = 0) -> None:
+        check(lib().sb_run(self.h, out_dir.encode() if out_dir else None, frames), "sb_run")
+
+    def stream(self) -> int:
+        return lib().sb_stream(self.h)
+
+
+def bytes_required(params: SbParams) -> int:
+    return lib().sb_bytes_required(C.byref(params))
+
+
+class Bubble:
+    """The reference's Bubble(...) + run() (include/bubble.cuh:78-88)."""
+
+    def __init__(self, radius=0.05, H=0.0000005, U=1.0, c_m=0.5, Gamma_m=0.000001, T=298.15,
+                 Ds=0.01, rm=0.000000005, nTheta=128, dt=0.005, DT=1.0 / 24.0, frames=1000,
+                 outputDir="../output/test/", thicknessImage="", device=0, AMGconfig="",
+                 blendCoeff=0.5):
+        p = default_params()
+        p.radius, p.H, p.U, p.c_m, p.Gamma_m, p.T, p.Ds, p.rm = radius, H, U, c_m, Gamma_m, T, Ds, rm
+        p.nTheta, p.dt, p.DT, p.frames = int(nTheta), dt, DT, frames
+        p.device, p.blendCoeff = device, blendCoeff
+        self.outputDir = outputDir
+        self.thicknessImage = thicknessImage
+        self.AMGconfig = AMGconfig
+        self.gpu = GpuBubble(p)
+        if thicknessImage:
+            raise NotImplementedError("thickness images are not supported yet")
+
+    def run(self) -> None:
+        if self.outputDir:
+            os.makedirs(self.outputDir, exist_ok=True)
+        self.gpu.run(self.outputDir or None)
+
+
+def read_config(path: str) -> dict:
+    """The 17 positional "key value" pairs of config.txt (kernel/main.cu:20-36)."""
+    toks = open(path).read().split()
+    vals = toks[1::2]
+    if len(vals) < 17:
+        raise ValueError(f"{path}: expected 17 key/value pairs, found {len(vals)}")
+    names = ["radius", "H", "U", "c_m", "Gamma_m", "T", "Ds", "rm", "nTheta", "dt", "DT",
+             "frames", "outputDir", "thicknessImage", "AMGconfig", "blendCoeff", "device"]
+    conv = {"nTheta": int, "frames": int, "device": int, "outputDir": str,
+            "thicknessImage": str, "AMGconfig": str}
+    cfg = {n: conv.get(n, float)(v) for n, v in zip(names, vals)}
+    if cfg["thicknessImage"] == "null":
+        cfg["thicknessImage"] = ""
+    return cfg

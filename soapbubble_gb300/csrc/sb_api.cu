@@ -1,0 +1,657 @@
+// C ABI of the GB300 soap-bubble step: bubble lifetime, device memory,
+// host<->device field conversion, step orchestration, frame output.
+//
+// Device memory of one bubble is a single arena (cudaMalloc once, carved
+// into 256-byte aligned arrays), so admission control can budget a bubble
+// exactly (sb_bytes_required) and creation is one allocation.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/soapbubble.h"
+#include "sb_exr.h"
+#include "sb_internal.h"
+
+using namespace sb;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? SB_ERR_OOM : SB_ERR_CUDA;
+}
+
+#define SB_CHECK(call)                                      \
+    do {                                                    \
+        cudaError_t _e = (call);                            \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+    } while (0)
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kHalfPi = 1.57079632679489661923;
+// include/header.cuh:76-83, 93
+constexpr double kGasR = 8.3144598, kSigmaA = 0.07275, kRho = 1e3, kG = 9.8;
+constexpr double kRhoA = 1.184, kNuA = 1.562e-5, kEvaporation = -0.00000003;
+
+struct Layout {
+    size_t bytes = 0;
+    size_t take(size_t n) {
+        size_t off = bytes;
+        bytes += (n + 255) & ~size_t(255);
+        return off;
+    }
+};
+
+bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+}  // namespace
+
+struct sb_bubble {
+    sb_params params;
+    SbGrid g;
+    SbPhys ph;
+    SbFields f;
+    SolverConfig solver;
+    int force_reinit;  // -1 decide, 0 never, 1 always
+    int device;
+    cudaStream_t stream = nullptr;
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    float* tables = nullptr;
+    int cur = 0;  // map ping-pong
+    long long steps = 0;
+    double last_dt = -1, last_t = -1e300;
+    SbStepParams* h_step = nullptr;  // pinned
+};
+
+namespace {
+
+// Nondimensional coefficients as Bubble::Bubble (kernel/bubble.cu:2568-2603)
+// and the constant upload of Bubble::run (2609-2638).
+void derive_phys(const sb_params& p, SbPhys& ph) {
+    const double U = 1.0;  // Bubble::Bubble forces U = 1
+    const double sigma_r = kGasR * p.T;
+    double M = p.Gamma_m * sigma_r / (3 * kRho * p.H * U * U);
+    double gs = kG * p.radius / (U * U);
+    if (p.M_scale > 0) M *= p.M_scale;
+    if (p.gs_scale > 0) gs *= p.gs_scale;
+    ph.M = (float)M;
+    ph.Cr = (float)(kRhoA * std::sqrt(kNuA * p.radius / U) / (kRho * p.H));
+    ph.gs = (float)gs;
+    ph.gmax = (float)(kSigmaA / sigma_r / p.Gamma_m);
+    ph.blend = (float)p.blendCoeff;
+    ph.evap = (float)(kEvaporation * p.radius / (p.H * U));
+}
+
+// Spatial factor of the air-flow corridor (airFlowU/V, kernel/bubble.cu:
+// 2301-2380) at one face; the time factor 3 - |t - 3| is applied per step.
+double corridor(double radius, double gTheta, double gPhi, bool phiComponent) {
+    const double sT = std::sin(gTheta), cT = std::cos(gTheta);
+    const double sP = std::sin(gPhi), cP = std::cos(gPhi);
+    const double angle = kPi / 2.;
+    double wind[3] = {0., std::cos(angle), std::sin(angle)};
+    double wl = 1.0 / std::sqrt(wind[0] * wind[0] + wind[1] * wind[1] + wind[2] * wind[2]);
+    for (double& v : wind) v *= wl;
+    const double pos[3] = {1., 0., 0.};
+    double nrm[3] = {pos[1] * wind[2] - pos[2] * wind[1], pos[2] * wind[0] - pos[0] * wind[2],
+                     pos[0] * wind[1] - pos[1] * wind[0]};
+    double nl = 1.0 / std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+    for (double& v : nrm) v *= nl;
+    const double cur[3] = {sT * cP, sT * sP, cT};
+    const double dn = nrm[0] * cur[0] + nrm[1] * cur[1] + nrm[2] * cur[2];
+    const double beta = std::acos(std::fmax(-1.0, std::fmin(1.0, dn)));
+    double prj[3] = {cur[0] - dn * nrm[0], cur[1] - dn * nrm[1], cur[2] - dn * nrm[2]};
+    double pl = 1.0 / std::sqrt(prj[0] * prj[0] + prj[1] * prj[1] + prj[2] * prj[2]);
+    for (double& v : prj) v *= pl;
+    const double pw[3] = {nrm[1] * prj[2] - nrm[2] * prj[1], nrm[2] * prj[0] - nrm[0] * prj[2],
+                          nrm[0] * prj[1] - nrm[1] * prj[0]};
+    double x = (std::fabs(beta - kHalfPi) - 0.2) / (0.4 - 0.2);
+    x = std::fmax(0.0, std::fmin(1.0, x));
+    const double ss = x * x * (3.0 - 2.0 * x);
+    const double s = 0.5 * std::sin(beta) / 1.0 * radius * (1. - ss);
+    if (phiComponent) return s * (pw[0] * -sP + pw[1] * cP);
+    return s * (pw[0] * cT * cP + pw[1] * cT * sP - pw[2] * sT);
+}
+
+struct ArenaPlan {
+    Layout L;
+    size_t tables, eta, gam, uth, uph, eta_adv, gam_adv, uth_adv, uph_adv;
+    size_t bim[8];
+    size_t fwd[2], bwd[2], bwdprev;
+    size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
+    size_t div, d_eta, d_gam, err_eta, err_gam;
+    size_t diag, cE, cS, rhs, x, r, z, p, q, x64, partials, step, stats;
+};
+
+ArenaPlan plan_arena(const SbGrid& g, int partials) {
+    ArenaPlan a;
+    const size_t N = (size_t)g.N, Nv = (size_t)g.Nv, F = sizeof(float);
+    a.tables = a.L.take((size_t)(4 * g.nT + 2) * F);
+    a.eta = a.L.take(N * F); a.gam = a.L.take(N * F);
+    a.uth = a.L.take(Nv * F); a.uph = a.L.take(N * F);
+    a.eta_adv = a.L.take(N * F); a.gam_adv = a.L.take(N * F);
+    a.uth_adv = a.L.take(Nv * F); a.uph_adv = a.L.take(N * F);
+    for (size_t& b : a.bim) b = a.L.take(N * F);
+    for (int k = 0; k < 2; ++k) { a.fwd[k] = a.L.take(N * 8); a.bwd[k] = a.L.take(N * 8); }
+    a.bwdprev = a.L.take(N * 8);
+    a.uair_init = a.L.take(N * F); a.vair_init = a.L.take(Nv * F);
+    a.corr_u = a.L.take(N * F); a.corr_v = a.L.take(Nv * F);
+    a.uair = a.L.take((N + 1) * F); a.vair = a.L.take((Nv + 1) * F);
+    a.div = a.L.take(N * F); a.d_eta = a.L.take(N * F); a.d_gam = a.L.take(N * F);
+    a.err_eta = a.L.take(N * F); a.err_gam = a.L.take(N * F);
+    a.diag = a.L.take(N * F); a.cE = a.L.take(N * F); a.cS = a.L.take(N * F);
+    a.rhs = a.L.take(N * F); a.x = a.L.take(N * F); a.r = a.L.take(N * F);
+    a.z = a.L.take(N * F); a.p = a.L.take(N * F); a.q = a.L.take(N * F);
+    a.x64 = a.L.take(N * 8);
+    a.partials = a.L.take((size_t)partials * 8);
+    a.step = a.L.take(sizeof(SbStepParams));
+    a.stats = a.L.take(sizeof(SbDevStats) + 64);
+    return a;
+}
+
+int validate(const sb_params* p) {
+    if (!p) return fail(SB_ERR_INVALID, "null params");
+    if (!is_pow2(p->nTheta) || p->nTheta < 8 || p->nTheta > 8192)
+        return fail(SB_ERR_INVALID, "nTheta must be a power of two in [8, 8192]");
+    if (!(p->radius > 0) || !(p->H > 0) || !(p->Gamma_m > 0) || !(p->T > 0))
+        return fail(SB_ERR_INVALID, "radius, H, Gamma_m and T must be positive");
+    if (!(p->dt > 0)) return fail(SB_ERR_INVALID, "timePerStep must be positive");
+    return SB_OK;
+}
+
+float* fptr(sb_bubble* b, sb_field w) {
+    SbFields& f = b->f;
+    switch (w) {
+        case SB_ETA: return f.eta;
+        case SB_GAMMA: return f.gam;
+        case SB_UTHETA: return f.uth;
+        case SB_UPHI: return f.uph;
+        case SB_ETA_INIT: return f.eta_init;
+        case SB_ETA_DELTA: return f.eta_delta;
+        case SB_ETA_INIT_LAST: return f.eta_initL;
+        case SB_ETA_DELTA_LAST: return f.eta_deltaL;
+        case SB_GAMMA_INIT: return f.gam_init;
+        case SB_GAMMA_DELTA: return f.gam_delta;
+        case SB_GAMMA_INIT_LAST: return f.gam_initL;
+        case SB_GAMMA_DELTA_LAST: return f.gam_deltaL;
+        case SB_UAIR_INIT: return f.uair_init;
+        case SB_VAIR_INIT: return f.vair_init;
+        case SB_UAIR: return f.uair;
+        case SB_VAIR: return f.vair;
+        default: return nullptr;
+    }
+}
+
+float2* map_ptr(sb_bubble* b, sb_field w, int& comp) {
+    comp = (w == SB_FWD_P || w == SB_BWD_P || w == SB_BWDPREV_P) ? 1 : 0;
+    switch (w) {
+        case SB_FWD_T: case SB_FWD_P: return b->f.fwd[b->cur];
+        case SB_BWD_T: case SB_BWD_P: return b->f.bwd[b->cur];
+        case SB_BWDPREV_T: case SB_BWDPREV_P: return b->f.bwdprev;
+        default: return nullptr;
+    }
+}
+
+int set_step_params(sb_bubble* b, double t, double dt_s) {
+    if (dt_s == b->last_dt && t == b->last_t) return SB_OK;
+    const double dtn = dt_s * 1.0 / b->params.radius;  // dt U / r with U = 1
+    SbStepParams* s = b->h_step;
+    SB_CHECK(cudaStreamSynchronize(b->stream));  // the pinned slot may be in flight
+    s->dt = (float)dtn;
+    s->invDt = (float)(1.0 / dtn);
+    s->windg = (float)(3.0 - std::fabs(t - 3.0));
+    s->mixA = (float)(t / 12.0);
+    s->mixB = (float)(1.0 - t / 12.0);
+    s->evapDt = (float)((double)b->ph.evap * dtn);
+    s->gsdt = 0.f;
+    s->pad = 0.f;
+    SB_CHECK(cudaMemcpyAsync(b->f.step, s, sizeof(SbStepParams), cudaMemcpyHostToDevice, b->stream));
+    b->last_dt = dt_s;
+    b->last_t = t;
+    return SB_OK;
+}
+
+int reset_bimocq(sb_bubble* b) {
+    const size_t N = (size_t)b->g.N * sizeof(float);
+    SbFields& f = b->f;
+    SB_CHECK(cudaMemcpyAsync(f.eta_init, f.eta, N, cudaMemcpyDeviceToDevice, b->stream));
+    SB_CHECK(cudaMemcpyAsync(f.eta_initL, f.eta, N, cudaMemcpyDeviceToDevice, b->stream));
+    SB_CHECK(cudaMemcpyAsync(f.gam_init, f.gam, N, cudaMemcpyDeviceToDevice, b->stream));
+    SB_CHECK(cudaMemcpyAsync(f.gam_initL, f.gam, N, cudaMemcpyDeviceToDevice, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.eta_delta, 0, N, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.eta_deltaL, 0, N, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.gam_delta, 0, N, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.gam_deltaL, 0, N, b->stream));
+    SB_CHECK(launch_reset_maps(b->g, b->f, b->stream));
+    return SB_OK;
+}
+
+int upload_f32(sb_bubble* b, float* dst, const double* src, size_t n) {
+    std::vector<float> tmp(n);
+    for (size_t i = 0; i < n; ++i) tmp[i] = (float)src[i];
+    SB_CHECK(cudaMemcpyAsync(dst, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    return SB_OK;
+}
+
+int fill_const(sb_bubble* b, float* dst, size_t n, float v) {
+    std::vector<float> tmp(n, v);
+    SB_CHECK(cudaMemcpyAsync(dst, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    return SB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sb_default_params(sb_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->radius = 0.05;
+    p->H = 0.000001;
+    p->U = 1.0;
+    p->c_m = 0.5;
+    p->Gamma_m = 0.000001;
+    p->T = 298.15;
+    p->Ds = 0.0;
+    p->rm = 0.000000005;
+    p->nTheta = 256;
+    p->dt = 0.005;
+    p->DT = 0.02;
+    p->frames = 500;
+    p->blendCoeff = 0.5;
+    p->device = 0;
+}
+
+size_t sb_bytes_required(const sb_params* p) {
+    if (validate(p) != SB_OK) return 0;
+    SbGrid g{};
+    g.nT = p->nTheta;
+    g.nP = 2 * p->nTheta;
+    g.N = g.nT * g.nP;
+    g.Nv = (g.nT - 1) * g.nP;
+    // partial slots: bounded by 6 per block of the cooperative solve
+    const int partials = 6 * ((g.N + 255) / 256);
+    return plan_arena(g, partials).L.bytes;
+}
+
+int sb_create(const sb_params* p, sb_bubble** out) {
+    if (!out) return fail(SB_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    int rc = validate(p);
+    if (rc != SB_OK) return rc;
+    SB_CHECK(cudaSetDevice(p->device));
+    sb_bubble* b = new sb_bubble();
+    b->params = *p;
+    b->device = p->device;
+    SbGrid& g = b->g;
+    g.nT = p->nTheta;
+    g.nP = 2 * p->nTheta;
+    g.maskP = g.nP - 1;
+    g.logP = 0;
+    while ((1 << g.logP) < g.nP) ++g.logP;
+    g.N = g.nT * g.nP;
+    g.Nv = (g.nT - 1) * g.nP;
+    g.h = (float)(kPi / g.nT);
+    g.invh = (float)(g.nT / kPi);
+    derive_phys(*p, b->ph);
+    b->solver.mode = p->solver_mode == 1 ? 0 : 1;
+    b->solver.tol = p->solver_tol > 0 ? p->solver_tol : 1e-6;
+    b->solver.max_iter = p->solver_max_iter > 0 ? p->solver_max_iter : 1000;
+    b->solver.precond = 0;
+    b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
+
+    const int partials = 6 * ((g.N + 255) / 256);
+    ArenaPlan a = plan_arena(g, partials);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->arena, a.L.bytes);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_step, sizeof(SbStepParams));
+    if (e != cudaSuccess) {
+        int r = cuda_fail(e, "sb_create allocation");
+        sb_destroy(b);
+        return r;
+    }
+    b->arena_bytes = a.L.bytes;
+    e = cudaMemset(b->arena, 0, a.L.bytes);
+    if (e != cudaSuccess) { int r = cuda_fail(e, "memset"); sb_destroy(b); return r; }
+    char* A = b->arena;
+    auto F32 = [&](size_t off) { return (float*)(A + off); };
+    SbFields& f = b->f;
+    b->tables = F32(a.tables);
+    f.eta = F32(a.eta); f.gam = F32(a.gam); f.uth = F32(a.uth); f.uph = F32(a.uph);
+    f.eta_adv = F32(a.eta_adv); f.gam_adv = F32(a.gam_adv);
+    f.uth_adv = F32(a.uth_adv); f.uph_adv = F32(a.uph_adv);
+    f.eta_init = F32(a.bim[0]); f.eta_delta = F32(a.bim[1]);
+    f.eta_initL = F32(a.bim[2]); f.eta_deltaL = F32(a.bim[3]);
+    f.gam_init = F32(a.bim[4]); f.gam_delta = F32(a.bim[5]);
+    f.gam_initL = F32(a.bim[6]); f.gam_deltaL = F32(a.bim[7]);
+    for (int k = 0; k < 2; ++k) {
+        f.fwd[k] = (float2*)(A + a.fwd[k]);
+        f.bwd[k] = (float2*)(A + a.bwd[k]);
+    }
+    f.bwdprev = (float2*)(A + a.bwdprev);
+    f.uair_init = F32(a.uair_init); f.vair_init = F32(a.vair_init);
+    f.corr_u = F32(a.corr_u); f.corr_v = F32(a.corr_v);
+    f.uair = F32(a.uair); f.vair = F32(a.vair);
+    f.div = F32(a.div); f.d_eta = F32(a.d_eta); f.d_gam = F32(a.d_gam);
+    f.err_eta = F32(a.err_eta); f.err_gam = F32(a.err_gam);
+    f.diag = F32(a.diag); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs);
+    f.x = F32(a.x); f.r = F32(a.r); f.z = F32(a.z); f.p = F32(a.p); f.q = F32(a.q);
+    f.x64 = (double*)(A + a.x64);
+    f.partials = (double*)(A + a.partials);
+    f.step = (SbStepParams*)(A + a.step);
+    f.stats = (SbDevStats*)(A + a.stats);
+    if (6 * 0 + solver_partials_needed(g) > partials) {
+        sb_destroy(b);
+        return fail(SB_ERR_INVALID, "solver partial buffer too small");
+    }
+
+    // trigonometric tables in FP64, stored FP32
+    std::vector<float> tab(4 * g.nT + 2);
+    float* sin_c = tab.data();
+    float* cos_c = sin_c + g.nT;
+    float* sin_e = cos_c + g.nT;
+    float* cos_e = sin_e + g.nT + 1;
+    const double h = kPi / g.nT;
+    for (int i = 0; i < g.nT; ++i) {
+        sin_c[i] = (float)std::sin((i + 0.5) * h);
+        cos_c[i] = (float)std::cos((i + 0.5) * h);
+    }
+    for (int i = 0; i <= g.nT; ++i) {
+        sin_e[i] = (float)std::sin(i * h);
+        cos_e[i] = (float)std::cos(i * h);
+    }
+    sin_e[0] = 0.0f;
+    sin_e[g.nT] = 0.0f;  // sin(0) and sin(pi): the pole couplings vanish
+    cos_e[0] = 1.0f;
+    cos_e[g.nT] = -1.0f;
+    g.sin_c = b->tables;
+    g.cos_c = b->tables + g.nT;
+    g.sin_e = b->tables + 2 * g.nT;
+    g.cos_e = b->tables + 3 * g.nT + 1;
+    e = cudaMemcpy(b->tables, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { int r = cuda_fail(e, "tables"); sb_destroy(b); return r; }
+
+    // static corridor factors
+    {
+        std::vector<float> cu((size_t)g.N), cv((size_t)g.Nv);
+        for (int i = 0; i < g.nT; ++i)
+            for (int j = 0; j < g.nP; ++j) {
+                double v = corridor(p->radius, (i + 0.5) * h, (j - 0.5) * h, true);
+                cu[(size_t)i * g.nP + j] = (float)v;
+                if (i < g.nT - 1) {
+                    double w = corridor(p->radius, (i + 1.0) * h, j * h, false);
+                    cv[(size_t)i * g.nP + j] = (float)w;
+                }
+            }
+        e = cudaMemcpy(f.corr_u, cu.data(), cu.size() * 4, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(f.corr_v, cv.data(), cv.size() * 4, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { int r = cuda_fail(e, "corridor"); sb_destroy(b); return r; }
+    }
+    // Solver::Solver initial state: eta = 0.5, gamma = 1, u = 0, no wind
+    rc = fill_const(b, f.eta, (size_t)g.N, 0.5f);
+    if (rc == SB_OK) rc = fill_const(b, f.gam, (size_t)g.N, 1.0f);
+    if (rc == SB_OK) rc = reset_bimocq(b);
+    if (rc == SB_OK) {
+        SbDevStats st{};
+        st.force_reinit = b->force_reinit;
+        e = cudaMemcpy(f.stats, &st, sizeof(st), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_fail(e, "stats");
+    }
+    if (rc == SB_OK) rc = set_step_params(b, 0.0, p->dt);
+    if (rc == SB_OK) {
+        e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "sb_create sync");
+    }
+    if (rc != SB_OK) {
+        sb_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return SB_OK;
+}
+
+int sb_destroy(sb_bubble* b) {
+    if (!b) return SB_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->arena) cudaFree(b->arena);
+    if (b->h_step) cudaFreeHost(b->h_step);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return SB_OK;
+}
+
+size_t sb_field_size(const sb_bubble* b, sb_field which) {
+    if (!b) return 0;
+    if (which == SB_UTHETA || which == SB_VAIR_INIT) return (size_t)b->g.Nv;
+    if (which == SB_UAIR) return (size_t)b->g.N + 1;
+    if (which == SB_VAIR) return (size_t)b->g.Nv + 1;
+    if (which < 0 || which >= SB_FIELD_COUNT) return 0;
+    return (size_t)b->g.N;
+}
+
+int sb_upload_field(sb_bubble* b, sb_field which, const double* src, size_t n) {
+    if (!b || !src) return fail(SB_ERR_INVALID, "null argument");
+    if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
+    SB_CHECK(cudaSetDevice(b->device));
+    int comp = 0;
+    float2* m = map_ptr(b, which, comp);
+    if (m) {
+        // absolute grid coordinates -> offsets from the cell centre
+        const int nT = b->g.nT, nP = b->g.nP;
+        std::vector<float2> tmp((size_t)b->g.N);
+        SB_CHECK(cudaMemcpyAsync(tmp.data(), m, tmp.size() * sizeof(float2), cudaMemcpyDeviceToHost,
+                                 b->stream));
+        SB_CHECK(cudaStreamSynchronize(b->stream));
+        for (int i = 0; i < nT; ++i)
+            for (int j = 0; j < nP; ++j) {
+                const size_t c = (size_t)i * nP + j;
+                if (comp == 0) {
+                    tmp[c].x = (float)(src[c] - (i + 0.5));
+                } else {
+                    double d = std::fmod(src[c] - j, (double)nP);
+                    if (d >= nT) d -= nP;
+                    if (d < -nT) d += nP;
+                    tmp[c].y = (float)d;
+                }
+            }
+        SB_CHECK(cudaMemcpyAsync(m, tmp.data(), tmp.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                                 b->stream));
+        SB_CHECK(cudaStreamSynchronize(b->stream));
+        return SB_OK;
+    }
+    float* d = fptr(b, which);
+    if (!d) return fail(SB_ERR_INVALID, "unknown field");
+    return upload_f32(b, d, src, n);
+}
+
+int sb_download_field(sb_bubble* b, sb_field which, double* dst, size_t n) {
+    if (!b || !dst) return fail(SB_ERR_INVALID, "null argument");
+    if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
+    SB_CHECK(cudaSetDevice(b->device));
+    int comp = 0;
+    float2* m = map_ptr(b, which, comp);
+    if (m) {
+        const int nT = b->g.nT, nP = b->g.nP;
+        std::vector<float2> tmp((size_t)b->g.N);
+        SB_CHECK(cudaMemcpyAsync(tmp.data(), m, tmp.size() * sizeof(float2), cudaMemcpyDeviceToHost,
+                                 b->stream));
+        SB_CHECK(cudaStreamSynchronize(b->stream));
+        for (int i = 0; i < nT; ++i)
+            for (int j = 0; j < nP; ++j) {
+                const size_t c = (size_t)i * nP + j;
+                if (comp == 0) {
+                    dst[c] = (i + 0.5) + (double)tmp[c].x;
+                } else {
+                    double v = std::fmod(j + (double)tmp[c].y + nP, (double)nP);
+                    dst[c] = v;
+                }
+            }
+        return SB_OK;
+    }
+    float* d = fptr(b, which);
+    if (!d) return fail(SB_ERR_INVALID, "unknown field");
+    std::vector<float> tmp(n);
+    SB_CHECK(cudaMemcpyAsync(tmp.data(), d, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i];
+    return SB_OK;
+}
+
+int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma, const double* u_theta,
+                     const double* u_phi, const double* uair_init, const double* vair_init) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    SB_CHECK(cudaSetDevice(b->device));
+    const size_t N = (size_t)b->g.N, Nv = (size_t)b->g.Nv;
+    int rc = SB_OK;
+    if (eta && rc == SB_OK) rc = upload_f32(b, b->f.eta, eta, N);
+    if (gamma && rc == SB_OK) rc = upload_f32(b, b->f.gam, gamma, N);
+    if (u_theta && rc == SB_OK) rc = upload_f32(b, b->f.uth, u_theta, Nv);
+    if (u_phi && rc == SB_OK) rc = upload_f32(b, b->f.uph, u_phi, N);
+    if (uair_init && rc == SB_OK) rc = upload_f32(b, b->f.uair_init, uair_init, N);
+    if (vair_init && rc == SB_OK) rc = upload_f32(b, b->f.vair_init, vair_init, Nv);
+    if (rc == SB_OK) rc = reset_bimocq(b);
+    if (rc == SB_OK) {
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "upload sync");
+    }
+    return rc;
+}
+
+int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
+    SB_CHECK(cudaSetDevice(b->device));
+    int rc = set_step_params(b, t_frame, dt);
+    if (rc != SB_OK) return rc;
+    for (int s = 0; s < n_steps; ++s) {
+        SB_CHECK(launch_advect(b->g, b->ph, b->f, b->cur, b->stream));
+        SB_CHECK(launch_assemble(b->g, b->ph, b->f, b->stream));
+        SB_CHECK(launch_solve(b->g, b->ph, b->f, b->solver, b->stream));
+        SB_CHECK(launch_post(b->g, b->ph, b->f, b->cur, b->stream));
+        SB_CHECK(launch_reinit(b->g, b->ph, b->f, b->cur, b->stream));
+        b->cur ^= 1;
+        b->steps++;
+    }
+    return SB_OK;
+}
+
+int sb_synchronize(sb_bubble* b) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    SB_CHECK(cudaSetDevice(b->device));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    return SB_OK;
+}
+
+int sb_get_stats(sb_bubble* b, sb_stats* out) {
+    if (!b || !out) return fail(SB_ERR_INVALID, "null argument");
+    SB_CHECK(cudaSetDevice(b->device));
+    SbDevStats st;
+    SB_CHECK(cudaMemcpyAsync(&st, b->f.stats, sizeof(st), cudaMemcpyDeviceToHost, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    std::memset(out, 0, sizeof(*out));
+    float d;
+    std::memcpy(&d, &st.distortion_bits, 4);
+    out->distortion = d;
+    out->reinit = st.reinit;
+    out->solver_iters = st.solver_iters;
+    out->solver_rel_resid = st.solver_rel_resid;
+    out->solver_converged = st.solver_converged;
+    out->broken_cells = st.broken_cells;
+    out->steps = b->steps;
+    out->reinits = st.reinit_total;
+    out->mass_eta = st.mass_eta;
+    out->mass_gamma = st.mass_gamma;
+    return SB_OK;
+}
+
+int sb_update_mass(sb_bubble* b) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    SB_CHECK(cudaSetDevice(b->device));
+    SB_CHECK(launch_mass(b->g, b->f, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    return SB_OK;
+}
+
+int sb_write_thickness_exr(sb_bubble* b, const char* path, int* broken) {
+    if (!b || !path) return fail(SB_ERR_INVALID, "null argument");
+    SB_CHECK(cudaSetDevice(b->device));
+    const size_t N = (size_t)b->g.N;
+    std::vector<float> eta(N);
+    SB_CHECK(cudaMemcpyAsync(eta.data(), b->f.eta, N * 4, cudaMemcpyDeviceToHost, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    // Solver::write_thickness_img (kernel/solver.cu:541-593)
+    const double ratio = 2e5;
+    bool br = true;
+    std::vector<float> img(N);
+    for (size_t c = 0; c < N; ++c) {
+        const double D = eta[c];
+        if (D > 0) br = false;
+        img[c] = (float)(D * b->params.H * ratio);
+    }
+    if (broken) *broken = br ? 1 : 0;
+    if (!write_exr_gray3(path, b->g.nP, b->g.nT, img.data()))
+        return fail(SB_ERR_IO, std::string("cannot write ") + path);
+    return SB_OK;
+}
+
+int sb_run(sb_bubble* b, const char* out_dir, int frames) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    const sb_params& p = b->params;
+    if (frames <= 0) frames = p.frames;
+    std::string dir = out_dir ? out_dir : "";
+    if (!dir.empty() && dir.back() != '/') dir.push_back('/');
+    auto frame_path = [&](int i) {
+        char name[32];
+        std::snprintf(name, sizeof(name), "frame%04d.exr", i);
+        return dir + name;
+    };
+    int broken = 0, rc = SB_OK;
+    if (out_dir) {
+        rc = sb_write_thickness_exr(b, frame_path(0).c_str(), &broken);
+        if (rc != SB_OK) return rc;
+    }
+    // Bubble::run frame loop (kernel/bubble.cu:2656-2696); U = 1
+    const double dt_ = p.dt, DT = p.DT;
+    double T = 0.0;
+    for (int i = 1; i < frames && !broken; ++i) {
+        const double tf = T;
+        int n = 0;
+        while ((T + dt_) <= i * DT) {
+            ++n;
+            T += dt_;
+        }
+        if (n > 0 && (rc = sb_step(b, n, tf, dt_)) != SB_OK) return rc;
+        if ((T + 1e-7) < i * DT) {
+            if ((rc = sb_step(b, 1, tf, i * DT - T)) != SB_OK) return rc;
+        }
+        sb_stats st;
+        if ((rc = sb_get_stats(b, &st)) != SB_OK) return rc;
+        if (!st.solver_converged) return fail(SB_ERR_NOT_CONVERGED, "implicit solve did not converge");
+        T = i * DT;
+        if (out_dir) {
+            rc = sb_write_thickness_exr(b, frame_path(i).c_str(), &broken);
+            if (rc != SB_OK) return rc;
+        }
+    }
+    if (broken) return fail(SB_ERR_BROKEN, "film is broken");
+    return SB_OK;
+}
+
+void* sb_stream(sb_bubble* b) { return b ? (void*)b->stream : nullptr; }
+
+const char* sb_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,405 @@
+// Device-side geometry of the lat-long MAC grid: samplers with pole
+// reflection, great-circle backtrace, and characteristic-map interpolation.
+//
+// Positions are kept relative to the thread's own grid point so that FP32
+// keeps ~1e-7 cell precision at every grid size:
+//   * a position is an integer base (bi, bj) plus float offsets (ox, oy) in
+//     grid units, raw coordinates theta/h = bi + ox and phi/h = bj + oy;
+//   * geometry is done in a local Cartesian frame rotated about z so that the
+//     base point sits at azimuth 0: C = (sin t0, 0, cos t0), e_theta =
+//     (cos t0, 0, -sin t0), e_phi = (0, 1, 0); nearby points are carried as
+//     displacements d = P - C, converted to and from grid offsets with
+//     half-angle formulas that never subtract two O(1) quantities;
+//   * characteristic maps store, per cell, the offset (in grid units) of the
+//     mapped point from the cell centre.
+// The arithmetic is the reference's (kernel/bubble.cu:116-606): geometric
+// pole reflection with vector sign flips, NaN-skipping bilinear lerp,
+// great-circle RK2 trace with parallel transport, spherical lerp of map
+// points.  Only the representation of positions differs.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "sb_types.h"
+
+namespace sb {
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float len3(f3 a) { return sqrtf(dot3(a, a)); }
+
+// Local frame at a base grid point: raw coordinates (bi + fi, bj + fj),
+// fi, fj in {0, 0.5, -0.5}; s0/c0 = sin/cos of its polar angle.
+struct Frame {
+    int bi, bj;
+    float fi, fj;
+    float s0, c0;
+};
+
+// A sample position: raw theta/h = bi + ox, raw phi/h = bj + oy.
+struct Pos {
+    int bi, bj;
+    float ox, oy;
+};
+
+// sin(x)/x, accurate to float rounding for all |x|.
+__device__ __forceinline__ float sincf_(float x) {
+    float x2 = x * x;
+    if (x2 < 1e-6f) return 1.0f - x2 * (1.0f / 6.0f);
+    return sinf(x) / x;
+}
+
+// NaN-skipping lerp (kernel/bubble.cu:153-160).
+__device__ __forceinline__ float blerp(float from, float to, float a) {
+    if (isnan(from)) return to;
+    if (isnan(to)) return from;
+    return (1.0f - a) * from + a * to;
+}
+
+// Displacement P - C, in the frame, of the point at grid offsets (dth, dph)
+// from the frame's base.
+__device__ __forceinline__ f3 disp_from_offsets(const Frame& F, float dth, float dph, float h) {
+    float sh, chh;
+    sincosf(0.5f * dth * h, &sh, &chh);
+    const float sm = F.s0 * chh + F.c0 * sh;  // sin(t0 + dt/2)
+    const float cm = F.c0 * chh - F.s0 * sh;  // cos(t0 + dt/2)
+    const float dS = 2.0f * cm * sh;          // sin t1 - sin t0
+    const float dC = -2.0f * sm * sh;         // cos t1 - cos t0
+    const float s1 = F.s0 + dS;
+    float sp, cp;
+    sincosf(0.5f * dph * h, &sp, &cp);
+    const float sinD = 2.0f * sp * cp;
+    const float cosDm1 = -2.0f * sp * sp;
+    return {dS + s1 * cosDm1, s1 * sinD, dC};
+}
+
+// Grid position of the point C + d.  Points past a pole come back with the
+// base column shifted by nTheta (azimuth + pi) so the float offset stays small.
+__device__ __forceinline__ Pos pos_from_disp(const Frame& F, f3 d, float invh, int nT) {
+    const float Px = F.s0 + d.x, Py = d.y, Pz = F.c0 + d.z;
+    const float rho = sqrtf(Px * Px + Py * Py);
+    const float den = rho + F.s0;
+    const float rms0 = den > 0.0f ? (2.0f * F.s0 * d.x + d.x * d.x + d.y * d.y) / den : 0.0f;
+    const float sdt = rms0 * F.c0 - d.z * F.s0;   // sin(t1 - t0) scaled by |P|
+    const float cdt = rho * F.s0 + Pz * F.c0;     // cos(t1 - t0) scaled by |P|
+    Pos q;
+    q.bi = F.bi;
+    q.ox = F.fi + atan2f(sdt, cdt) * invh;
+    if (Px >= 0.0f) {
+        q.bj = F.bj;
+        q.oy = F.fj + atan2f(Py, Px) * invh;
+    } else {
+        q.bj = F.bj + nT;
+        q.oy = F.fj + atan2f(-Py, -Px) * invh;
+    }
+    return q;
+}
+
+// Great-circle angle (grid units) between the frame's base and C + d.
+__device__ __forceinline__ float dist_from_disp(f3 d, float invh) {
+    const float ch = len3(d);
+    return 2.0f * asinf(fminf(0.5f * ch, 1.0f)) * invh;
+}
+
+// Spherical lerp between C + dA and C + dB, returned as a displacement.
+// Same great-circle interpolation as lerpCoords (kernel/bubble.cu:512-536):
+// slerp(A, B, a) = sin((1-a)W)/sin W A + sin(aW)/sin W B, written so that
+// nearby points keep full precision.
+__device__ __forceinline__ f3 slerp_disp(const Frame& F, f3 dA, f3 dB, float a) {
+    const f3 e = dB - dA;
+    const float ch = len3(e);
+    const float W = 2.0f * asinf(fminf(0.5f * ch, 1.0f));
+    const float b = 1.0f - a;
+    const float sW = sincf_(W);
+    const float cA = b * sincf_(b * W) / sW;
+    const float cB = a * sincf_(a * W) / sW;
+    const float k = 0.5f * a * b * W * W * sincf_(0.5f * b * W) * sincf_(0.5f * a * W) /
+                    cosf(0.5f * W);  // cA + cB - 1
+    const f3 C = {F.s0, 0.0f, F.c0};
+    return cA * dA + cB * dB + k * C;
+}
+
+// ---------------------------------------------------------------------------
+// Stencils
+// ---------------------------------------------------------------------------
+
+// Geometric unfolding of a raw position across the poles (validateCoord,
+// kernel/bubble.cu:116-137, in raw coordinates).  Returns true when flipped.
+__device__ __forceinline__ bool unfold(int nT, int& bi, float& ox, int& bj) {
+    if ((float)bi + ox < 0.0f) {
+        bi = -bi;
+        ox = -ox;
+        bj += nT;
+        return true;
+    }
+    if ((float)(bi - nT) + ox > 0.0f) {
+        bi = 2 * nT - bi;
+        ox = -ox;
+        bj += nT;
+        return true;
+    }
+    return false;
+}
+
+// Row and column stencil of a cell-centred grid (rows at raw theta i + 0.5,
+// columns at raw phi j).  Rows -1 and nT are the across-pole reflections of
+// rows 0 and nT-1 (azimuth + pi); `neg` marks them for vector fields.
+struct CStencil {
+    int r0, r1;        // physical rows
+    int c00, c01;      // columns of the lower row
+    int c10, c11;      // columns of the upper row
+    bool v0, v1;       // lower / upper row is an across-pole reflection
+    float a, b;        // theta / phi fractions
+    bool flipped;
+};
+
+// Bound offsets to a finite range (NaN maps to the bound) so that the
+// float-to-int conversions below never overflow.
+__device__ __forceinline__ float bound_off(float v, float lim) {
+    return fmaxf(fminf(v, lim), -lim);
+}
+
+__device__ __forceinline__ CStencil centred_stencil(const SbGrid& g, Pos q, float colOff) {
+    CStencil s;
+    int bi = q.bi, bj = q.bj;
+    float ox = bound_off(q.ox, 4.0f * g.nT);
+    q.oy = bound_off(q.oy, 4.0f * g.nP);
+    s.flipped = unfold(g.nT, bi, ox, bj);
+    const float t = ox - 0.5f;
+    const float kf = floorf(t);
+    int lo = bi + (int)kf;
+    s.a = t - kf;
+    // positions lie in [0, nT] after unfolding; the clamp keeps every access
+    // in bounds even for non-finite input
+    lo = max(-1, min(lo, g.nT - 1));
+    const float ty = q.oy - colOff;
+    const float kj = floorf(ty);
+    const int j0 = (bj + (int)kj) & g.maskP;
+    const int j1 = (j0 + 1) & g.maskP;
+    s.b = ty - kj;
+    const int nT = g.nT;
+    // lower row
+    if (lo < 0) {
+        s.r0 = 0; s.v0 = true;
+        s.c00 = (j0 + nT) & g.maskP; s.c01 = (j1 + nT) & g.maskP;
+    } else {
+        s.r0 = lo; s.v0 = false; s.c00 = j0; s.c01 = j1;
+    }
+    const int hi = lo + 1;
+    if (hi > nT - 1) {
+        s.r1 = nT - 1; s.v1 = true;
+        s.c10 = (j0 + nT) & g.maskP; s.c11 = (j1 + nT) & g.maskP;
+    } else {
+        s.r1 = hi; s.v1 = false; s.c10 = j0; s.c11 = j1;
+    }
+    return s;
+}
+
+// Scalar or u_phi sample (sampleCentered kernel/bubble.cu:320-376, sampleVPhi
+// 178-240).  VEC: across-pole rows and flipped positions change sign.
+template <bool VEC>
+__device__ __forceinline__ float sample_centred(const SbGrid& g, const float* __restrict__ f,
+                                                Pos q, float colOff) {
+    const CStencil s = centred_stencil(g, q, colOff);
+    const int nP = g.nP;
+    float l = blerp(f[s.r0 * nP + s.c00], f[s.r0 * nP + s.c01], s.b);
+    float u = blerp(f[s.r1 * nP + s.c10], f[s.r1 * nP + s.c11], s.b);
+    if (VEC) {
+        if (s.v0) l = -l;
+        if (s.v1) u = -u;
+    }
+    float r = blerp(l, u, s.a);
+    if (VEC && s.flipped) r = -r;
+    return r;
+}
+
+__device__ __forceinline__ float sample_scalar(const SbGrid& g, const float* __restrict__ f, Pos q) {
+    return sample_centred<false>(g, f, q, 0.0f);
+}
+__device__ __forceinline__ float sample_uphi(const SbGrid& g, const float* __restrict__ f, Pos q) {
+    return sample_centred<true>(g, f, q, -0.5f);
+}
+
+// u_theta sample (sampleVTheta, kernel/bubble.cu:247-313).  Rows sit at raw
+// theta i + 1, i = 0..nT-2; next to a pole the nearest samples are the row and
+// its across-pole reflection two cells away.
+__device__ __forceinline__ float sample_utheta(const SbGrid& g, const float* __restrict__ f, Pos q) {
+    int bi = q.bi, bj = q.bj;
+    float ox = bound_off(q.ox, 4.0f * g.nT);
+    q.oy = bound_off(q.oy, 4.0f * g.nP);
+    const bool flipped = unfold(g.nT, bi, ox, bj);
+    const int nT = g.nT, nP = g.nP;
+    const float kf = floorf(ox);
+    int lo = bi - 1 + (int)kf;  // row coordinate s = raw - 1
+    float a = ox - kf;
+    lo = max(-1, min(lo, nT - 1));
+    const float ty = q.oy;
+    const float kj = floorf(ty);
+    const int j0 = (bj + (int)kj) & g.maskP;
+    const int j1 = (j0 + 1) & g.maskP;
+    const float b = ty - kj;
+    float r;
+    if (lo < 0) {
+        // between the reflection of row 0 (s = -2) and row 0 (s = 0)
+        const float s = (float)lo + a;  // in [-1, 0)
+        const float w = 0.5f * (s + 2.0f);
+        const float l = -blerp(f[(j0 + nT) & g.maskP], f[(j1 + nT) & g.maskP], b);
+        const float u = blerp(f[j0], f[j1], b);
+        r = blerp(l, u, w);
+    } else if (lo >= nT - 2) {
+        // between row nT-2 (s = nT-2) and its reflection (s = nT)
+        const float s = (float)(lo - (nT - 2)) + a;  // in [0, 1]
+        const int row = (nT - 2) * nP;
+        const float l = blerp(f[row + j0], f[row + j1], b);
+        const float u = -blerp(f[row + ((j0 + nT) & g.maskP)], f[row + ((j1 + nT) & g.maskP)], b);
+        r = blerp(l, u, 0.5f * s);
+    } else {
+        const float l = blerp(f[lo * nP + j0], f[lo * nP + j1], b);
+        const float u = blerp(f[(lo + 1) * nP + j0], f[(lo + 1) * nP + j1], b);
+        r = blerp(l, u, a);
+    }
+    return flipped ? -r : r;
+}
+
+// Characteristic-map lookup (sampleMapping, kernel/bubble.cu:539-606): the
+// four map points around q, slerped along phi on each row and then along
+// theta.  Map entries are float2 offsets from their own cell centre.  The
+// result is a displacement in frame F.
+__device__ __forceinline__ f3 sample_map(const SbGrid& g, const float2* __restrict__ map,
+                                         const Frame& F, Pos q) {
+    const CStencil s = centred_stencil(g, q, 0.0f);
+    const int nP = g.nP, nT = g.nT;
+    const float baseI = (float)0.5f - F.fi;
+    auto point = [&](int r, int c) -> f3 {
+        const float2 m = map[r * nP + c];
+        const float dth = (float)(r - F.bi) + baseI + m.x;
+        int dj = c - F.bj;
+        dj = ((dj + nT) & g.maskP) - nT;  // wrap to [-nT, nT)
+        const float dph = (float)dj + (m.y - F.fj);
+        return disp_from_offsets(F, dth, dph, g.h);
+    };
+    const f3 ll = point(s.r0, s.c00), lr = point(s.r0, s.c01);
+    const f3 hl = point(s.r1, s.c10), hr = point(s.r1, s.c11);
+    const f3 lo = slerp_disp(F, ll, lr, s.b);
+    const f3 hi = slerp_disp(F, hl, hr, s.b);
+    return slerp_disp(F, lo, hi, s.a);
+}
+
+// Offsets (grid units) of C + d from the frame base, for storing as a map
+// entry of a cell frame: phi offset wrapped to [-nT, nT).
+__device__ __forceinline__ float2 map_entry_from_disp(const SbGrid& g, const Frame& F, f3 d) {
+    const Pos q = pos_from_disp(F, d, g.invh, g.nT);
+    float dth = (float)(q.bi - F.bi) + (q.ox - F.fi);
+    float dph = (float)(q.bj - F.bj) + (q.oy - F.fj);
+    if (dph >= (float)g.nT) dph -= (float)g.nP;
+    if (dph < -(float)g.nT) dph += (float)g.nP;
+    return make_float2(dth, dph);
+}
+
+// Velocity (u_theta, u_phi) at an arbitrary position.
+__device__ __forceinline__ void velocity_at(const SbGrid& g, const float* __restrict__ uth,
+                                            const float* __restrict__ uph, Pos q, float& vt,
+                                            float& vp) {
+    vt = sample_utheta(g, uth, q);
+    vp = sample_uphi(g, uph, q);
+}
+
+// Local basis at the point P (unnormalised), as the reference derives it from
+// (acos(Pz), atan2(Py, Px)) (kernel/bubble.cu:462-471).
+__device__ __forceinline__ void basis_at(f3 P, f3& eth, f3& eph) {
+    const float rho = sqrtf(P.x * P.x + P.y * P.y);
+    const float r = sqrtf(rho * rho + P.z * P.z);
+    float cph = 1.0f, sph = 0.0f;
+    if (rho > 0.0f) {
+        cph = P.x / rho;
+        sph = P.y / rho;
+    }
+    const float ct = P.z / r, st = rho / r;
+    eth = {ct * cph, ct * sph, -st};
+    eph = {-sph, cph, 0.0f};
+}
+
+// Result of a great-circle backtrace from a frame base.
+struct Trace {
+    f3 d;        // displacement of the departure point
+    f3 u_, v_;   // final great-circle direction and its normal
+    float sd, cd;  // sin / cos of the final arc step
+    float fail;    // the zero or NaN speed that stopped the trace
+    bool moved;
+};
+
+// traceGreatCircle (kernel/bubble.cu:416-506) from the frame base with the
+// base velocity (gt, gp) already known.  dt > 0 traces backward.
+__device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restrict__ uth,
+                                          const float* __restrict__ uph, const Frame& F,
+                                          float gt, float gp, float dt) {
+    Trace T;
+    T.moved = false;
+    T.fail = 0.0f;
+    T.d = {0.0f, 0.0f, 0.0f};
+    const f3 w = {F.s0, 0.0f, F.c0};
+    const f3 eth = {F.c0, 0.0f, -F.s0};
+    const f3 eph = {0.0f, 1.0f, 0.0f};
+    f3 u = gt * eth + gp * eph;
+    float un = len3(u);
+    if (!(un > 0.0f)) { T.fail = un; return T; }
+    f3 u_ = (1.0f / un) * u;
+    f3 v_ = cross3(w, u_);
+    float dS = -0.5f * un * dt;
+    float sd, sh, ch;
+    sincosf(0.5f * dS, &sh, &ch);
+    sd = 2.0f * sh * ch;
+    float cdm1 = -2.0f * sh * sh;
+    const f3 dmid = sd * u_ + cdm1 * w;
+    const f3 midx = w + dmid;
+    const Pos qm = pos_from_disp(F, dmid, g.invh, g.nT);
+    float mt, mp;
+    velocity_at(g, uth, uph, qm, mt, mp);
+    f3 beth, beph;
+    basis_at(midx, beth, beph);
+    const f3 mu = mt * beth + mp * beph;
+    const f3 uCircleMid = (1.0f + cdm1) * u_ - sd * w;
+    const f3 vCircleMid = cross3(midx, uCircleMid);
+    const float mgt = dot3(mu, vCircleMid);
+    const float mgp = dot3(mu, uCircleMid);
+    u = mgp * u_ + mgt * v_;
+    un = len3(u);
+    if (!(un > 0.0f)) { T.fail = un; return T; }
+    u_ = (1.0f / un) * u;
+    v_ = cross3(w, u_);
+    dS = -un * dt;
+    sincosf(0.5f * dS, &sh, &ch);
+    sd = 2.0f * sh * ch;
+    cdm1 = -2.0f * sh * sh;
+    T.d = sd * u_ + cdm1 * w;
+    T.u_ = u_;
+    T.v_ = v_;
+    T.sd = sd;
+    T.cd = 1.0f + cdm1;
+    T.moved = true;
+    return T;
+}
+
+__device__ __forceinline__ Frame cell_frame(const SbGrid& g, int i, int j) {
+    Frame F;
+    F.bi = i; F.bj = j; F.fi = 0.5f; F.fj = 0.0f;
+    F.s0 = g.sin_c[i]; F.c0 = g.cos_c[i];
+    return F;
+}
+
+__device__ __forceinline__ Pos frame_pos(const Frame& F, float dth, float dph) {
+    Pos q;
+    q.bi = F.bi; q.bj = F.bj; q.ox = F.fi + dth; q.oy = F.fj + dph;
+    return q;
+}
+
+}  // namespace sb

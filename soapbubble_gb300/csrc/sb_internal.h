@@ -1,0 +1,52 @@
+// Internal declarations shared by the CUDA translation units and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sb_types.h"
+
+namespace sb {
+
+// Every device array of one bubble.  Fields are FP32, row-major [theta][phi]
+// with row stride nPhi; u_theta has nTheta-1 rows.  "A" buffers hold the
+// state between steps, "adv" buffers the advected intermediate state.
+struct SbFields {
+    float *eta, *gam, *uth, *uph;                  // state
+    float *eta_adv, *gam_adv, *uth_adv, *uph_adv;  // after advection
+    float *eta_init, *eta_delta, *eta_initL, *eta_deltaL;
+    float *gam_init, *gam_delta, *gam_initL, *gam_deltaL;
+    float2 *fwd[2], *bwd[2], *bwdprev;             // map offsets (ping-pong)
+    float *uair_init, *vair_init, *corr_u, *corr_v;
+    float *uair, *vair;                            // N+1, Nv+1 (last element 0)
+    float *div, *d_eta, *d_gam, *err_eta, *err_gam;
+    float *diag, *cE, *cS, *rhs;                   // implicit system
+    float *x, *r, *z, *p, *q;                      // solver vectors
+    double *x64;                                   // mixed-precision iterate
+    double *partials;                              // per-block reduction slots
+    SbStepParams* step;                            // device copy of step scalars
+    SbDevStats* stats;
+};
+
+struct SolverConfig {
+    int mode;       // 0: plain FP32, 1: mixed precision (FP64 dots + refinement)
+    int max_iter;
+    double tol;     // relative residual ||b - A x|| / ||b||
+    int precond;    // 0: Jacobi
+};
+
+// Step stages (sb_step.cu).  `cur` selects the map ping-pong buffers.
+cudaError_t launch_advect(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                          cudaStream_t s);
+cudaError_t launch_assemble(const SbGrid& g, const SbPhys& ph, const SbFields& f, cudaStream_t s);
+cudaError_t launch_post(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                        cudaStream_t s);
+cudaError_t launch_reinit(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                          cudaStream_t s);
+cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s);
+cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s);
+
+// Implicit surfactant solve (sb_solver.cu).
+cudaError_t launch_solve(const SbGrid& g, const SbPhys& ph, const SbFields& f,
+                         const SolverConfig& cfg, cudaStream_t s);
+int solver_partials_needed(const SbGrid& g);
+
+}  // namespace sb

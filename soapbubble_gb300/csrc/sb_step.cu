@@ -1,0 +1,554 @@
+// Step kernels of the soap-bubble solver (everything except the implicit
+// solve).  One thread per grid cell; a warp covers 32 consecutive phi cells
+// of one theta row, so direct loads are coalesced and the sampler gathers of
+// nearby departure points hit L1/L2.
+//
+// Stage map against the reference (kernel/solver.cu:260-292):
+//   k_advect_maps  updateForward/updateBackward (bubble.cu:609-633, 1049-1116),
+//                  advectionCentered for gamma (910-931), airFlowU/V (2301-2380)
+//   k_velocity     advectionVSphereTheta/PhiKernel (639-904)
+//   k_bimocq       advectionCenteredBimocq (967-1013)
+//   k_assemble     concentrationLinearSystemKernel (1301-1473)
+//   k_post         divergenceKernel_fromGamma, applyforcevel{theta,phi},
+//                  applyforceThickness, substractPitched (1276-1295, 1819-1935,
+//                  2041-2078)
+//   k_accum        accumulateChangesCentered x2 (2081-2114) and
+//                  estimateDistortionKernel + maxAbs (1131-1168, 1019-1043)
+//   k_reinit{1,2,3} reInitializeMapping, correctCentered1/2 (2180-2280, 2509-2564)
+// van der Waals is identically zero in the reference (W1 = W2 = 0,
+// bubble.cu:2633-2638) and is folded out.
+#include "sb_device.cuh"
+#include "sb_internal.h"
+
+namespace sb {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr float kEps = 1e-7f;  // bubble.cu:28
+
+__constant__ float kW5[5] = {0.125f, 0.125f, 0.125f, 0.125f, 0.5f};
+__constant__ float kDirT[5] = {-0.25f, 0.25f, -0.25f, 0.25f, 0.0f};  // theta offsets
+__constant__ float kDirP[5] = {-0.25f, -0.25f, 0.25f, 0.25f, 0.0f};  // phi offsets
+
+__device__ __forceinline__ Frame face_frame_uphi(const SbGrid& g, int i, int j) {
+    Frame F;
+    F.bi = i; F.bj = j; F.fi = 0.5f; F.fj = -0.5f;
+    F.s0 = g.sin_c[i]; F.c0 = g.cos_c[i];
+    return F;
+}
+
+__device__ __forceinline__ Frame face_frame_utheta(const SbGrid& g, int i, int j) {
+    Frame F;
+    F.bi = i + 1; F.bj = j; F.fi = 0.0f; F.fj = 0.0f;
+    F.s0 = g.sin_e[i + 1]; F.c0 = g.cos_e[i + 1];
+    return F;
+}
+
+__device__ __forceinline__ Pos pos_of(const Frame& F, const Trace& T, const SbGrid& g) {
+    return T.moved ? pos_from_disp(F, T.d, g.invh, g.nT) : frame_pos(F, 0.0f, 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock)
+k_advect_maps(SbGrid g, SbFields f, int cur) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx == 0) {
+        f.stats->distortion_bits = 0u;
+        f.stats->reinit = 0;
+        f.stats->broken_cells = 0;
+    }
+    if (idx >= g.N) return;
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const float dt = f.step->dt;
+    const Frame F = cell_frame(g, i, j);
+    const Pos q0 = frame_pos(F, 0.0f, 0.0f);
+    float gt, gp;
+    velocity_at(g, f.uth, f.uph, q0, gt, gp);
+
+    // forward map: trace forward in time (negative step), sample the old map
+    const Trace Tf = trace_gc(g, f.uth, f.uph, F, gt, gp, -dt);
+    const f3 df = sample_map(g, f.fwd[cur], F, pos_of(F, Tf, g));
+    f.fwd[cur ^ 1][idx] = map_entry_from_disp(g, F, df);
+
+    // backward map and gamma share the backward trace
+    const Trace Tb = trace_gc(g, f.uth, f.uph, F, gt, gp, dt);
+    const Pos qb = pos_of(F, Tb, g);
+    const f3 db = sample_map(g, f.bwd[cur], F, qb);
+    f.bwd[cur ^ 1][idx] = map_entry_from_disp(g, F, db);
+    f.gam_adv[idx] = sample_scalar(g, f.gam, qb);
+
+    // air flow = initial wind + corridor(t); NaN -> 0
+    const float wg = f.step->windg;
+    float ua = f.uair_init[idx] + wg * f.corr_u[idx];
+    f.uair[idx] = isnan(ua) ? 0.0f : ua;
+    if (i < g.nT - 1) {
+        float va = f.vair_init[idx] + wg * f.corr_v[idx];
+        f.vair[idx] = isnan(va) ? 0.0f : va;
+    }
+}
+
+// Velocity self-advection with parallel transport (RUNGE_KUTTA path).
+__device__ __forceinline__ float advect_velocity(const SbGrid& g, const float* __restrict__ uth,
+                                                 const float* __restrict__ uph, const Frame& F,
+                                                 float gt, float gp, float dt, bool outPhi) {
+    const f3 w = {F.s0, 0.0f, F.c0};
+    // a zero or NaN speed stops the trace; the reference then writes that
+    // speed (bubble.cu:689-692, 727-730)
+    const Trace T = trace_gc(g, uth, uph, F, gt, gp, dt);
+    if (!T.moved) return T.fail;
+    const f3 P = w + T.d;
+    const Pos qp = pos_from_disp(F, T.d, g.invh, g.nT);
+    float pt, pp;
+    velocity_at(g, uth, uph, qp, pt, pp);
+    f3 beth, beph;
+    basis_at(P, beth, beph);
+    const f3 pu = pt * beth + pp * beph;
+    const f3 uCircleP = T.cd * T.u_ - T.sd * w;
+    const f3 vCircleP = cross3(P, uCircleP);
+    const float a = dot3(pu, vCircleP);
+    const float b = dot3(pu, uCircleP);
+    const f3 pu2 = b * T.u_ + a * T.v_;
+    if (outPhi) return pu2.y;                       // e_phi = (0, 1, 0)
+    return pu2.x * F.c0 - pu2.z * F.s0;             // e_theta = (c0, 0, -s0)
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_velocity(SbGrid g, SbFields f) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N) return;
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const float dt = f.step->dt;
+    {
+        const Frame F = face_frame_uphi(g, i, j);
+        const float gp = f.uph[idx];
+        const float gt = sample_utheta(g, f.uth, frame_pos(F, 0.0f, 0.0f));
+        f.uph_adv[idx] = advect_velocity(g, f.uth, f.uph, F, gt, gp, dt, true);
+    }
+    if (i < g.nT - 1) {
+        const Frame F = face_frame_utheta(g, i, j);
+        const float gt = f.uth[idx];
+        const float gp = sample_uphi(g, f.uph, frame_pos(F, 0.0f, 0.0f));
+        f.uth_adv[idx] = advect_velocity(g, f.uth, f.uph, F, gt, gp, dt, false);
+    }
+}
+
+// BIMOCQ thickness: compose the new backward map with the previous one and
+// blend the two reconstructions (MULTISAMPLE, 5 samples).
+__global__ void __launch_bounds__(kBlock)
+k_bimocq(SbGrid g, SbPhys ph, SbFields f, int cur) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N) return;
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    if (f.eta[idx] == 0.0f) {
+        f.eta_adv[idx] = 0.0f;
+        return;
+    }
+    const Frame F = cell_frame(g, i, j);
+    const float2* bwd = f.bwd[cur ^ 1];
+    const float blend = ph.blend;
+    float attrib = 0.0f;
+#pragma unroll 1
+    for (int k = 0; k < 5; ++k) {
+        const Pos q = frame_pos(F, kDirT[k], kDirP[k]);
+        const f3 d1 = sample_map(g, bwd, F, q);
+        const Pos q1 = pos_from_disp(F, d1, g.invh, g.nT);
+        const f3 d2 = sample_map(g, f.bwdprev, F, q1);
+        const Pos q2 = pos_from_disp(F, d2, g.invh, g.nT);
+        const float sDelta = sample_scalar(g, f.eta_delta, q1);
+        attrib += (1.0f - blend) * kW5[k] *
+                  (sample_scalar(g, f.eta_initL, q2) + sDelta + sample_scalar(g, f.eta_deltaL, q2));
+        attrib += blend * kW5[k] * (sample_scalar(g, f.eta_init, q1) + sDelta);
+    }
+    f.eta_adv[idx] = fmaxf(0.0f, attrib);
+}
+
+__device__ __forceinline__ bool is_broken(float gamma, float eta, float gmax) {
+    return gamma > gmax - kEps || eta == 0.0f;
+}
+
+// Implicit surfactant system (paper eq. 26) in symmetric 5-point form:
+// diag, coupling to the east neighbour (cE) and to the south neighbour (cS).
+// The reference's couplings across the poles carry sin(0) and sin(pi) and
+// are zero.  A broken cell (gamma at its maximum or no film) is an identity
+// row with value gmax; its couplings are moved to the neighbours'
+// right-hand sides so that the matrix stays symmetric positive definite.
+__global__ void __launch_bounds__(kBlock)
+k_assemble(SbGrid g, SbPhys ph, SbFields f) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N) return;
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const int nP = g.nP, nT = g.nT;
+    const float dt = f.step->dt, invDt = f.step->invDt;
+    const float mixA = f.step->mixA, mixB = f.step->mixB;
+    const float gmax = ph.gmax, Cr = ph.Cr;
+    const float* eta_a = f.eta_adv;
+    const float gamma = f.gam_adv[idx];
+    const float eta = eta_a[idx];
+    const int jE = (j + 1) & g.maskP, jW = (j - 1) & g.maskP;
+    const int iE = i * nP + jE, iW = i * nP + jW;
+    if (is_broken(gamma, eta, gmax)) {
+        f.diag[idx] = 1.0f;
+        f.cE[idx] = 0.0f;
+        f.cS[idx] = 0.0f;
+        f.rhs[idx] = gmax;
+        f.gam_adv[idx] = gmax;
+        atomicAdd(&f.stats->broken_cells, 1);
+        return;
+    }
+    const float sinT = g.sin_c[i];
+    const float sinN = g.sin_e[i];
+    const float sinS = g.sin_e[i + 1];
+    const float cscT = 1.0f / sinT;
+    const float etaW = eta_a[iW], etaE = eta_a[iE];
+    float etaN, etaS;
+    float vN = 0.0f, vS = 0.0f, vAirN = 0.0f, vAirS = 0.0f;
+    const int opp = nP - j;            // flat mirrored index (reads next row at j = 0)
+    const int oppE = nP - jE;
+    if (i != 0) {
+        const int n = (i - 1) * nP + j;
+        vAirN = 0.5f * (f.vair[n] * mixA - f.vair[(i - 1) * nP + opp] * mixB);
+        vN = f.uth_adv[n];
+        etaN = eta_a[n];
+    } else {
+        etaN = eta_a[(j + nT) & g.maskP];
+    }
+    if (i != nT - 1) {
+        vAirS = 0.5f * (f.vair[idx] * mixA - f.vair[i * nP + opp] * mixB);
+        vS = f.uth_adv[idx];
+        etaS = eta_a[idx + nP];
+    } else {
+        etaS = eta_a[i * nP + ((j + nT) & g.maskP)];
+    }
+    float uW = f.uph_adv[idx], uE = f.uph_adv[iE];
+    if (isnan(vN)) vN = 0.0f;
+    if (isnan(vS)) vS = 0.0f;
+    if (isnan(uW)) uW = 0.0f;
+    if (isnan(uE)) uE = 0.0f;
+    const float uAirW = 0.5f * (f.uair[idx] * mixA + f.uair[i * nP + opp] * mixB);
+    const float uAirE = 0.5f * (f.uair[iE] * mixA + f.uair[i * nP + oppE] * mixB);
+
+    const float CrDt = Cr * dt, MDt = ph.M * dt;
+    const float s2 = g.invh * g.invh;
+    const float etaUp = (etaN + eta) * 0.5f;
+    const float etaLeft = (etaW + eta) * 0.5f;
+    const float etaRight = (etaE + eta) * 0.5f;
+    const float etaDown = (etaS + eta) * 0.5f;
+    const float up = (i == 0) ? 0.0f : -s2 * sinN * MDt / (etaUp + CrDt);
+    const float left = -s2 * cscT * MDt / (etaLeft + CrDt);
+    const float right = -s2 * cscT * MDt / (etaRight + CrDt);
+    const float down = (i == nT - 1) ? 0.0f : -s2 * sinS * MDt / (etaDown + CrDt);
+    const float diag = sinT * invDt / gamma - (up + left + right + down);
+
+    float sinThetaDiv = g.invh * (uE * etaRight / (etaRight + CrDt) - uW * etaLeft / (etaLeft + CrDt) +
+                                  (vS * sinS * etaDown / (etaDown + CrDt) -
+                                   vN * sinN * etaUp / (etaUp + CrDt)));
+    sinThetaDiv += g.invh * (uAirE / (etaRight / Cr * invDt + 1.0f) -
+                             uAirW / (etaLeft / Cr * invDt + 1.0f) +
+                             vAirS * sinS / (etaDown / Cr * invDt + 1.0f) -
+                             vAirN * sinN / (etaUp / Cr * invDt + 1.0f));
+    sinThetaDiv += ph.gs * g.invh *
+                   (sinS * sinS * etaDown / (invDt * etaDown + Cr) -
+                    sinN * sinN * etaUp / (invDt * etaUp + Cr));
+    float rhs = sinT * invDt - sinThetaDiv;
+
+    // eliminate couplings to broken neighbours (their value is gmax)
+    const bool bE = is_broken(f.gam_adv[iE], etaE, gmax);
+    const bool bW = is_broken(f.gam_adv[iW], etaW, gmax);
+    if (bE) rhs -= right * gmax;
+    if (bW) rhs -= left * gmax;
+    bool bS = false;
+    if (i != 0 && is_broken(f.gam_adv[idx - nP], etaN, gmax)) rhs -= up * gmax;
+    if (i != nT - 1) {
+        bS = is_broken(f.gam_adv[idx + nP], etaS, gmax);
+        if (bS) rhs -= down * gmax;
+    }
+    f.diag[idx] = diag;
+    f.cE[idx] = bE ? 0.0f : right;
+    f.cS[idx] = bS ? 0.0f : down;
+    f.rhs[idx] = rhs;
+}
+
+__device__ __forceinline__ float clamp_gamma(float gm, float gmax) {
+    return (gm <= 0.0f || gm > gmax - kEps) ? gmax : gm;
+}
+
+// After the solve: divergence from gamma, friction/Marangoni/gravity velocity
+// update, thickness update with evaporation, and the per-step changes that
+// BIMOCQ accumulates.  Neighbouring new gamma values are clamped on the fly
+// exactly as divergenceKernel_fromGamma clamps them in place.
+__global__ void __launch_bounds__(kBlock)
+k_post(SbGrid g, SbPhys ph, SbFields f) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N) return;
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const int nP = g.nP;
+    const float dt = f.step->dt, invDt = f.step->invDt;
+    const float gmax = ph.gmax, M = ph.M, Cr = ph.Cr;
+    const float gOld = f.gam_adv[idx];
+    const float gNew = f.x[idx];
+    float div, gFin;
+    if (gNew <= 0.0f || gNew > gmax - kEps) {
+        gFin = gmax;
+        div = invDt;
+    } else {
+        gFin = gNew;
+        div = (1.0f - fminf(gNew, 2.0f * gOld) / gOld) / dt;
+    }
+    f.gam[idx] = gFin;
+    f.d_gam[idx] = gFin - gOld;
+
+    const float e = f.eta_adv[idx];
+    float eo = e * (1.0f - dt * div);
+    eo += f.step->evapDt;
+    eo = fmaxf(0.0f, eo);
+    f.eta[idx] = eo;
+    f.d_eta[idx] = eo - e;
+
+    // u_phi face between (i, j-1) and (i, j)
+    {
+        const int w = i * nP + ((j - 1) & g.maskP);
+        const float etaW = f.eta_adv[w];
+        const float gW = clamp_gamma(f.x[w], gmax);
+        const float invEta = 2.0f / (etaW + e);
+        const float u1 = f.uph_adv[idx];
+        if (isinf(invEta)) {
+            f.uph[idx] = __int_as_float(0x7fffffff);
+        } else {
+            const float cscT = 1.0f / g.sin_c[i];
+            const float pGpx = g.invh * (gFin - gW) * cscT;
+            const float f1 = -M * invEta * pGpx;
+            const float f2 = Cr * invEta * f.uair[idx];
+            f.uph[idx] = (u1 * invDt + f1 + f2) / (invDt + Cr * invEta);
+        }
+    }
+    // u_theta face between (i, j) and (i+1, j)
+    if (i < g.nT - 1) {
+        const int s = idx + nP;
+        const float etaS = f.eta_adv[s];
+        const float gS = clamp_gamma(f.x[s], gmax);
+        const float invEta = 2.0f / (e + etaS);
+        const float v1 = f.uth_adv[idx];
+        if (isinf(invEta)) {
+            f.uth[idx] = __int_as_float(0x7fffffff);
+        } else {
+            const float pGpy = g.invh * (gS - gFin);
+            const float f1 = -M * invEta * pGpy;
+            const float f2 = Cr * invEta * f.vair[idx];
+            const float f3v = ph.gs * g.sin_e[i + 1];
+            f.uth[idx] = (v1 * invDt + f1 + f2 + f3v) / (invDt + Cr * invEta);
+        }
+    }
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// BIMOCQ change accumulation through the forward map, fused with the
+// forward/backward distortion estimate of the same maps.
+__global__ void __launch_bounds__(kBlock)
+k_accum(SbGrid g, SbFields f, int cur) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    float dist = 0.0f;
+    if (idx < g.N) {
+        const int i = idx >> g.logP, j = idx & g.maskP;
+        const Frame F = cell_frame(g, i, j);
+        const float2* fwd = f.fwd[cur ^ 1];
+        const float2* bwd = f.bwd[cur ^ 1];
+        float ed = f.eta_delta[idx], gd = f.gam_delta[idx];
+#pragma unroll 1
+        for (int k = 0; k < 5; ++k) {
+            const f3 d = sample_map(g, fwd, F, frame_pos(F, kDirT[k], kDirP[k]));
+            const Pos q = pos_from_disp(F, d, g.invh, g.nT);
+            ed += kW5[k] * sample_scalar(g, f.d_eta, q);
+            gd += kW5[k] * sample_scalar(g, f.d_gam, q);
+        }
+        f.eta_delta[idx] = ed;
+        f.gam_delta[idx] = gd;
+        // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
+        float2 m = fwd[idx];
+        const float d1 = dist_from_disp(sample_map(g, bwd, F, frame_pos(F, m.x, m.y)), g.invh);
+        m = bwd[idx];
+        const float d2 = dist_from_disp(sample_map(g, fwd, F, frame_pos(F, m.x, m.y)), g.invh);
+        dist = fmaxf(fabsf(d1), fabsf(d2));
+        if (isnan(dist)) dist = 0.0f;
+    }
+    __shared__ float smax[kBlock / 32];
+    dist = warp_max(dist);
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = dist;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float v = threadIdx.x < kBlock / 32 ? smax[threadIdx.x] : 0.0f;
+        v = warp_max(v);
+        if (threadIdx.x == 0) atomicMax(&f.stats->distortion_bits, __float_as_uint(v));
+    }
+}
+
+__device__ __forceinline__ bool reinit_now(const SbDevStats* st) {
+    if (st->force_reinit >= 0) return st->force_reinit != 0;
+    return __uint_as_float(st->distortion_bits) > 4.0f;
+}
+
+// correctCentered1: BIMOCQ error estimate through the forward map.
+__global__ void __launch_bounds__(kBlock)
+k_reinit1(SbGrid g, SbFields f, int cur) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N || !reinit_now(f.stats)) return;
+    if (idx == 0) {
+        f.stats->reinit = 1;
+        f.stats->reinit_total += 1;
+    }
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const Frame F = cell_frame(g, i, j);
+    const float2* fwd = f.fwd[cur ^ 1];
+    float th = 0.0f, gm = 0.0f;
+#pragma unroll 1
+    for (int k = 0; k < 5; ++k) {
+        const f3 d = sample_map(g, fwd, F, frame_pos(F, kDirT[k], kDirP[k]));
+        const Pos q = pos_from_disp(F, d, g.invh, g.nT);
+        th += kW5[k] * sample_scalar(g, f.eta, q);
+        gm += kW5[k] * sample_scalar(g, f.gam, q);
+    }
+    f.err_eta[idx] = (th - f.eta_delta[idx] - f.eta_init[idx]) * 0.5f;
+    f.err_gam[idx] = (gm - f.gam_delta[idx] - f.gam_init[idx]) * 0.5f;
+}
+
+// 3x3 neighbour of (i, j) with the reference's across-pole rule (validateId).
+__device__ __forceinline__ int nb_index(const SbGrid& g, int i, int j) {
+    if (i < 0) { i = 0; j += g.nT; }
+    else if (i >= g.nT) { i = g.nT - 1; j += g.nT; }
+    return i * g.nP + (j & g.maskP);
+}
+
+// correctCentered2: subtract the error pulled back through the backward map,
+// clamp to the 3x3 range of the uncorrected field, keep non-negative.  The
+// result goes to the *_adv buffers; k_reinit3 commits it.
+__global__ void __launch_bounds__(kBlock)
+k_reinit2(SbGrid g, SbFields f, int cur) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N || !reinit_now(f.stats)) return;
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const Frame F = cell_frame(g, i, j);
+    const float2* bwd = f.bwd[cur ^ 1];
+    float th = f.eta[idx], gm = f.gam[idx];
+#pragma unroll 1
+    for (int k = 0; k < 5; ++k) {
+        const f3 d = sample_map(g, bwd, F, frame_pos(F, kDirT[k], kDirP[k]));
+        const Pos q = pos_from_disp(F, d, g.invh, g.nT);
+        th -= kW5[k] * sample_scalar(g, f.err_eta, q);
+        gm -= kW5[k] * sample_scalar(g, f.err_gam, q);
+    }
+    float emin = f.eta[idx], emax = emin, gmin = f.gam[idx], gmx = gmin;
+    for (int t = -1; t <= 1; ++t)
+        for (int p = -1; p <= 1; ++p) {
+            const int n = nb_index(g, i + t, j + p);
+            const float ev = f.eta[n], gv = f.gam[n];
+            emin = fminf(emin, ev); emax = fmaxf(emax, ev);
+            gmin = fminf(gmin, gv); gmx = fmaxf(gmx, gv);
+        }
+    th = (th < emin) ? emin : (emax < th) ? emax : th;
+    gm = (gm < gmin) ? gmin : (gmx < gm) ? gmx : gm;
+    f.eta_adv[idx] = fmaxf(0.0f, th);
+    f.gam_adv[idx] = fmaxf(0.0f, gm);
+}
+
+// Commit the correction, rotate the BIMOCQ buffers and reset the maps.
+__global__ void __launch_bounds__(kBlock)
+k_reinit3(SbGrid g, SbFields f, int cur) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N || !reinit_now(f.stats)) return;
+    const float e = f.eta_adv[idx], gm = f.gam_adv[idx];
+    f.eta[idx] = e;
+    f.gam[idx] = gm;
+    f.eta_initL[idx] = f.eta_init[idx];
+    f.eta_deltaL[idx] = f.eta_delta[idx];
+    f.gam_initL[idx] = f.gam_init[idx];
+    f.gam_deltaL[idx] = f.gam_delta[idx];
+    f.eta_init[idx] = e;
+    f.eta_delta[idx] = 0.0f;
+    f.gam_init[idx] = gm;
+    f.gam_delta[idx] = 0.0f;
+    f.bwdprev[idx] = f.bwd[cur ^ 1][idx];
+    f.fwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
+    f.bwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
+}
+
+__global__ void k_reset_maps(SbGrid g, SbFields f) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.N) return;
+    const float2 z = make_float2(0.0f, 0.0f);
+    f.fwd[0][idx] = z; f.fwd[1][idx] = z;
+    f.bwd[0][idx] = z; f.bwd[1][idx] = z;
+    f.bwdprev[idx] = z;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Mass integrals sum(eta sin theta), sum(gamma sin theta) for conservation checks.
+__global__ void k_mass(SbGrid g, SbFields f) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    double me = 0.0, mg = 0.0;
+    if (idx < g.N) {
+        const double s = (double)g.sin_c[idx >> g.logP];
+        me = (double)f.eta[idx] * s;
+        mg = (double)f.gam[idx] * s;
+    }
+    me = warp_sum_d(me);
+    mg = warp_sum_d(mg);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&f.stats->mass_eta, me);
+        atomicAdd(&f.stats->mass_gamma, mg);
+    }
+}
+
+inline dim3 grid_for(const SbGrid& g) { return dim3((g.N + kBlock - 1) / kBlock); }
+
+}  // namespace
+
+cudaError_t launch_advect(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                          cudaStream_t s) {
+    k_advect_maps<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
+    k_velocity<<<grid_for(g), kBlock, 0, s>>>(g, f);
+    k_bimocq<<<grid_for(g), kBlock, 0, s>>>(g, ph, f, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble(const SbGrid& g, const SbPhys& ph, const SbFields& f, cudaStream_t s) {
+    k_assemble<<<grid_for(g), kBlock, 0, s>>>(g, ph, f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_post(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                        cudaStream_t s) {
+    k_post<<<grid_for(g), kBlock, 0, s>>>(g, ph, f);
+    k_accum<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reinit(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                          cudaStream_t s) {
+    (void)ph;
+    k_reinit1<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
+    k_reinit2<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
+    k_reinit3<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s) {
+    k_reset_maps<<<grid_for(g), kBlock, 0, s>>>(g, f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&f.stats->mass_eta, 0, 2 * sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    k_mass<<<grid_for(g), kBlock, 0, s>>>(g, f);
+    return cudaGetLastError();
+}
+
+}  // namespace sb

@@ -1,0 +1,52 @@
+// Plain-data structures shared by host and device code.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sb {
+
+// Grid geometry and per-row trigonometric tables of one bubble.
+struct SbGrid {
+    int nT, nP, maskP, logP;  // nTheta, nPhi = 2 nTheta (power of two)
+    int N, Nv;                // nT*nP cells, (nT-1)*nP u_theta faces
+    float h, invh;            // pi / nT and its inverse
+    const float* sin_c;       // sin((i + 0.5) h), i < nT
+    const float* cos_c;
+    const float* sin_e;       // sin(i h), i <= nT (row edges; u_theta faces at i + 1)
+    const float* cos_e;
+};
+
+// Scalars that change per step (kept in device memory so a captured graph
+// can be replayed with new values).
+struct SbStepParams {
+    float dt;       // nondimensional step (timeStepGlobal)
+    float invDt;
+    float windg;    // air-flow corridor time factor 3 - |t - 3|
+    float mixA;     // t / 12 (mirrored wind mix, kernel/bubble.cu:1360-1392)
+    float mixB;     // 1 - t / 12
+    float evapDt;   // evaporationRate * dt
+    float gsdt;     // unused scratch
+    float pad;
+};
+
+// Constant physical coefficients of one bubble.
+struct SbPhys {
+    float M, Cr, gs, gmax, blend, evap;
+};
+
+// Per-step diagnostics written by the kernels.
+struct SbDevStats {
+    unsigned int distortion_bits;  // max distortion (float bits, non-negative)
+    int reinit;                    // 1 when this step re-initialised the maps
+    int solver_iters;
+    int broken_cells;
+    double solver_rel_resid;
+    double solver_b_norm;
+    int solver_converged;
+    int force_reinit;              // -1 decide, 0 never, 1 always
+    double mass_eta;               // sum eta * sin(theta)
+    double mass_gamma;
+    long long reinit_total;        // re-initialisations since creation
+};
+
+}  // namespace sb

@@ -1,0 +1,54 @@
+"""Shared helpers of the parity tests: state transfer between the FP64
+oracle and the GPU bubble, and error metrics."""
+from __future__ import annotations
+
+import numpy as np
+
+# GPU field name -> oracle array name
+FIELD_MAP = {
+    "eta": "eta", "gamma": "gamma", "u_theta": "uth", "u_phi": "uph",
+    "eta_init": "eta_init", "eta_delta": "eta_delta", "eta_init_last": "eta_initLast",
+    "eta_delta_last": "eta_deltaLast", "gamma_init": "gam_init", "gamma_delta": "gam_delta",
+    "gamma_init_last": "gam_initLast", "gamma_delta_last": "gam_deltaLast",
+    "fwd_t": "fwd_t", "fwd_p": "fwd_p", "bwd_t": "bwd_t", "bwd_p": "bwd_p",
+    "bwdprev_t": "bwdprev_t", "bwdprev_p": "bwdprev_p",
+    "uair_init": "uair_init", "vair_init": "vair_init",
+}
+SCALARS = ["eta", "gamma", "u_theta", "u_phi", "eta_init", "eta_delta", "eta_init_last",
+           "eta_delta_last", "gamma_init", "gamma_delta", "gamma_init_last", "gamma_delta_last"]
+MAPS = [("fwd_t", "fwd_p"), ("bwd_t", "bwd_p"), ("bwdprev_t", "bwdprev_p")]
+
+
+def sync_state(gb, ob) -> None:
+    """Upload the oracle state to the GPU, then copy the GPU's (FP32-rounded)
+    state back into the oracle, so that both start from identical values."""
+    for gname, oname in FIELD_MAP.items():
+        gb.upload(gname, ob.a[oname])
+    for gname, oname in FIELD_MAP.items():
+        ob.a[oname][...] = gb.download(gname).reshape(ob.a[oname].shape)
+
+
+def rel_err(gpu: np.ndarray, ref: np.ndarray, floor: float = 1e-30) -> float:
+    """Normwise relative error max|gpu - ref| / max|ref|."""
+    d = np.abs(gpu - ref)
+    m = np.nanmax(np.abs(ref))
+    return float(np.nanmax(d) / max(m, floor))
+
+
+def map_err_cells(gt, gp, ot, op, nTheta: int) -> float:
+    """Largest distance (grid units) between GPU and oracle map points."""
+    nPhi = 2 * nTheta
+    dth = gt - ot
+    dph = np.mod(gp - op + nTheta, nPhi) - nTheta
+    s = np.sin(np.pi * ot / nTheta)
+    return float(np.max(np.sqrt(dth ** 2 + (s * dph) ** 2)))
+
+
+def compare(gb, ob, names=None) -> dict:
+    out = {}
+    for gname in names or SCALARS:
+        out[gname] = rel_err(gb.download(gname), ob.a[FIELD_MAP[gname]])
+    for t, p in MAPS:
+        out[t[:-2]] = map_err_cells(gb.download(t), gb.download(p), ob.a[FIELD_MAP[t]],
+                                    ob.a[FIELD_MAP[p]], gb.nTheta)
+    return out
