@@ -146,6 +146,11 @@ int sb_update_mass(sb_bubble* b);
  * *broken when no cell has eta > 0. */
 int sb_write_thickness_exr(sb_bubble* b, const char* path, int* broken);
 
+/* Host-only: writes img (height rows of width floats) as the reference's
+ * grayscale frame format: 3 equal HALF channels B, G, R, no compression
+ * (Solver::write_image, kernel/solver.cu:338-385).  Needs no GPU. */
+int sb_write_exr_gray(const char* path, int width, int height, const float* img);
+
 /* Replaces Bubble::run (kernel/bubble.cu:2607-2704): the frame loop with
  * full steps, a fractional last step per frame, and frame%04d.exr output
  * into out_dir (NULL: no output).  frames <= 0 uses p->frames. */

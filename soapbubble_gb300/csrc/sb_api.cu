@@ -131,7 +131,7 @@ struct ArenaPlan {
     size_t fwd[2], bwd[2], bwdprev;
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
     size_t div, d_eta, d_gam, err_eta, err_gam;
-    size_t diag, cE, cS, rhs, x, r, z, p, q, x64, partials, step, stats;
+    size_t dmass, cE, cS, rhs, r0, x, dx, r, z, p, q, x64, partials, step, stats;
 };
 
 ArenaPlan plan_arena(const SbGrid& g, int partials) {
@@ -150,8 +150,9 @@ ArenaPlan plan_arena(const SbGrid& g, int partials) {
     a.uair = a.L.take((N + 1) * F); a.vair = a.L.take((Nv + 1) * F);
     a.div = a.L.take(N * F); a.d_eta = a.L.take(N * F); a.d_gam = a.L.take(N * F);
     a.err_eta = a.L.take(N * F); a.err_gam = a.L.take(N * F);
-    a.diag = a.L.take(N * F); a.cE = a.L.take(N * F); a.cS = a.L.take(N * F);
-    a.rhs = a.L.take(N * F); a.x = a.L.take(N * F); a.r = a.L.take(N * F);
+    a.dmass = a.L.take(N * F); a.cE = a.L.take(N * F); a.cS = a.L.take(N * F);
+    a.rhs = a.L.take(N * F); a.r0 = a.L.take(N * F); a.x = a.L.take(N * F); a.dx = a.L.take(N * F);
+    a.r = a.L.take(N * F);
     a.z = a.L.take(N * F); a.p = a.L.take(N * F); a.q = a.L.take(N * F);
     a.x64 = a.L.take(N * 8);
     a.partials = a.L.take((size_t)partials * 8);
@@ -162,8 +163,8 @@ ArenaPlan plan_arena(const SbGrid& g, int partials) {
 
 int validate(const sb_params* p) {
     if (!p) return fail(SB_ERR_INVALID, "null params");
-    if (!is_pow2(p->nTheta) || p->nTheta < 8 || p->nTheta > 8192)
-        return fail(SB_ERR_INVALID, "nTheta must be a power of two in [8, 8192]");
+    if (!is_pow2(p->nTheta) || p->nTheta < 8 || p->nTheta > 1024)
+        return fail(SB_ERR_INVALID, "nTheta must be a power of two in [8, 1024]");
     if (!(p->radius > 0) || !(p->H > 0) || !(p->Gamma_m > 0) || !(p->T > 0))
         return fail(SB_ERR_INVALID, "radius, H, Gamma_m and T must be positive");
     if (!(p->dt > 0)) return fail(SB_ERR_INVALID, "timePerStep must be positive");
@@ -281,8 +282,8 @@ size_t sb_bytes_required(const sb_params* p) {
     g.nP = 2 * p->nTheta;
     g.N = g.nT * g.nP;
     g.Nv = (g.nT - 1) * g.nP;
-    // partial slots: bounded by 6 per block of the cooperative solve
-    const int partials = 6 * ((g.N + 255) / 256);
+    // partial slots: 6 per block of the cooperative solve (blocks <= rows)
+    const int partials = 6 * g.nT;
     return plan_arena(g, partials).L.bytes;
 }
 
@@ -309,10 +310,10 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     b->solver.mode = p->solver_mode == 1 ? 0 : 1;
     b->solver.tol = p->solver_tol > 0 ? p->solver_tol : 1e-6;
     b->solver.max_iter = p->solver_max_iter > 0 ? p->solver_max_iter : 1000;
-    b->solver.precond = 0;
+    b->solver.precond = 1;
     b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
 
-    const int partials = 6 * ((g.N + 255) / 256);
+    const int partials = 6 * g.nT;
     ArenaPlan a = plan_arena(g, partials);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->arena, a.L.bytes);
@@ -346,8 +347,8 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.uair = F32(a.uair); f.vair = F32(a.vair);
     f.div = F32(a.div); f.d_eta = F32(a.d_eta); f.d_gam = F32(a.d_gam);
     f.err_eta = F32(a.err_eta); f.err_gam = F32(a.err_gam);
-    f.diag = F32(a.diag); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs);
-    f.x = F32(a.x); f.r = F32(a.r); f.z = F32(a.z); f.p = F32(a.p); f.q = F32(a.q);
+    f.dmass = F32(a.dmass); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs); f.r0 = F32(a.r0);
+    f.x = F32(a.x); f.dx = F32(a.dx); f.r = F32(a.r); f.z = F32(a.z); f.p = F32(a.p); f.q = F32(a.q);
     f.x64 = (double*)(A + a.x64);
     f.partials = (double*)(A + a.partials);
     f.step = (SbStepParams*)(A + a.step);
@@ -647,6 +648,13 @@ int sb_run(sb_bubble* b, const char* out_dir, int frames) {
         }
     }
     if (broken) return fail(SB_ERR_BROKEN, "film is broken");
+    return SB_OK;
+}
+
+int sb_write_exr_gray(const char* path, int width, int height, const float* img) {
+    if (!path || !img || width <= 0 || height <= 0) return fail(SB_ERR_INVALID, "bad image");
+    if (!write_exr_gray3(path, width, height, img))
+        return fail(SB_ERR_IO, std::string("cannot write ") + path);
     return SB_OK;
 }
 

@@ -18,8 +18,12 @@ struct SbFields {
     float *uair_init, *vair_init, *corr_u, *corr_v;
     float *uair, *vair;                            // N+1, Nv+1 (last element 0)
     float *div, *d_eta, *d_gam, *err_eta, *err_gam;
-    float *diag, *cE, *cS, *rhs;                   // implicit system
-    float *x, *r, *z, *p, *q;                      // solver vectors
+    // implicit system for the increment dx = gamma_new - gamma_adv:
+    // (A dx)_c = dmass_c dx_c + sum_n w_cn (dx_c - dx_n), weights w > 0 to
+    // the east (cE) and south (cS) neighbours; r = b - A gamma_adv formed
+    // analytically; rhs = b (for the norm only)
+    float *dmass, *cE, *cS, *rhs, *r0;
+    float *x, *dx, *r, *z, *p, *q;                 // solver vectors
     double *x64;                                   // mixed-precision iterate
     double *partials;                              // per-block reduction slots
     SbStepParams* step;                            // device copy of step scalars
@@ -30,7 +34,7 @@ struct SolverConfig {
     int mode;       // 0: plain FP32, 1: mixed precision (FP64 dots + refinement)
     int max_iter;
     double tol;     // relative residual ||b - A x|| / ||b||
-    int precond;    // 0: Jacobi
+    int precond;    // 0: Jacobi, 1: exact phi-line (periodic tridiagonal per row)
 };
 
 // Step stages (sb_step.cu).  `cur` selects the map ping-pong buffers.

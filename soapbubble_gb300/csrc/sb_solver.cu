@@ -1,17 +1,29 @@
 // Implicit surfactant solve: preconditioned conjugate gradients on the
-// symmetric 5-point system assembled by k_assemble.  It replaces the
-// reference's AmgX PCGF + AMG solve (kernel/bubble.cu:1479-1508,
-// init/PCGF_F.json); x0 is the current gamma, as in the reference.
+// symmetric positive definite 5-point system assembled by k_assemble.  It
+// replaces the reference's AmgX PCGF + AMG solve (kernel/bubble.cu:1479-1508,
+// init/PCGF_F.json).  The reference starts from x0 = gamma; here the unknown
+// is the increment dx = gamma_new - gamma_adv, starting from dx = 0, which is
+// the same iteration with the large common part removed.
 //
-// One cooperative launch runs the whole solve: every thread owns a strided
-// set of cells, phases are separated by grid-wide barriers, and the dot
-// products are reduced per block and then summed by every block in the same
-// block order, so all blocks see bit-identical scalars and take identical
-// loop decisions (the iteration count is bounded by max_iter).
+// One cooperative launch runs the whole solve.  Each block owns whole theta
+// rows; phases are separated by grid-wide barriers; dot products are summed
+// per block and then by every block in the same block order, so every block
+// sees bit-identical scalars and takes the same loop decisions (the
+// iteration count is bounded by max_iter).
 //
-// Modes: plain FP32 (FP32 vectors and per-thread sums), or mixed precision
-// (FP32 SpMV and preconditioner, FP64 iterate and dot products, and a true
-// FP64 residual check that restarts CG from the refined iterate until the
+// Preconditioner: exact solve of each theta row's periodic tridiagonal block
+// (phi couplings; the theta couplings stay on its diagonal).  Near the poles
+// the phi couplings carry 1/sin(theta) and dominate the diagonal by 1e4-1e5,
+// which is what makes point Jacobi slow there.  The row solve is parallel
+// cyclic reduction in shared memory, written in "excess" form: each equation
+// keeps (excess e, |lower|, |upper|, rhs) with diagonal = e + |lower| + |upper|,
+// and every update adds positive terms, so FP32 keeps full relative accuracy
+// even when the diagonal exceeds the off-diagonal sum by a factor 1 + 1e-5
+// (the Grassmann-Taksar-Heyman idea applied to cyclic reduction).
+//
+// Modes: plain FP32 (FP32 vectors and sums), or mixed precision (FP32 SpMV
+// and preconditioner, FP64 iterate and dot products, and a true FP64
+// residual check that restarts CG from the refined iterate until the
 // relative residual target holds).
 #include <cooperative_groups.h>
 
@@ -24,10 +36,6 @@ namespace sb {
 namespace {
 
 constexpr int kSolveBlock = 256;
-
-struct SolveCtx {
-    int G;  // blocks
-};
 
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -76,61 +84,127 @@ __device__ __forceinline__ void all_sum3(const double* part, int G, double& A, d
     __syncthreads();
 }
 
-template <typename T>
-__device__ __forceinline__ double spmv_at(const SbGrid& g, const SbFields& f, const T* __restrict__ v,
-                                          int c) {
-    const int i = c >> g.logP, j = c & g.maskP;
+// (A v)_c for a cell c = (i, j); T is float or double.
+template <typename T, typename A>
+__device__ __forceinline__ A apply_A(const SbGrid& g, const SbFields& f, const T* __restrict__ v,
+                                     int c, int i, int j) {
     const int nP = g.nP;
     const int e = i * nP + ((j + 1) & g.maskP);
     const int w = i * nP + ((j - 1) & g.maskP);
-    double s = (double)f.diag[c] * (double)v[c] + (double)f.cE[c] * (double)v[e] +
-               (double)f.cE[w] * (double)v[w];
-    if (i < g.nT - 1) s += (double)f.cS[c] * (double)v[c + nP];
-    if (i > 0) s += (double)f.cS[c - nP] * (double)v[c - nP];
+    const A vc = (A)v[c];
+    A s = (A)f.dmass[c] * vc + (A)f.cE[c] * (vc - (A)v[e]) + (A)f.cE[w] * (vc - (A)v[w]);
+    if (i < g.nT - 1) s += (A)f.cS[c] * (vc - (A)v[c + nP]);
+    if (i > 0) s += (A)f.cS[c - nP] * (vc - (A)v[c - nP]);
     return s;
 }
 
-__device__ __forceinline__ float spmv_f(const SbGrid& g, const SbFields& f, const float* __restrict__ v,
-                                        int c) {
-    const int i = c >> g.logP, j = c & g.maskP;
-    const int nP = g.nP;
-    const int e = i * nP + ((j + 1) & g.maskP);
-    const int w = i * nP + ((j - 1) & g.maskP);
-    float s = f.diag[c] * v[c] + f.cE[c] * v[e] + f.cE[w] * v[w];
-    if (i < g.nT - 1) s += f.cS[c] * v[c + nP];
-    if (i > 0) s += f.cS[c - nP] * v[c - nP];
-    return s;
+// z = M^-1 r on theta row i: Jacobi, or the exact periodic tridiagonal solve.
+// sm holds 4 * nP floats.  Returns partial sums of r.z and r.r for this row.
+template <bool MIXED>
+__device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f,
+                                                 const SolverConfig& cfg, int i, float* sm,
+                                                 double& rz, double& rr) {
+    const int nP = g.nP, nT = g.nT, mask = g.maskP;
+    const int row = i * nP;
+    if (cfg.precond == 0) {
+        for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+            const int c = row + j;
+            float dg = f.dmass[c] + f.cE[c] + f.cE[row + ((j - 1) & mask)];
+            if (i < nT - 1) dg += f.cS[c];
+            if (i > 0) dg += f.cS[c - nP];
+            const float rc = f.r[c];
+            const float zc = rc / dg;
+            f.z[c] = zc;
+            rz += MIXED ? (double)rc * (double)zc : (double)(rc * zc);
+            rr += MIXED ? (double)rc * (double)rc : (double)(rc * rc);
+        }
+        return;
+    }
+    float* E = sm;            // excess: diagonal minus the phi couplings
+    float* L = sm + nP;       // |coupling to j - s|
+    float* U = sm + 2 * nP;   // |coupling to j + s|
+    float* D = sm + 3 * nP;   // right-hand side
+    for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+        const int c = row + j;
+        float ex = f.dmass[c];
+        if (i < nT - 1) ex += f.cS[c];
+        if (i > 0) ex += f.cS[c - nP];
+        E[j] = ex;
+        U[j] = f.cE[c];
+        L[j] = f.cE[row + ((j - 1) & mask)];
+        D[j] = f.r[c];
+    }
+    __syncthreads();
+    // parallel cyclic reduction: after the step with stride s every
+    // equation couples j to j -/+ 2s (indices mod nP)
+    constexpr int kMaxPer = 8;  // nP <= kMaxPer * kSolveBlock
+    for (int s = 1; s <= nP / 4; s <<= 1) {
+        float nE[kMaxPer], nL[kMaxPer], nU[kMaxPer], nD[kMaxPer];
+#pragma unroll
+        for (int k = 0; k < kMaxPer; ++k) {
+            const int j = threadIdx.x + k * kSolveBlock;
+            if (j < nP) {
+                const int jm = (j - s) & mask, jp = (j + s) & mask;
+                const float bm = E[jm] + L[jm] + U[jm];
+                const float bp = E[jp] + L[jp] + U[jp];
+                const float am = L[j] / bm;
+                const float cp = U[j] / bp;
+                nE[k] = E[j] + am * E[jm] + cp * E[jp];
+                nL[k] = am * L[jm];
+                nU[k] = cp * U[jp];
+                nD[k] = D[j] + am * D[jm] + cp * D[jp];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kMaxPer; ++k) {
+            const int j = threadIdx.x + k * kSolveBlock;
+            if (j < nP) { E[j] = nE[k]; L[j] = nL[k]; U[j] = nU[k]; D[j] = nD[k]; }
+        }
+        __syncthreads();
+    }
+    // each equation now couples j with k = j + nP/2 only: 2x2 solves
+    for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+        const int k = (j + nP / 2) & mask;
+        const float mj = L[j] + U[j], mk = L[k] + U[k];
+        const float ej = E[j], ek = E[k];
+        const float det = ej * ek + ej * mk + mj * ek;
+        const float zj = (D[j] * (ek + mk) + mj * D[k]) / det;
+        const int c = row + j;
+        const float rc = f.r[c];
+        f.z[c] = zj;
+        rz += MIXED ? (double)rc * (double)zj : (double)(rc * zj);
+        rr += MIXED ? (double)rc * (double)rc : (double)(rc * rc);
+    }
+    __syncthreads();
 }
 
 template <bool MIXED>
 __global__ void __launch_bounds__(kSolveBlock)
 k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
+    extern __shared__ float sm[];
     cg::grid_group grid = cg::this_grid();
     const int G = gridDim.x;
-    const int stride = G * kSolveBlock;
-    const int t0 = blockIdx.x * kSolveBlock + threadIdx.x;
+    const int nP = g.nP, nT = g.nT;
     double* partA = f.partials;
     double* partB = f.partials + 3 * G;
-    const int N = g.N;
 
-    // r = b - A x0, z = M^-1 r, p = z
+    // dx = 0, r = r0 (assembled), z = M^-1 r, p = z
     double rz = 0, rr = 0, bb = 0;
     {
         double a = 0, b2 = 0, c2 = 0;
-        for (int c = t0; c < N; c += stride) {
-            const float x0 = f.gam_adv[c];
-            if (MIXED) f.x64[c] = (double)x0;
-            f.x[c] = x0;
-            const double b = (double)f.rhs[c];
-            const double r = b - spmv_at(g, f, f.gam_adv, c);
-            const float rf = (float)r;
-            const float zf = rf / f.diag[c];
-            f.r[c] = rf;
-            f.z[c] = zf;
-            f.p[c] = zf;
-            a += (double)rf * (double)zf;
-            b2 += r * r;
-            c2 += b * b;
+        for (int i = blockIdx.x; i < nT; i += G) {
+            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                const int c = i * nP + j;
+                if (MIXED) f.x64[c] = 0.0;
+                else f.dx[c] = 0.0f;
+                f.r[c] = f.r0[c];
+                const double b = (double)f.rhs[c];
+                c2 += b * b;
+            }
+            __syncthreads();
+            precondition_row<MIXED>(g, f, cfg, i, sm, a, b2);
+            for (int j = threadIdx.x; j < nP; j += blockDim.x) f.p[i * nP + j] = f.z[i * nP + j];
         }
         block_partial3(a, b2, c2, partA);
     }
@@ -146,15 +220,15 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
             if (!MIXED) { conv = true; break; }
             // true FP64 residual of the refined iterate; restart CG from it
             double a = 0, b2 = 0;
-            for (int c = t0; c < N; c += stride) {
-                const double r = (double)f.rhs[c] - spmv_at(g, f, f.x64, c);
-                const float rf = (float)r;
-                const float zf = rf / f.diag[c];
-                f.r[c] = rf;
-                f.z[c] = zf;
-                f.p[c] = zf;
-                a += (double)rf * (double)zf;
-                b2 += r * r;
+            for (int i = blockIdx.x; i < nT; i += G) {
+                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                    const int c = i * nP + j;
+                    const double r = (double)f.r0[c] - apply_A<double, double>(g, f, f.x64, c, i, j);
+                    f.r[c] = (float)r;
+                }
+                __syncthreads();
+                precondition_row<MIXED>(g, f, cfg, i, sm, a, b2);
+                for (int j = threadIdx.x; j < nP; j += blockDim.x) f.p[i * nP + j] = f.z[i * nP + j];
             }
             block_partial3(a, b2, 0.0, partB);
             grid.sync();
@@ -165,11 +239,13 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
         // q = A p, <p, q>
         {
             double pq = 0;
-            for (int c = t0; c < N; c += stride) {
-                const float qf = spmv_f(g, f, f.p, c);
-                f.q[c] = qf;
-                pq += MIXED ? (double)f.p[c] * (double)qf : (double)(f.p[c] * qf);
-            }
+            for (int i = blockIdx.x; i < nT; i += G)
+                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                    const int c = i * nP + j;
+                    const float qf = apply_A<float, float>(g, f, f.p, c, i, j);
+                    f.q[c] = qf;
+                    pq += MIXED ? (double)f.p[c] * (double)qf : (double)(f.p[c] * qf);
+                }
             block_partial3(pq, 0.0, 0.0, partA);
         }
         grid.sync();
@@ -179,16 +255,16 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
         const double alpha = rz / pq;
         const float af = (float)alpha;
         double rz2 = 0, rr2 = 0;
-        for (int c = t0; c < N; c += stride) {
-            const float pc = f.p[c];
-            if (MIXED) f.x64[c] += alpha * (double)pc;
-            else f.x[c] += af * pc;
-            const float rf = f.r[c] - af * f.q[c];
-            const float zf = rf / f.diag[c];
-            f.r[c] = rf;
-            f.z[c] = zf;
-            rz2 += MIXED ? (double)rf * (double)zf : (double)(rf * zf);
-            rr2 += MIXED ? (double)rf * (double)rf : (double)(rf * rf);
+        for (int i = blockIdx.x; i < nT; i += G) {
+            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                const int c = i * nP + j;
+                const float pc = f.p[c];
+                if (MIXED) f.x64[c] += alpha * (double)pc;
+                else f.dx[c] += af * pc;
+                f.r[c] = f.r[c] - af * f.q[c];
+            }
+            __syncthreads();
+            precondition_row<MIXED>(g, f, cfg, i, sm, rz2, rr2);
         }
         block_partial3(rz2, rr2, 0.0, partB);
         grid.sync();
@@ -197,20 +273,35 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
         const float bf = (float)(rz2 / rz);
         rz = rz2;
         rr = rr2;
-        for (int c = t0; c < N; c += stride) f.p[c] = f.z[c] + bf * f.p[c];
+        for (int i = blockIdx.x; i < nT; i += G)
+            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                const int c = i * nP + j;
+                f.p[c] = f.z[c] + bf * f.p[c];
+            }
         grid.sync();
         ++it;
     }
-    // final iterate and its true relative residual
-    if (MIXED)
-        for (int c = t0; c < N; c += stride) f.x[c] = (float)f.x64[c];
+    // final increment, new gamma, and the true relative residual of the
+    // returned (FP32) gamma
+    for (int i = blockIdx.x; i < nT; i += G)
+        for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+            const int c = i * nP + j;
+            const float dx = MIXED ? (float)f.x64[c] : f.dx[c];
+            const float g0 = f.gam_adv[c];
+            const float xn = g0 + dx;
+            f.dx[c] = dx;
+            f.x[c] = xn;
+            f.q[c] = xn - g0;  // stored increment, exact in FP32
+        }
     grid.sync();
     {
         double a = 0;
-        for (int c = t0; c < N; c += stride) {
-            const double r = (double)f.rhs[c] - spmv_at(g, f, f.x, c);
-            a += r * r;
-        }
+        for (int i = blockIdx.x; i < nT; i += G)
+            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                const int c = i * nP + j;
+                const double r = (double)f.r0[c] - apply_A<float, double>(g, f, f.q, c, i, j);
+                a += r * r;
+            }
         block_partial3(a, 0.0, 0.0, partA);
     }
     grid.sync();
@@ -224,22 +315,28 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
     }
 }
 
-int g_blocks_cache_n = -1;
-int g_blocks_cache_val = 0;
+struct Occ {
+    int sms = 0;
+    int blocks = 0;
+    int nP = -1;
+};
 
 int solve_blocks(const SbGrid& g) {
-    static int sms = 0, occ[2] = {0, 0};
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_pcg<false>, kSolveBlock, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_pcg<true>, kSolveBlock, 0);
+    static Occ cache[16];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    Occ& o = cache[dev & 15];
+    if (o.nP != g.nP) {
+        cudaDeviceGetAttribute(&o.sms, cudaDevAttrMultiProcessorCount, dev);
+        const size_t smem = 4 * sizeof(float) * (size_t)g.nP;
+        int a = 0, b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pcg<false>, kSolveBlock, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pcg<true>, kSolveBlock, smem);
+        o.blocks = o.sms * (a < b ? a : b);
+        o.nP = g.nP;
     }
-    const int per = occ[0] < occ[1] ? occ[0] : occ[1];
-    int maxb = sms * (per > 0 ? per : 1);
-    int need = (g.N + kSolveBlock - 1) / kSolveBlock;
-    return need < maxb ? need : maxb;
+    const int b = o.blocks > 0 ? o.blocks : 1;
+    return g.nT < b ? g.nT : b;
 }
 
 }  // namespace
@@ -249,16 +346,19 @@ int solver_partials_needed(const SbGrid& g) { return 6 * solve_blocks(g); }
 cudaError_t launch_solve(const SbGrid& g, const SbPhys& ph, const SbFields& f,
                          const SolverConfig& cfg, cudaStream_t s) {
     (void)ph;
+    if (g.nP > 8 * kSolveBlock) return cudaErrorInvalidValue;
     const int G = solve_blocks(g);
+    const size_t smem = 4 * sizeof(float) * (size_t)g.nP;
     SbGrid gg = g;
     SbFields ff = f;
     SolverConfig cc = cfg;
     void* args[] = {&gg, &ff, &cc};
-    if (cfg.mode == 1)
-        return cudaLaunchCooperativeKernel((const void*)k_pcg<true>, dim3(G), dim3(kSolveBlock),
-                                           args, 0, s);
-    return cudaLaunchCooperativeKernel((const void*)k_pcg<false>, dim3(G), dim3(kSolveBlock), args,
-                                       0, s);
+    const void* fn = cfg.mode == 1 ? (const void*)k_pcg<true> : (const void*)k_pcg<false>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kSolveBlock), args, smem, s);
 }
 
 }  // namespace sb

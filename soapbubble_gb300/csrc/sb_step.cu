@@ -167,12 +167,19 @@ __device__ __forceinline__ bool is_broken(float gamma, float eta, float gmax) {
     return gamma > gmax - kEps || eta == 0.0f;
 }
 
-// Implicit surfactant system (paper eq. 26) in symmetric 5-point form:
-// diag, coupling to the east neighbour (cE) and to the south neighbour (cS).
-// The reference's couplings across the poles carry sin(0) and sin(pi) and
-// are zero.  A broken cell (gamma at its maximum or no film) is an identity
-// row with value gmax; its couplings are moved to the neighbours'
-// right-hand sides so that the matrix stays symmetric positive definite.
+// Implicit surfactant system (paper eq. 26), assembled for the increment
+// dx = gamma_new - gamma_adv so that FP32 keeps its precision:
+//   (A dx)_c = dmass_c dx_c + sum_n w_cn (dx_c - dx_n)
+// with dmass = sin(theta) / (dt gamma) and the positive couplings w_cn (the
+// reference's off-diagonals with the sign flipped; its diagonal is dmass +
+// sum w).  The right-hand side r = b - A gamma_adv is formed analytically:
+// dmass gamma = sin(theta) / dt cancels the leading term of b, leaving
+// r = -sinThetaDiv - sum w (gamma_c - gamma_n).  The couplings across the
+// poles carry sin(0) and sin(pi) and vanish.  A broken cell (gamma at its
+// maximum or no film) keeps gamma = gmax: its row is dx = 0 and the weight
+// of its couplings moves into the neighbours' dmass, which keeps A
+// symmetric positive definite with the same solution as the reference's
+// identity row.
 __global__ void __launch_bounds__(kBlock)
 k_assemble(SbGrid g, SbPhys ph, SbFields f) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -188,9 +195,10 @@ k_assemble(SbGrid g, SbPhys ph, SbFields f) {
     const int jE = (j + 1) & g.maskP, jW = (j - 1) & g.maskP;
     const int iE = i * nP + jE, iW = i * nP + jW;
     if (is_broken(gamma, eta, gmax)) {
-        f.diag[idx] = 1.0f;
+        f.dmass[idx] = 1.0f;
         f.cE[idx] = 0.0f;
         f.cS[idx] = 0.0f;
+        f.r0[idx] = 0.0f;
         f.rhs[idx] = gmax;
         f.gam_adv[idx] = gmax;
         atomicAdd(&f.stats->broken_cells, 1);
@@ -234,11 +242,10 @@ k_assemble(SbGrid g, SbPhys ph, SbFields f) {
     const float etaLeft = (etaW + eta) * 0.5f;
     const float etaRight = (etaE + eta) * 0.5f;
     const float etaDown = (etaS + eta) * 0.5f;
-    const float up = (i == 0) ? 0.0f : -s2 * sinN * MDt / (etaUp + CrDt);
-    const float left = -s2 * cscT * MDt / (etaLeft + CrDt);
-    const float right = -s2 * cscT * MDt / (etaRight + CrDt);
-    const float down = (i == nT - 1) ? 0.0f : -s2 * sinS * MDt / (etaDown + CrDt);
-    const float diag = sinT * invDt / gamma - (up + left + right + down);
+    const float wN = (i == 0) ? 0.0f : s2 * sinN * MDt / (etaUp + CrDt);
+    const float wW = s2 * cscT * MDt / (etaLeft + CrDt);
+    const float wE = s2 * cscT * MDt / (etaRight + CrDt);
+    const float wS = (i == nT - 1) ? 0.0f : s2 * sinS * MDt / (etaDown + CrDt);
 
     float sinThetaDiv = g.invh * (uE * etaRight / (etaRight + CrDt) - uW * etaLeft / (etaLeft + CrDt) +
                                   (vS * sinS * etaDown / (etaDown + CrDt) -
@@ -250,33 +257,54 @@ k_assemble(SbGrid g, SbPhys ph, SbFields f) {
     sinThetaDiv += ph.gs * g.invh *
                    (sinS * sinS * etaDown / (invDt * etaDown + Cr) -
                     sinN * sinN * etaUp / (invDt * etaUp + Cr));
-    float rhs = sinT * invDt - sinThetaDiv;
 
-    // eliminate couplings to broken neighbours (their value is gmax)
-    const bool bE = is_broken(f.gam_adv[iE], etaE, gmax);
-    const bool bW = is_broken(f.gam_adv[iW], etaW, gmax);
-    if (bE) rhs -= right * gmax;
-    if (bW) rhs -= left * gmax;
-    bool bS = false;
-    if (i != 0 && is_broken(f.gam_adv[idx - nP], etaN, gmax)) rhs -= up * gmax;
-    if (i != nT - 1) {
-        bS = is_broken(f.gam_adv[idx + nP], etaS, gmax);
-        if (bS) rhs -= down * gmax;
+    // neighbour gamma (a broken neighbour holds gmax) and broken flags
+    const float gEr = f.gam_adv[iE], gWr = f.gam_adv[iW];
+    const bool bE = is_broken(gEr, etaE, gmax), bW = is_broken(gWr, etaW, gmax);
+    const float gE = bE ? gmax : gEr, gW = bW ? gmax : gWr;
+    bool bN = false, bS = false;
+    float gN = gamma, gS = gamma;
+    if (i != 0) {
+        const float gr = f.gam_adv[idx - nP];
+        bN = is_broken(gr, etaN, gmax);
+        gN = bN ? gmax : gr;
     }
-    f.diag[idx] = diag;
-    f.cE[idx] = bE ? 0.0f : right;
-    f.cS[idx] = bS ? 0.0f : down;
-    f.rhs[idx] = rhs;
-}
-
-__device__ __forceinline__ float clamp_gamma(float gm, float gmax) {
-    return (gm <= 0.0f || gm > gmax - kEps) ? gmax : gm;
+    if (i != nT - 1) {
+        const float gr = f.gam_adv[idx + nP];
+        bS = is_broken(gr, etaS, gmax);
+        gS = bS ? gmax : gr;
+    }
+    const float lap = wE * (gamma - gE) + wW * (gamma - gW) + wN * (gamma - gN) + wS * (gamma - gS);
+    float dmass = sinT * invDt / gamma;
+    if (bE) dmass += wE;
+    if (bW) dmass += wW;
+    if (bN) dmass += wN;
+    if (bS) dmass += wS;
+    f.dmass[idx] = dmass;
+    f.cE[idx] = bE ? 0.0f : wE;
+    f.cS[idx] = bS ? 0.0f : wS;
+    f.r0[idx] = -sinThetaDiv - lap;
+    f.rhs[idx] = sinT * invDt - sinThetaDiv;
 }
 
 // After the solve: divergence from gamma, friction/Marangoni/gravity velocity
 // update, thickness update with evaporation, and the per-step changes that
-// BIMOCQ accumulates.  Neighbouring new gamma values are clamped on the fly
-// exactly as divergenceKernel_fromGamma clamps them in place.
+// BIMOCQ accumulates.  Increments are carried directly (dx from the solve,
+// d_eta = -eta dt div + evap dt) instead of as differences of O(1) values.
+// Neighbouring new gamma values are clamped on the fly exactly as
+// divergenceKernel_fromGamma clamps them in place.
+__device__ __forceinline__ bool gamma_clamped(float gm, float gmax) {
+    return gm <= 0.0f || gm > gmax - kEps;
+}
+
+// Difference gamma_new(a) - gamma_new(b) of two cells.
+__device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, float gmax) {
+    const float xa = f.x[a], xb = f.x[b];
+    const bool ca = gamma_clamped(xa, gmax), cb = gamma_clamped(xb, gmax);
+    if (!ca && !cb) return (f.gam_adv[a] - f.gam_adv[b]) + (f.dx[a] - f.dx[b]);
+    return (ca ? gmax : xa) - (cb ? gmax : xb);
+}
+
 __global__ void __launch_bounds__(kBlock)
 k_post(SbGrid g, SbPhys ph, SbFields f) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -287,36 +315,40 @@ k_post(SbGrid g, SbPhys ph, SbFields f) {
     const float gmax = ph.gmax, M = ph.M, Cr = ph.Cr;
     const float gOld = f.gam_adv[idx];
     const float gNew = f.x[idx];
-    float div, gFin;
-    if (gNew <= 0.0f || gNew > gmax - kEps) {
-        gFin = gmax;
-        div = invDt;
+    float mdtdiv;  // -dt * div
+    if (gamma_clamped(gNew, gmax)) {
+        f.gam[idx] = gmax;
+        f.d_gam[idx] = gmax - gOld;
+        mdtdiv = -1.0f;
     } else {
-        gFin = gNew;
-        div = (1.0f - fminf(gNew, 2.0f * gOld) / gOld) / dt;
+        const float dx = f.dx[idx];
+        f.gam[idx] = gNew;
+        f.d_gam[idx] = dx;
+        // div = (1 - min(gNew, 2 gOld) / gOld) / dt
+        mdtdiv = (gNew > 2.0f * gOld) ? 1.0f : dx / gOld;
     }
-    f.gam[idx] = gFin;
-    f.d_gam[idx] = gFin - gOld;
 
     const float e = f.eta_adv[idx];
-    float eo = e * (1.0f - dt * div);
-    eo += f.step->evapDt;
-    eo = fmaxf(0.0f, eo);
-    f.eta[idx] = eo;
-    f.d_eta[idx] = eo - e;
+    const float de = e * mdtdiv + f.step->evapDt;
+    if (e + de >= 0.0f) {
+        f.eta[idx] = e + de;
+        f.d_eta[idx] = de;
+    } else {
+        f.eta[idx] = 0.0f;
+        f.d_eta[idx] = -e;
+    }
 
     // u_phi face between (i, j-1) and (i, j)
     {
         const int w = i * nP + ((j - 1) & g.maskP);
         const float etaW = f.eta_adv[w];
-        const float gW = clamp_gamma(f.x[w], gmax);
         const float invEta = 2.0f / (etaW + e);
         const float u1 = f.uph_adv[idx];
         if (isinf(invEta)) {
             f.uph[idx] = __int_as_float(0x7fffffff);
         } else {
             const float cscT = 1.0f / g.sin_c[i];
-            const float pGpx = g.invh * (gFin - gW) * cscT;
+            const float pGpx = g.invh * gnew_diff(f, idx, w, gmax) * cscT;
             const float f1 = -M * invEta * pGpx;
             const float f2 = Cr * invEta * f.uair[idx];
             f.uph[idx] = (u1 * invDt + f1 + f2) / (invDt + Cr * invEta);
@@ -326,13 +358,12 @@ k_post(SbGrid g, SbPhys ph, SbFields f) {
     if (i < g.nT - 1) {
         const int s = idx + nP;
         const float etaS = f.eta_adv[s];
-        const float gS = clamp_gamma(f.x[s], gmax);
         const float invEta = 2.0f / (e + etaS);
         const float v1 = f.uth_adv[idx];
         if (isinf(invEta)) {
             f.uth[idx] = __int_as_float(0x7fffffff);
         } else {
-            const float pGpy = g.invh * (gS - gFin);
+            const float pGpy = g.invh * gnew_diff(f, s, idx, gmax);
             const float f1 = -M * invEta * pGpy;
             const float f2 = Cr * invEta * f.vair[idx];
             const float f3v = ph.gs * g.sin_e[i + 1];

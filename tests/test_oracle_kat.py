@@ -1,0 +1,228 @@
+"""Known-answer tests that pin the FP64 oracle (CPU only).
+
+The reference ships no tests or golden vectors and cannot be built here
+(AmgX, Boost, OpenCV are absent), so the oracle's restatement of
+kernel/bubble.cu is pinned by cases whose answers follow from the
+mathematics: exact grid-point sampling, pole reflection weights, a
+zero-velocity trace, an exact great-circle trace along the equator, an
+identity-map lookup, the invariance of a uniform film without gravity or
+wind, the structure of the implicit system, and the solve residual.
+"""
+import numpy as np
+import pytest
+
+nT = 16
+nP = 32
+
+
+@pytest.fixture(scope="module")
+def P(oracle):
+    p = oracle.default_params(nT, radius=1.0, dt_s=0.005)
+    return p
+
+
+def rng(seed=0):
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def test_centred_sampler_grid_points(oracle, P):
+    f = rng(1).standard_normal((nT, nP))
+    ii, jj = np.meshgrid(np.arange(nT), np.arange(nP), indexing="ij")
+    coords = np.stack([ii.ravel() + 0.5, jj.ravel() + 0.0], axis=1)
+    out = oracle.sample(P, 0, f, coords)
+    np.testing.assert_allclose(out, f.ravel(), rtol=0, atol=1e-14)
+
+
+def test_face_samplers_grid_points(oracle, P):
+    up = rng(2).standard_normal((nT, nP))
+    ut = rng(3).standard_normal((nT - 1, nP))
+    ii, jj = np.meshgrid(np.arange(nT), np.arange(nP), indexing="ij")
+    c = np.stack([ii.ravel() + 0.5, jj.ravel() - 0.5], axis=1)
+    np.testing.assert_allclose(oracle.sample(P, 1, up, c), up.ravel(), atol=1e-14)
+    ii, jj = np.meshgrid(np.arange(nT - 1), np.arange(nP), indexing="ij")
+    c = np.stack([ii.ravel() + 1.0, jj.ravel() + 0.0], axis=1)
+    np.testing.assert_allclose(oracle.sample(P, 2, ut, c), ut.ravel(), atol=1e-14)
+
+
+def test_samplers_across_north_pole(oracle, P):
+    """Between a pole row and its reflection: scalar weights, vector sign flip."""
+    f = rng(4).standard_normal((nT, nP))
+    up = rng(5).standard_normal((nT, nP))
+    ut = rng(6).standard_normal((nT - 1, nP))
+    j = 5
+    # scalar at raw theta 0.25: 3/4 of row 0, 1/4 of row 0 across the pole
+    s = oracle.sample(P, 0, f, np.array([[0.25, j]]))[0]
+    assert s == pytest.approx(0.75 * f[0, j] + 0.25 * f[0, j + nT], abs=1e-13)
+    # u_phi at raw (0.25, j - 0.5): the reflected component changes sign
+    s = oracle.sample(P, 1, up, np.array([[0.25, j - 0.5]]))[0]
+    assert s == pytest.approx(0.75 * up[0, j] - 0.25 * up[0, j + nT], abs=1e-13)
+    # u_theta at raw 0.5: rows at raw 1 and -1 (reflection), weights 3/4, 1/4
+    s = oracle.sample(P, 2, ut, np.array([[0.5, j]]))[0]
+    assert s == pytest.approx(0.75 * ut[0, j] - 0.25 * ut[0, j + nT], abs=1e-13)
+
+
+def test_samplers_across_south_pole(oracle, P):
+    f = rng(7).standard_normal((nT, nP))
+    ut = rng(8).standard_normal((nT - 1, nP))
+    j = 3
+    s = oracle.sample(P, 0, f, np.array([[nT - 0.25, j]]))[0]
+    assert s == pytest.approx(0.75 * f[nT - 1, j] + 0.25 * f[nT - 1, j + nT], abs=1e-13)
+    s = oracle.sample(P, 2, ut, np.array([[nT - 0.5, j]]))[0]
+    assert s == pytest.approx(0.75 * ut[nT - 2, j] - 0.25 * ut[nT - 2, j + nT], abs=1e-13)
+
+
+def test_phi_wrap(oracle, P):
+    f = rng(9).standard_normal((nT, nP))
+    i = 7
+    s = oracle.sample(P, 0, f, np.array([[i + 0.5, nP - 0.5]]))[0]
+    assert s == pytest.approx(0.5 * f[i, nP - 1] + 0.5 * f[i, 0], abs=1e-13)
+
+
+def test_trace_zero_velocity_is_identity(oracle, P):
+    ut, up = np.zeros((nT - 1, nP)), np.zeros((nT, nP))
+    c = np.array([[3.5, 4.0], [0.5, 1.0], [nT - 0.5, 7.0]])
+    np.testing.assert_array_equal(oracle.trace(P, ut, up, 0.01, c), c)
+
+
+def test_trace_along_equator_is_exact(oracle, P):
+    """Uniform u_phi = c, u_theta = 0: the equator is a great circle, so the
+    RK2 great-circle trace moves exactly c*dt backward along it."""
+    cvel, dt = 0.7, 0.05
+    ut, up = np.zeros((nT - 1, nP)), np.full((nT, nP), cvel)
+    h = np.pi / nT
+    c = np.array([[nT / 2, 5.0], [nT / 2, 11.3]])
+    out = oracle.trace(P, ut, up, dt, c)
+    np.testing.assert_allclose(out[:, 0], nT / 2, atol=1e-12)
+    np.testing.assert_allclose(out[:, 1], c[:, 1] - cvel * dt / h, atol=1e-11)
+
+
+def test_identity_map_lookup(oracle, P):
+    mt, mp = oracle.identity_map(nT)
+    ii, jj = np.meshgrid(np.arange(nT), np.arange(nP), indexing="ij")
+    c = np.stack([ii.ravel() + 0.5, jj.ravel() + 0.0], axis=1)
+    out = oracle.sample_mapping(P, mt, mp, c)
+    np.testing.assert_allclose(out[:, 0], c[:, 0], atol=1e-10)
+    dphi = np.mod(out[:, 1] - c[:, 1] + nT, nP) - nT
+    np.testing.assert_allclose(dphi, 0, atol=1e-10)
+
+
+def _uniform_bubble(oracle, gs_zero=True, eta=0.8, gamma=1.3):
+    p = oracle.default_params(nT, radius=1.0, dt_s=0.005)
+    if gs_zero:
+        p.gs = 0.0
+    p.t = 0.0  # corridor factor 3 - |t - 3| vanishes
+    z = np.zeros((nT, nP))
+    return oracle.OracleBubble(p, np.full((nT, nP), eta), np.full((nT, nP), gamma),
+                               np.zeros((nT - 1, nP)), z, z, np.zeros((nT - 1, nP)))
+
+
+def test_uniform_film_without_forcing_is_steady(oracle):
+    """No gravity, no wind, uniform eta and gamma: only evaporation acts."""
+    b = _uniform_bubble(oracle)
+    st = b.step()
+    eta_expect = 0.8 + b.p.evapRate * b.p.dt
+    np.testing.assert_allclose(b.a["eta"], eta_expect, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(b.a["gamma"], 1.3, rtol=0, atol=1e-11)
+    np.testing.assert_allclose(b.a["uth"], 0, atol=1e-11)
+    np.testing.assert_allclose(b.a["uph"], 0, atol=1e-11)
+    assert st.reinit == 0
+
+
+def test_gravity_drives_u_theta_only(oracle):
+    b = _uniform_bubble(oracle, gs_zero=False)
+    b.step()
+    assert np.max(np.abs(b.a["uth"])) > 1e-3
+    # the flow is zonally symmetric: every column identical
+    np.testing.assert_allclose(b.a["uth"], b.a["uth"][:, :1].repeat(nP, 1), atol=1e-12)
+    np.testing.assert_allclose(b.a["uph"], 0, atol=1e-10)
+
+
+def _matrix(oracle, seed=11):
+    from soapbubble_gb300 import synth
+    f = synth.make_fields("c0", nT, seed)
+    p = oracle.default_params(nT, radius=1.0, dt_s=0.005)
+    p.t = 1.5
+    up = rng(seed).standard_normal((nT, nP)) * 0.1
+    ut = rng(seed + 1).standard_normal((nT - 1, nP)) * 0.1
+    b = oracle.OracleBubble(p, f.eta, f.gamma, ut, up, f.uair_init, f.vair_init)
+    return b, b.assemble()
+
+
+def _col(idx, k):
+    if k == 0:
+        return (idx + nT) % nP if idx < nP else idx - nP
+    if k == 1:
+        return idx + nP - 1 if idx % nP == 0 else idx - 1
+    if k == 2:
+        return idx
+    if k == 3:
+        return idx - nP + 1 if idx % nP == nP - 1 else idx + 1
+    if idx >= (nT - 1) * nP + nT:
+        return idx - nT
+    if idx >= (nT - 1) * nP:
+        return idx + nT
+    return idx + nP
+
+
+def test_system_symmetric_and_dominant(oracle):
+    b, sysm = _matrix(oracle)
+    val = sysm["val"]
+    N = nT * nP
+    A = np.zeros((N, N))
+    for i in range(N):
+        for k in range(5):
+            A[i, _col(i, k)] += val[i, k]
+    np.testing.assert_allclose(A, A.T, rtol=0, atol=1e-9 * np.max(np.abs(A)))
+    off = np.abs(A - np.diag(np.diag(A))).sum(1)
+    assert np.all(np.diag(A) > off)
+    # pole couplings carry sin(0) / sin(pi)
+    assert np.all(np.abs(val[:nP, 0]) == 0)
+    assert np.all(np.abs(val[-nP:, 4]) < 1e-12 * np.max(np.abs(val)))
+
+
+def test_solve_matches_direct(oracle):
+    b, sysm = _matrix(oracle, seed=12)
+    N = nT * nP
+    A = np.zeros((N, N))
+    for i in range(N):
+        for k in range(5):
+            A[i, _col(i, k)] += sysm["val"][i, k]
+    x_direct = np.linalg.solve(A, sysm["rhs"])
+    x, it, rel = b.solve(sysm["val"], sysm["rhs"], sysm["gamma"])
+    assert rel < 1e-12
+    np.testing.assert_allclose(x, x_direct, rtol=0, atol=1e-11)
+
+
+def test_strict_mode_close_to_fp64(oracle):
+    """The reference's float intrinsics move the step by far less than 1e-5."""
+    from soapbubble_gb300 import synth
+    f = synth.make_fields("c0", nT, 5)
+    outs = []
+    for strict in (0, 1):
+        p = oracle.default_params(nT, radius=1.0, dt_s=0.005)
+        p.strict = strict
+        p.t = 1.0
+        b = oracle.OracleBubble(p, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+        for _ in range(3):
+            b.step()
+        outs.append(b)
+    for k in ("eta", "gamma", "uth", "uph"):
+        ref = outs[0].a[k]
+        err = np.max(np.abs(outs[1].a[k] - ref)) / np.max(np.abs(ref))
+        assert err < 1e-5, (k, err)
+
+
+def test_forced_reinit_resets_maps(oracle):
+    from soapbubble_gb300 import synth
+    f = synth.make_fields("c0", nT, 6)
+    p = oracle.default_params(nT, radius=1.0, dt_s=0.005)
+    p.force_reinit = 1
+    b = oracle.OracleBubble(p, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    b.step()
+    b.step()
+    mt, mp = oracle.identity_map(nT)
+    np.testing.assert_array_equal(b.a["fwd_t"], mt)
+    np.testing.assert_array_equal(b.a["bwd_p"], mp)
+    np.testing.assert_array_equal(b.a["eta_init"], b.a["eta"])
+    assert np.all(b.a["eta_delta"] == 0)
+    assert b.stats.reinit == 1
