@@ -1,0 +1,354 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 soap-bubble time step.
+
+Workload (config c1): one bubble on the 512 x 1024 lat-long MAC grid,
+radius 1, dt = 0.002 s, seeded thickness 1 + 0.2 SH(8..32), surfactant
+1 + 0.01 U(-1,1), stream-function wind of max speed 1, velocities from zero,
+mixed-precision PCG to relative residual 1e-6.  A step is one full time
+step (Solver::stepForward of the reference).  Frames last 10 steps (t is the
+frame start time, as in the reference's frame loop).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  value = cell-steps/s over all ranks with the
+state resident in HBM (device time from CUDA events around every step, L2
+flushed between steps); e2e = the same metric through the C ABI with the
+step's wind forcing uploaded from pinned host memory and the thickness field
+read back every step.  With N > 1 every rank steps its own independent
+replica (the single-bubble step does not shard).
+
+--impl reference times the CPU restatement of the reference step (the FP64
+oracle, all host threads) on the same workload: the reference itself needs
+AmgX, Boost and OpenCV and cannot be built here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s on 1 GB300 (plain vs batched mixed-prec @1e-6); p50/p99 latency"
+UNIT = "cell-steps/s"
+NTHETA, DT, RECIPE, SEED = 512, 0.002, "c1", 20261203
+STEPS_PER_FRAME = 10
+L2_FLUSH_BYTES = 512 << 20
+
+# Algorithmic bytes per cell and launch (FP32 = 4 B, map entry = 8 B; every
+# array a kernel must read or write counted once; halo re-reads excluded).
+ALG_BYTES_PER_CELL = {
+    "k_advect_maps": 72,  # u_th,u_ph,fwd,bwd,gamma,uair0,corr_u,vair0,corr_v -> fwd',bwd',gamma',uair,vair
+    "k_velocity": 16,     # u_th,u_ph -> u_th',u_ph'
+    "k_bimocq": 40,       # eta,bwd',bwdprev,init,delta,initLast,deltaLast -> eta'
+    "k_assemble": 44,     # eta',gamma',u_th',u_ph',uair,vair -> dmass,cE,cS,r0,b
+    "k_post": 56,         # gamma',x,dx,eta',u_th',u_ph',uair,vair -> gamma,dgamma,eta,deta,u_th,u_ph
+    "k_accum": 40,        # eta_delta,gamma_delta,fwd',bwd',deta,dgamma -> eta_delta,gamma_delta
+    "k_reinit1": 0, "k_reinit2": 0, "k_reinit3": 0,  # no traffic unless re-initialising
+}
+PCG_BYTES_FIXED, PCG_BYTES_PER_ITER = 84, 80
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic_c1.json")
+    if os.path.exists(path):
+        return json.load(open(path))
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(x: float, dist) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_config(extra=None):
+    c = {"workload": "c1: single bubble, lat-long MAC grid 512 x 1024, radius 1, dt 0.002 s, "
+                     "thickness 1+0.2*SH(8..32), surfactant 1+0.01*U(-1,1), wind max speed 1, "
+                     "mixed-precision PCG to relative residual 1e-6",
+         "nTheta": NTHETA, "nPhi": 2 * NTHETA, "cells": NTHETA * 2 * NTHETA, "dt": DT,
+         "steps_per_frame": STEPS_PER_FRAME, "solver": "mixed FP32/FP64 PCG, phi-line preconditioner",
+         "solver_tol": 1e-6, "seed": SEED,
+         "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); state ~105 MB"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def cpu_oracle_rate(target_s: float, nthreads: int, max_steps: int = 1000):
+    """FP64 oracle (CPU restatement of the reference step) on the same
+    workload: cell-steps/s over a bounded number of steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    from soapbubble_gb300 import synth
+    po.build()
+    f = synth.make_fields(RECIPE, NTHETA, SEED)
+    p = po.default_params(NTHETA, dt_s=DT)
+    p.solver_tol = 1e-6
+    p.nthreads = nthreads
+    ob = po.OracleBubble(p, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    t0 = time.perf_counter()
+    ob.step()  # first step: estimates the cost
+    first = time.perf_counter() - t0
+    n = max(1, min(max_steps, int(target_s / max(first, 1e-3))))
+    t0 = time.perf_counter()
+    for k in range(n):
+        ob.p.t = ((k + 1) // STEPS_PER_FRAME) * STEPS_PER_FRAME * DT
+        ob.step()
+    el = time.perf_counter() - t0
+    cells = NTHETA * 2 * NTHETA
+    return cells * n / el, n, el
+
+
+def run_reference(args):
+    world, rank, _, dist = dist_setup()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    rate, n, el = cpu_oracle_rate(target_s=min(120.0, 20.0 + 2.0 * args.steps), nthreads=threads,
+                                  max_steps=max(1, args.steps))
+    line = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": n,
+        "requested_steps": args.steps, "warmup": 1, "ms_per_step": 1e3 * el / n,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(), "impl": "reference",
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} steps of the 512x1024 workload after 1 warm-up step, "
+                                   f"FP64 oracle, OpenMP {threads} threads (the reference needs "
+                                   "AmgX/Boost/OpenCV and cannot be built)"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    world, rank, local, dist = dist_setup()
+    from soapbubble_gb300 import build, cudart, synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params, stage_names
+    build.build()
+    cudart.set_device(local)
+    names = stage_names()
+    nst = len(names)
+    f = synth.make_fields(RECIPE, NTHETA, SEED + rank)
+    gb = GpuBubble(make_params(NTHETA, DT, solver_tol=1e-6, solver_mode=0, device=local))
+    gb.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    stream = gb.stream()
+    flush = cudart.DeviceBuffer(L2_FLUSH_BYTES)
+    N = NTHETA * 2 * NTHETA
+    Nv = (NTHETA - 1) * 2 * NTHETA
+
+    def t_of(k):
+        return (k // STEPS_PER_FRAME) * STEPS_PER_FRAME * DT
+
+    for k in range(args.warmup):
+        gb.step(1, t_of(k), DT)
+    gb.synchronize()
+    k0 = args.warmup
+    launches0 = gb.stats().launches
+    stage_ms = np.zeros(nst)
+    iters = []
+    barrier(dist)
+    gb.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            gb.step_timed(1, t_of(k0 + k), DT, stage_ms)
+            iters.append(gb.stats().solver_iters)
+            flush.memset_async(k & 0xff, stream)
+        gb.synchronize()
+    barrier(dist)
+    st = gb.stats()
+    launches = st.launches - launches0
+    total_ms = float(stage_ms.sum())
+    total_ms_max = max_over_ranks(total_ms, dist)
+    value = world * N * args.steps / (total_ms_max / 1e3)
+
+    # roofline of the dominant kernel (live CUDA-event times)
+    k_dom = int(np.argmax(stage_ms))
+    dom = names[k_dom]
+    mean_iters = float(np.mean(iters)) if iters else 0.0
+    alg = dict(ALG_BYTES_PER_CELL)
+    alg["k_pcg"] = PCG_BYTES_FIXED + PCG_BYTES_PER_ITER * mean_iters
+    per_launch_bytes = alg[dom] * N
+    avg_launch_s = stage_ms[k_dom] / 1e3 / args.steps
+    achieved = per_launch_bytes / avg_launch_s / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = load_traffic().get(dom)
+    stage_share = {n: round(float(m / total_ms), 4) for n, m in zip(names, stage_ms)}
+    stage_us = {n: round(float(1e3 * m / args.steps), 2) for n, m in zip(names, stage_ms)}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e_steps = min(args.steps, 200)
+    h_u = cudart.PinnedArray((N,))
+    h_v = cudart.PinnedArray((Nv,))
+    h_eta = cudart.PinnedArray((N,))
+    h_u.array[:] = f.uair_init.ravel().astype(np.float32)
+    h_v.array[:] = f.vair_init.ravel().astype(np.float32)
+    barrier(dist)
+    gb.synchronize()
+    e2e_s = 0.0
+    kk = k0 + args.steps
+    for k in range(e2e_steps):
+        t0 = time.perf_counter()
+        gb.upload_f32("uair_init", h_u.array)
+        gb.upload_f32("vair_init", h_v.array)
+        gb.step(1, t_of(kk + k), DT)
+        gb.download_f32("eta", h_eta.array)
+        gb.synchronize()
+        e2e_s += time.perf_counter() - t0
+        flush.memset_async(k & 0xff, stream)
+        gb.synchronize()
+    e2e_s_max = max_over_ranks(e2e_s, dist)
+    e2e_value = world * N * e2e_steps / e2e_s_max
+    finite = bool(np.isfinite(h_eta.array).all())
+    final = gb.stats()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, n, el = cpu_oracle_rate(target_s=15.0, nthreads=threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} steps of the same 512x1024 workload (FP64 oracle, OpenMP "
+                         f"{threads} threads, PCG to 1e-6), {el:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": workload_config({"parallelism": f"replicas x{world}" if world > 1 else "single"}),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "alg_bytes_per_launch": per_launch_bytes,
+                         "avg_launch_us": avg_launch_s * 1e6},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
+                    "h2d_bytes_per_step": 4 * (N + Nv), "d2h_bytes_per_step": 4 * N,
+                    "inputs": "uair_init + vair_init (wind forcing) from pinned host memory",
+                    "result": "eta (thickness) to pinned host memory, read every step"},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "stage_share": stage_share, "stage_us_per_step": stage_us,
+            "solver_iters_mean": mean_iters, "solver_rel_resid_last": st.solver_rel_resid,
+            "reinits": int(final.reinits), "result_finite": finite,
+        }
+        print(json.dumps(line), flush=True)
+    h_u.free(); h_v.free(); h_eta.free(); flush.free()
+    gb.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

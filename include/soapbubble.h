@@ -77,6 +77,7 @@ typedef struct {
     long long reinits;        /* re-initialisations so far */
     double mass_eta;          /* sum eta sin(theta) (after sb_update_mass) */
     double mass_gamma;        /* sum gamma sin(theta) */
+    long long launches;       /* CUDA kernels launched by this handle */
 } sb_stats;
 
 typedef struct sb_bubble sb_bubble;
@@ -130,6 +131,24 @@ size_t sb_field_size(const sb_bubble* b, sb_field which);
  * frame (kernel/bubble.cu:2661-2678).  Asynchronous on the handle's stream
  * unless an error must be reported. */
 int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt);
+
+/* sb_step with CUDA events between the kernels of every step: adds each
+ * stage's device time (ms) to stage_ms[0 .. sb_stage_count()-1] and
+ * synchronises after each step.  Same results as sb_step.  The reference
+ * times its phases with cudaEvent timers (kernel/solver.cu:261-279). */
+int sb_step_timed(sb_bubble* b, int n_steps, double t_frame, double dt, double* stage_ms);
+
+/* Number of kernel stages of one step, and the kernel name of a stage. */
+int sb_stage_count(void);
+const char* sb_stage_name(int stage);
+
+/* Asynchronous FP32 copies between a caller's host buffer (pinned for true
+ * overlap) and one non-map field, ordered on the handle's stream; the
+ * caller synchronises (sb_synchronize) before reading dst or reusing src.
+ * The FP32 counterparts of Quantity::copyToGPU / copyBackToCPU
+ * (kernel/quantity.cu:3-18). */
+int sb_upload_field_f32(sb_bubble* b, sb_field which, const float* src, size_t n);
+int sb_download_field_f32(sb_bubble* b, sb_field which, float* dst, size_t n);
 
 /* Wait for the handle's queued work; returns SB_ERR_NOT_CONVERGED if the
  * last solve missed its tolerance. */

@@ -37,7 +37,7 @@ class SbStats(C.Structure):
         ("distortion", C.c_double), ("reinit", C.c_int), ("solver_iters", C.c_int),
         ("solver_rel_resid", C.c_double), ("solver_converged", C.c_int),
         ("broken_cells", C.c_int), ("steps", C.c_longlong), ("reinits", C.c_longlong),
-        ("mass_eta", C.c_double), ("mass_gamma", C.c_double),
+        ("mass_eta", C.c_double), ("mass_gamma", C.c_double), ("launches", C.c_longlong),
     ]
 
 
@@ -73,6 +73,14 @@ def lib() -> C.CDLL:
     L.sb_field_size.argtypes = [H, C.c_int]
     L.sb_field_size.restype = C.c_size_t
     L.sb_step.argtypes = [H, C.c_int, C.c_double, C.c_double]
+    L.sb_step_timed.argtypes = [H, C.c_int, C.c_double, C.c_double, dp]
+    L.sb_stage_count.argtypes = []
+    L.sb_stage_count.restype = C.c_int
+    L.sb_stage_name.argtypes = [C.c_int]
+    L.sb_stage_name.restype = C.c_char_p
+    fp = C.POINTER(C.c_float)
+    L.sb_upload_field_f32.argtypes = [H, C.c_int, fp, C.c_size_t]
+    L.sb_download_field_f32.argtypes = [H, C.c_int, fp, C.c_size_t]
     L.sb_synchronize.argtypes = [H]
     L.sb_get_stats.argtypes = [H, S]
     L.sb_update_mass.argtypes = [H]
@@ -87,7 +95,8 @@ def lib() -> C.CDLL:
     L.sb_last_error.argtypes = []
     L.sb_last_error.restype = C.c_char_p
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
-                 "sb_download_field", "sb_step", "sb_synchronize", "sb_get_stats",
+                 "sb_download_field", "sb_step", "sb_step_timed", "sb_upload_field_f32",
+                 "sb_download_field_f32", "sb_synchronize", "sb_get_stats",
                  "sb_update_mass", "sb_write_thickness_exr", "sb_run"):
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -102,5 +111,6 @@ def check(code: int, what: str) -> None:
 # Every symbol include/soapbubble.h declares (checked by the CPU tests).
 EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_upload_field", "sb_download_field", "sb_field_size", "sb_step",
-           "sb_synchronize", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
+           "sb_step_timed", "sb_stage_count", "sb_stage_name", "sb_upload_field_f32",
+           "sb_download_field_f32", "sb_synchronize", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
            "sb_run", "sb_write_exr_gray", "sb_bytes_required", "sb_stream", "sb_last_error"]

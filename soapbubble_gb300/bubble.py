@@ -108,6 +108,25 @@ class GpuBubble:
     def step(self, n: int = 1, t: float = 0.0, dt: Optional[float] = None) -> None:
         check(lib().sb_step(self.h, n, t, self.params.dt if dt is None else dt), "sb_step")
 
+    def step_timed(self, n: int, t: float, dt: float, stage_ms: np.ndarray) -> None:
+        """sb_step_timed: adds per-stage device milliseconds into stage_ms."""
+        assert stage_ms.dtype == np.float64 and stage_ms.size >= lib().sb_stage_count()
+        check(lib().sb_step_timed(self.h, n, t, dt, _dp(stage_ms)), "sb_step_timed")
+
+    def upload_f32(self, name: str, a: np.ndarray) -> None:
+        """Asynchronous FP32 upload from a host buffer the caller keeps alive."""
+        assert a.dtype == np.float32 and a.flags.c_contiguous
+        check(lib().sb_upload_field_f32(self.h, _lib.FIELD_ID[name],
+                                        a.ctypes.data_as(C.POINTER(C.c_float)), a.size),
+              "sb_upload_field_f32")
+
+    def download_f32(self, name: str, out: np.ndarray) -> None:
+        """Asynchronous FP32 download; synchronize() before reading `out`."""
+        assert out.dtype == np.float32 and out.flags.c_contiguous
+        check(lib().sb_download_field_f32(self.h, _lib.FIELD_ID[name],
+                                          out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
+              "sb_download_field_f32")
+
     def synchronize(self) -> None:
         check(lib().sb_synchronize(self.h), "sb_synchronize")
 
@@ -129,6 +148,10 @@ class GpuBubble:
 
     def stream(self) -> int:
         return lib().sb_stream(self.h)
+
+
+def stage_names() -> list:
+    return [lib().sb_stage_name(i).decode() for i in range(lib().sb_stage_count())]
 
 
 def bytes_required(params: SbParams) -> int:

@@ -73,6 +73,8 @@ struct sb_bubble {
     long long steps = 0;
     double last_dt = -1, last_t = -1e300;
     SbStepParams* h_step = nullptr;  // pinned
+    long long launches = 0;          // kernels launched by this handle
+    cudaEvent_t ev[STAGE_COUNT + 1] = {};
 };
 
 namespace {
@@ -427,6 +429,8 @@ int sb_destroy(sb_bubble* b) {
     if (!b) return SB_OK;
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
+    for (cudaEvent_t e : b->ev)
+        if (e) cudaEventDestroy(e);
     if (b->arena) cudaFree(b->arena);
     if (b->h_step) cudaFreeHost(b->h_step);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -538,14 +542,69 @@ int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt) {
     int rc = set_step_params(b, t_frame, dt);
     if (rc != SB_OK) return rc;
     for (int s = 0; s < n_steps; ++s) {
-        SB_CHECK(launch_advect(b->g, b->ph, b->f, b->cur, b->stream));
-        SB_CHECK(launch_assemble(b->g, b->ph, b->f, b->stream));
-        SB_CHECK(launch_solve(b->g, b->ph, b->f, b->solver, b->stream));
-        SB_CHECK(launch_post(b->g, b->ph, b->f, b->cur, b->stream));
-        SB_CHECK(launch_reinit(b->g, b->ph, b->f, b->cur, b->stream));
+        for (int st = 0; st < STAGE_COUNT; ++st)
+            SB_CHECK(launch_stage(st, b->g, b->ph, b->f, b->solver, b->cur, b->stream));
+        b->launches += STAGE_COUNT;
         b->cur ^= 1;
         b->steps++;
     }
+    return SB_OK;
+}
+
+int sb_step_timed(sb_bubble* b, int n_steps, double t_frame, double dt, double* stage_ms) {
+    if (!b || !stage_ms) return fail(SB_ERR_INVALID, "null argument");
+    if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
+    SB_CHECK(cudaSetDevice(b->device));
+    int rc = set_step_params(b, t_frame, dt);
+    if (rc != SB_OK) return rc;
+    if (!b->ev[0]) {
+        for (cudaEvent_t& e : b->ev) SB_CHECK(cudaEventCreate(&e));
+    }
+    for (int s = 0; s < n_steps; ++s) {
+        SB_CHECK(cudaEventRecord(b->ev[0], b->stream));
+        for (int st = 0; st < STAGE_COUNT; ++st) {
+            SB_CHECK(launch_stage(st, b->g, b->ph, b->f, b->solver, b->cur, b->stream));
+            SB_CHECK(cudaEventRecord(b->ev[st + 1], b->stream));
+        }
+        b->launches += STAGE_COUNT;
+        b->cur ^= 1;
+        b->steps++;
+        SB_CHECK(cudaEventSynchronize(b->ev[STAGE_COUNT]));
+        for (int st = 0; st < STAGE_COUNT; ++st) {
+            float ms = 0.f;
+            SB_CHECK(cudaEventElapsedTime(&ms, b->ev[st], b->ev[st + 1]));
+            stage_ms[st] += ms;
+        }
+    }
+    return SB_OK;
+}
+
+int sb_stage_count(void) { return STAGE_COUNT; }
+
+const char* sb_stage_name(int stage) {
+    static const char* names[STAGE_COUNT] = {"k_advect_maps", "k_velocity", "k_bimocq",
+                                             "k_assemble", "k_pcg", "k_post", "k_accum",
+                                             "k_reinit1", "k_reinit2", "k_reinit3"};
+    return (stage >= 0 && stage < STAGE_COUNT) ? names[stage] : "";
+}
+
+int sb_upload_field_f32(sb_bubble* b, sb_field which, const float* src, size_t n) {
+    if (!b || !src) return fail(SB_ERR_INVALID, "null argument");
+    if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
+    float* d = fptr(b, which);
+    if (!d) return fail(SB_ERR_INVALID, "maps move through sb_upload_field");
+    SB_CHECK(cudaSetDevice(b->device));
+    SB_CHECK(cudaMemcpyAsync(d, src, n * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+    return SB_OK;
+}
+
+int sb_download_field_f32(sb_bubble* b, sb_field which, float* dst, size_t n) {
+    if (!b || !dst) return fail(SB_ERR_INVALID, "null argument");
+    if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
+    float* d = fptr(b, which);
+    if (!d) return fail(SB_ERR_INVALID, "maps move through sb_download_field");
+    SB_CHECK(cudaSetDevice(b->device));
+    SB_CHECK(cudaMemcpyAsync(dst, d, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
     return SB_OK;
 }
 
@@ -573,6 +632,7 @@ int sb_get_stats(sb_bubble* b, sb_stats* out) {
     out->broken_cells = st.broken_cells;
     out->steps = b->steps;
     out->reinits = st.reinit_total;
+    out->launches = b->launches;
     out->mass_eta = st.mass_eta;
     out->mass_gamma = st.mass_gamma;
     return SB_OK;
@@ -582,6 +642,7 @@ int sb_update_mass(sb_bubble* b) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     SB_CHECK(cudaSetDevice(b->device));
     SB_CHECK(launch_mass(b->g, b->f, b->stream));
+    b->launches += 1;
     SB_CHECK(cudaStreamSynchronize(b->stream));
     return SB_OK;
 }

@@ -37,14 +37,24 @@ struct SolverConfig {
     int precond;    // 0: Jacobi, 1: exact phi-line (periodic tridiagonal per row)
 };
 
-// Step stages (sb_step.cu).  `cur` selects the map ping-pong buffers.
-cudaError_t launch_advect(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
-                          cudaStream_t s);
-cudaError_t launch_assemble(const SbGrid& g, const SbPhys& ph, const SbFields& f, cudaStream_t s);
-cudaError_t launch_post(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
-                        cudaStream_t s);
-cudaError_t launch_reinit(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
-                          cudaStream_t s);
+// Step stages in launch order (sb_step.cu, sb_solver.cu).  `cur` selects the
+// map ping-pong buffers.  Each stage is one kernel launch.
+enum SbStage {
+    STAGE_MAPS = 0,   // k_advect_maps: characteristic maps, gamma, air flow
+    STAGE_VELOCITY,   // k_velocity: u_theta / u_phi self-advection
+    STAGE_BIMOCQ,     // k_bimocq: thickness through the composed maps
+    STAGE_ASSEMBLE,   // k_assemble: implicit surfactant system
+    STAGE_SOLVE,      // k_pcg: cooperative PCG
+    STAGE_POST,       // k_post: forces, thickness, increments
+    STAGE_ACCUM,      // k_accum: BIMOCQ accumulation + distortion
+    STAGE_REINIT1,    // k_reinit1..3: conditional map re-initialisation
+    STAGE_REINIT2,
+    STAGE_REINIT3,
+    STAGE_COUNT
+};
+
+cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbFields& f,
+                         const struct SolverConfig& cfg, int cur, cudaStream_t s);
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s);
 cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s);
 

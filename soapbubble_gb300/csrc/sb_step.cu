@@ -541,32 +541,22 @@ inline dim3 grid_for(const SbGrid& g) { return dim3((g.N + kBlock - 1) / kBlock)
 
 }  // namespace
 
-cudaError_t launch_advect(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
-                          cudaStream_t s) {
-    k_advect_maps<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
-    k_velocity<<<grid_for(g), kBlock, 0, s>>>(g, f);
-    k_bimocq<<<grid_for(g), kBlock, 0, s>>>(g, ph, f, cur);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_assemble(const SbGrid& g, const SbPhys& ph, const SbFields& f, cudaStream_t s) {
-    k_assemble<<<grid_for(g), kBlock, 0, s>>>(g, ph, f);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_post(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
-                        cudaStream_t s) {
-    k_post<<<grid_for(g), kBlock, 0, s>>>(g, ph, f);
-    k_accum<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_reinit(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
-                          cudaStream_t s) {
-    (void)ph;
-    k_reinit1<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
-    k_reinit2<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
-    k_reinit3<<<grid_for(g), kBlock, 0, s>>>(g, f, cur);
+cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbFields& f,
+                         const SolverConfig& cfg, int cur, cudaStream_t s) {
+    const dim3 grid = grid_for(g);
+    switch (stage) {
+        case STAGE_MAPS: k_advect_maps<<<grid, kBlock, 0, s>>>(g, f, cur); break;
+        case STAGE_VELOCITY: k_velocity<<<grid, kBlock, 0, s>>>(g, f); break;
+        case STAGE_BIMOCQ: k_bimocq<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
+        case STAGE_ASSEMBLE: k_assemble<<<grid, kBlock, 0, s>>>(g, ph, f); break;
+        case STAGE_SOLVE: return launch_solve(g, ph, f, cfg, s);
+        case STAGE_POST: k_post<<<grid, kBlock, 0, s>>>(g, ph, f); break;
+        case STAGE_ACCUM: k_accum<<<grid, kBlock, 0, s>>>(g, f, cur); break;
+        case STAGE_REINIT1: k_reinit1<<<grid, kBlock, 0, s>>>(g, f, cur); break;
+        case STAGE_REINIT2: k_reinit2<<<grid, kBlock, 0, s>>>(g, f, cur); break;
+        case STAGE_REINIT3: k_reinit3<<<grid, kBlock, 0, s>>>(g, f, cur); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -1,0 +1,40 @@
+"""The oracle reproduces the committed golden step fixtures (CPU only).
+
+The fixtures (tests/golden/*.npz, made by tests/golden/make_golden.py) hold
+an FP32-exact input state and the FP64 oracle's output after one step.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def load_case(oracle, path):
+    z = np.load(path)
+    nT, dt, t, strict, force = z["meta"][:5]
+    nT = int(nT)
+    p = oracle.default_params(nT, dt_s=float(dt))
+    p.t, p.strict, p.force_reinit, p.nthreads = float(t), int(strict), int(force), 1
+    a = {k[3:]: z[k].astype(np.float64) for k in z.files if k.startswith("in_")}
+    ob = oracle.OracleBubble(p, a["eta"], a["gamma"], a["uth"], a["uph"], a["uair_init"],
+                             a["vair_init"])
+    for k, v in a.items():
+        ob.a[k][...] = v
+    return z, ob
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(g) for g in GOLDEN])
+def test_oracle_reproduces_golden(oracle, path):
+    z, ob = load_case(oracle, path)
+    st = ob.step()
+    assert st.reinit == int(z["meta"][5])
+    for k in z.files:
+        if not k.startswith("out_"):
+            continue
+        ref = z[k]
+        got = ob.a[k[4:]]
+        scale = max(np.max(np.abs(ref)), 1e-30)
+        assert np.max(np.abs(got - ref)) / scale < 1e-10, k
