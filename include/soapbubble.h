@@ -175,6 +175,24 @@ int sb_write_exr_gray(const char* path, int width, int height, const float* img)
  * into out_dir (NULL: no output).  frames <= 0 uses p->frames. */
 int sb_run(sb_bubble* b, const char* out_dir, int frames);
 
+/* No counterpart in the reference.  The two mass integrals of
+ * sb_update_mass (sum of eta sin(theta) and gamma sin(theta)) for callers
+ * that may not allocate device memory: a framework that owns all device
+ * memory through its own pool, code running while another component
+ * captures the device's streams, or a real-time loop that cannot afford
+ * cudaMalloc's implicit synchronisation.  eta and gamma are the caller's
+ * device arrays ([theta][phi], nTheta x 2 nTheta FP32); mass_out is the
+ * caller's device array of 2 doubles, written asynchronously on `stream`
+ * (a cudaStream_t, NULL = legacy default stream).  It allocates nothing:
+ * its scratch is a 20 KiB array compiled into the library (held on every
+ * GPU that loads it), so nTheta is limited to powers of two in [8, 1024]
+ * and larger grids are rejected with SB_ERR_INVALID.  The first call on
+ * each device looks up the array's address and should come before any
+ * stream capture.  All calls share the array: calls whose kernels overlap
+ * on the GPU race and must be serialised by the caller. */
+int sb_mass_integrals_noalloc(int nTheta, const float* eta, const float* gamma,
+                              double* mass_out, void* stream);
+
 /* Device bytes held by one bubble of this configuration (for admission). */
 size_t sb_bytes_required(const sb_params* p);
 

@@ -88,6 +88,9 @@ def lib() -> C.CDLL:
     L.sb_run.argtypes = [H, C.c_char_p, C.c_int]
     L.sb_write_exr_gray.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.sb_write_exr_gray.restype = C.c_int
+    L.sb_mass_integrals_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p]
+    L.sb_mass_integrals_noalloc.restype = C.c_int
     L.sb_bytes_required.argtypes = [P]
     L.sb_bytes_required.restype = C.c_size_t
     L.sb_stream.argtypes = [H]
@@ -113,4 +116,5 @@ EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_upload_field", "sb_download_field", "sb_field_size", "sb_step",
            "sb_step_timed", "sb_stage_count", "sb_stage_name", "sb_upload_field_f32",
            "sb_download_field_f32", "sb_synchronize", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
-           "sb_run", "sb_write_exr_gray", "sb_bytes_required", "sb_stream", "sb_last_error"]
+           "sb_run", "sb_write_exr_gray", "sb_mass_integrals_noalloc", "sb_bytes_required",
+           "sb_stream", "sb_last_error"]

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
-LIB_SOURCES = ["sb_step.cu", "sb_solver.cu", "sb_api.cu", "sb_exr.cpp"]
+LIB_SOURCES = ["sb_step.cu", "sb_solver.cu", "sb_api.cu", "sb_exr.cpp", "sb_noalloc.cu"]
 CLI_SOURCES = ["sb_bubble.cpp", "sb_main.cpp"]
 
 

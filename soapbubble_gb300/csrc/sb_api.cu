@@ -57,6 +57,11 @@ bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
 }  // namespace
 
+namespace sb {
+// Records an error for sb_last_error() from other translation units.
+int api_fail(int code, const char* msg) { return fail(code, msg); }
+}  // namespace sb
+
 struct sb_bubble {
     sb_params params;
     SbGrid g;

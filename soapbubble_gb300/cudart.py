@@ -32,6 +32,7 @@ def rt() -> C.CDLL:
         _rt.cudaEventSynchronize.argtypes = [vp]
         _rt.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), vp, vp]
         _rt.cudaEventDestroy.argtypes = [vp]
+        _rt.cudaMemcpy.argtypes = [vp, vp, sz, C.c_int]
     return _rt
 
 
@@ -95,3 +96,14 @@ class Event:
         ms = C.c_float(0)
         _ok(rt().cudaEventElapsedTime(C.byref(ms), self.ev, end.ev), "cudaEventElapsedTime")
         return ms.value
+
+
+def memcpy_htod(dst: DeviceBuffer, src: np.ndarray) -> None:
+    src = np.ascontiguousarray(src)
+    assert src.nbytes <= dst.nbytes
+    _ok(rt().cudaMemcpy(dst.ptr, src.ctypes.data_as(C.c_void_p), src.nbytes, 1), "cudaMemcpy")
+
+
+def memcpy_dtoh(dst: np.ndarray, src: DeviceBuffer) -> None:
+    assert dst.flags.c_contiguous and dst.nbytes <= src.nbytes
+    _ok(rt().cudaMemcpy(dst.ctypes.data_as(C.c_void_p), src.ptr, dst.nbytes, 2), "cudaMemcpy")
