@@ -80,6 +80,7 @@ struct sb_bubble {
     SbStepParams* h_step = nullptr;  // pinned
     long long launches = 0;          // kernels launched by this handle
     cudaEvent_t ev[STAGE_COUNT + 1] = {};
+    cudaGraphExec_t graph[2] = {};   // one captured step per map parity
 };
 
 namespace {
@@ -417,6 +418,10 @@ int sb_create(const sb_params* p, sb_bubble** out) {
         e = cudaMemcpy(f.stats, &st, sizeof(st), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) rc = cuda_fail(e, "stats");
     }
+    if (rc == SB_OK) {
+        e = prepare_launches(g, b->solver);
+        if (e != cudaSuccess) rc = cuda_fail(e, "prepare_launches");
+    }
     if (rc == SB_OK) rc = set_step_params(b, 0.0, p->dt);
     if (rc == SB_OK) {
         e = cudaStreamSynchronize(b->stream);
@@ -436,6 +441,8 @@ int sb_destroy(sb_bubble* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (cudaEvent_t e : b->ev)
         if (e) cudaEventDestroy(e);
+    for (cudaGraphExec_t gx : b->graph)
+        if (gx) cudaGraphExecDestroy(gx);
     if (b->arena) cudaFree(b->arena);
     if (b->h_step) cudaFreeHost(b->h_step);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -540,6 +547,22 @@ int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma, const
     return rc;
 }
 
+// One step of map parity `cur` captured as a CUDA graph (the per-step
+// scalars live in device memory, so the graph is replayed unchanged).
+static int capture_step(sb_bubble* b, int cur) {
+    cudaGraph_t graph = nullptr;
+    SB_CHECK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int st = 0; st < STAGE_COUNT && e == cudaSuccess; ++st)
+        e = launch_stage(st, b->g, b->ph, b->f, b->solver, cur, b->stream);
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[cur], graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "step graph capture");
+    return SB_OK;
+}
+
 int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
@@ -547,8 +570,11 @@ int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt) {
     int rc = set_step_params(b, t_frame, dt);
     if (rc != SB_OK) return rc;
     for (int s = 0; s < n_steps; ++s) {
-        for (int st = 0; st < STAGE_COUNT; ++st)
-            SB_CHECK(launch_stage(st, b->g, b->ph, b->f, b->solver, b->cur, b->stream));
+        if (!b->graph[b->cur]) {
+            rc = capture_step(b, b->cur);
+            if (rc != SB_OK) return rc;
+        }
+        SB_CHECK(cudaGraphLaunch(b->graph[b->cur], b->stream));
         b->launches += STAGE_COUNT;
         b->cur ^= 1;
         b->steps++;
@@ -589,7 +615,7 @@ int sb_stage_count(void) { return STAGE_COUNT; }
 const char* sb_stage_name(int stage) {
     static const char* names[STAGE_COUNT] = {"k_advect_maps", "k_velocity", "k_bimocq",
                                              "k_assemble", "k_pcg", "k_post", "k_accum",
-                                             "k_reinit1", "k_reinit2", "k_reinit3"};
+                                             "k_reinit"};
     return (stage >= 0 && stage < STAGE_COUNT) ? names[stage] : "";
 }
 

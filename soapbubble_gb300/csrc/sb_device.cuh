@@ -21,7 +21,14 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "sb_fastmath.cuh"
 #include "sb_types.h"
+
+// Inlining of the heavy geometry helpers (conversions, slerp, map lookup):
+// out-of-line calls keep the map kernels small in the instruction cache.
+#ifndef SB_GEOM_INLINE
+#define SB_GEOM_INLINE __noinline__
+#endif
 
 namespace sb {
 
@@ -51,13 +58,6 @@ struct Pos {
     float ox, oy;
 };
 
-// sin(x)/x, accurate to float rounding for all |x|.
-__device__ __forceinline__ float sincf_(float x) {
-    float x2 = x * x;
-    if (x2 < 1e-6f) return 1.0f - x2 * (1.0f / 6.0f);
-    return sinf(x) / x;
-}
-
 // NaN-skipping lerp (kernel/bubble.cu:153-160).
 __device__ __forceinline__ float blerp(float from, float to, float a) {
     if (isnan(from)) return to;
@@ -67,16 +67,16 @@ __device__ __forceinline__ float blerp(float from, float to, float a) {
 
 // Displacement P - C, in the frame, of the point at grid offsets (dth, dph)
 // from the frame's base.
-__device__ __forceinline__ f3 disp_from_offsets(const Frame& F, float dth, float dph, float h) {
+__device__ SB_GEOM_INLINE f3 disp_from_offsets(Frame F, float dth, float dph, float h) {
     float sh, chh;
-    sincosf(0.5f * dth * h, &sh, &chh);
+    fsincos(0.5f * dth * h, &sh, &chh);
     const float sm = F.s0 * chh + F.c0 * sh;  // sin(t0 + dt/2)
     const float cm = F.c0 * chh - F.s0 * sh;  // cos(t0 + dt/2)
     const float dS = 2.0f * cm * sh;          // sin t1 - sin t0
     const float dC = -2.0f * sm * sh;         // cos t1 - cos t0
     const float s1 = F.s0 + dS;
     float sp, cp;
-    sincosf(0.5f * dph * h, &sp, &cp);
+    fsincos(0.5f * dph * h, &sp, &cp);
     const float sinD = 2.0f * sp * cp;
     const float cosDm1 = -2.0f * sp * sp;
     return {dS + s1 * cosDm1, s1 * sinD, dC};
@@ -84,7 +84,7 @@ __device__ __forceinline__ f3 disp_from_offsets(const Frame& F, float dth, float
 
 // Grid position of the point C + d.  Points past a pole come back with the
 // base column shifted by nTheta (azimuth + pi) so the float offset stays small.
-__device__ __forceinline__ Pos pos_from_disp(const Frame& F, f3 d, float invh, int nT) {
+__device__ SB_GEOM_INLINE Pos pos_from_disp(Frame F, f3 d, float invh, int nT) {
     const float Px = F.s0 + d.x, Py = d.y, Pz = F.c0 + d.z;
     const float rho = sqrtf(Px * Px + Py * Py);
     const float den = rho + F.s0;
@@ -93,38 +93,36 @@ __device__ __forceinline__ Pos pos_from_disp(const Frame& F, f3 d, float invh, i
     const float cdt = rho * F.s0 + Pz * F.c0;     // cos(t1 - t0) scaled by |P|
     Pos q;
     q.bi = F.bi;
-    q.ox = F.fi + atan2f(sdt, cdt) * invh;
+    q.ox = F.fi + fatan2(sdt, cdt) * invh;
     if (Px >= 0.0f) {
         q.bj = F.bj;
-        q.oy = F.fj + atan2f(Py, Px) * invh;
+        q.oy = F.fj + fatan2(Py, Px) * invh;
     } else {
         q.bj = F.bj + nT;
-        q.oy = F.fj + atan2f(-Py, -Px) * invh;
+        q.oy = F.fj + fatan2(-Py, -Px) * invh;
     }
     return q;
 }
 
 // Great-circle angle (grid units) between the frame's base and C + d.
 __device__ __forceinline__ float dist_from_disp(f3 d, float invh) {
-    const float ch = len3(d);
-    return 2.0f * asinf(fminf(0.5f * ch, 1.0f)) * invh;
+    return farc_of_chord(len3(d)) * invh;
 }
 
 // Spherical lerp between C + dA and C + dB, returned as a displacement.
 // Same great-circle interpolation as lerpCoords (kernel/bubble.cu:512-536):
 // slerp(A, B, a) = sin((1-a)W)/sin W A + sin(aW)/sin W B, written so that
 // nearby points keep full precision.
-__device__ __forceinline__ f3 slerp_disp(const Frame& F, f3 dA, f3 dB, float a) {
+__device__ SB_GEOM_INLINE f3 slerp_disp(float s0, float c0, f3 dA, f3 dB, float a) {
     const f3 e = dB - dA;
-    const float ch = len3(e);
-    const float W = 2.0f * asinf(fminf(0.5f * ch, 1.0f));
+    const float W = farc_of_chord(len3(e));
     const float b = 1.0f - a;
-    const float sW = sincf_(W);
-    const float cA = b * sincf_(b * W) / sW;
-    const float cB = a * sincf_(a * W) / sW;
-    const float k = 0.5f * a * b * W * W * sincf_(0.5f * b * W) * sincf_(0.5f * a * W) /
-                    cosf(0.5f * W);  // cA + cB - 1
-    const f3 C = {F.s0, 0.0f, F.c0};
+    const float isW = 1.0f / fsinc(W);
+    const float cA = b * fsinc(b * W) * isW;
+    const float cB = a * fsinc(a * W) * isW;
+    const float k = 0.5f * a * b * W * W * fsinc(0.5f * b * W) * fsinc(0.5f * a * W) /
+                    fcos_small(0.5f * W);  // cA + cB - 1
+    const f3 C = {s0, 0.0f, c0};
     return cA * dA + cB * dB + k * C;
 }
 
@@ -274,10 +272,16 @@ __device__ __forceinline__ float sample_utheta(const SbGrid& g, const float* __r
 // four map points around q, slerped along phi on each row and then along
 // theta.  Map entries are float2 offsets from their own cell centre.  The
 // result is a displacement in frame F.
-__device__ __forceinline__ f3 sample_map(const SbGrid& g, const float2* __restrict__ map,
-                                         const Frame& F, Pos q) {
+__device__ SB_GEOM_INLINE f3 sample_map_impl(const float2* __restrict__ map, Frame F, Pos q,
+                                              int nT, float h, float invh) {
+    SbGrid g;
+    g.nT = nT;
+    g.nP = 2 * nT;
+    g.maskP = g.nP - 1;
+    g.h = h;
+    g.invh = invh;
     const CStencil s = centred_stencil(g, q, 0.0f);
-    const int nP = g.nP, nT = g.nT;
+    const int nP = g.nP;
     const float baseI = (float)0.5f - F.fi;
     auto point = [&](int r, int c) -> f3 {
         const float2 m = map[r * nP + c];
@@ -289,9 +293,14 @@ __device__ __forceinline__ f3 sample_map(const SbGrid& g, const float2* __restri
     };
     const f3 ll = point(s.r0, s.c00), lr = point(s.r0, s.c01);
     const f3 hl = point(s.r1, s.c10), hr = point(s.r1, s.c11);
-    const f3 lo = slerp_disp(F, ll, lr, s.b);
-    const f3 hi = slerp_disp(F, hl, hr, s.b);
-    return slerp_disp(F, lo, hi, s.a);
+    const f3 lo = slerp_disp(F.s0, F.c0, ll, lr, s.b);
+    const f3 hi = slerp_disp(F.s0, F.c0, hl, hr, s.b);
+    return slerp_disp(F.s0, F.c0, lo, hi, s.a);
+}
+
+__device__ __forceinline__ f3 sample_map(const SbGrid& g, const float2* __restrict__ map,
+                                         const Frame& F, Pos q) {
+    return sample_map_impl(map, F, q, g.nT, g.h, g.invh);
 }
 
 // Offsets (grid units) of C + d from the frame base, for storing as a map
@@ -356,7 +365,7 @@ __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restri
     f3 v_ = cross3(w, u_);
     float dS = -0.5f * un * dt;
     float sd, sh, ch;
-    sincosf(0.5f * dS, &sh, &ch);
+    fsincos(0.5f * dS, &sh, &ch);
     sd = 2.0f * sh * ch;
     float cdm1 = -2.0f * sh * sh;
     const f3 dmid = sd * u_ + cdm1 * w;
@@ -377,7 +386,7 @@ __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restri
     u_ = (1.0f / un) * u;
     v_ = cross3(w, u_);
     dS = -un * dt;
-    sincosf(0.5f * dS, &sh, &ch);
+    fsincos(0.5f * dS, &sh, &ch);
     sd = 2.0f * sh * ch;
     cdm1 = -2.0f * sh * sh;
     T.d = sd * u_ + cdm1 * w;
@@ -387,6 +396,69 @@ __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restri
     T.cd = 1.0f + cdm1;
     T.moved = true;
     return T;
+}
+
+// Bilinear stencil of a cell-centred scalar at q (flat indices), so that
+// several fields sampled at one position share the index work.
+struct SStencil {
+    int i00, i01, i10, i11;
+    float a, b;
+};
+
+__device__ __forceinline__ SStencil scalar_stencil(const SbGrid& g, Pos q) {
+    const CStencil c = centred_stencil(g, q, 0.0f);
+    SStencil s;
+    s.i00 = c.r0 * g.nP + c.c00;
+    s.i01 = c.r0 * g.nP + c.c01;
+    s.i10 = c.r1 * g.nP + c.c10;
+    s.i11 = c.r1 * g.nP + c.c11;
+    s.a = c.a;
+    s.b = c.b;
+    return s;
+}
+
+__device__ __forceinline__ float gather(const float* __restrict__ f, const SStencil& s) {
+    const float l = blerp(f[s.i00], f[s.i01], s.b);
+    const float u = blerp(f[s.i10], f[s.i11], s.b);
+    return blerp(l, u, s.a);
+}
+
+// Map lookups at the five MULTISAMPLE points of a cell, c + (-1/4, -1/4),
+// (+1/4, -1/4), (-1/4, +1/4), (+1/4, +1/4), c (kernel/bubble.cu:981-993),
+// in that order.  Their stencils all lie in the 3 x 3 neighbourhood of the
+// cell, so its nine map points are converted once (rows -1 and nTheta are
+// the across-pole reflections, as in the single lookup).  Results are
+// displacements in the cell's frame F.
+__device__ __forceinline__ void sample_map_multi5(const SbGrid& g, const float2* __restrict__ map,
+                                                  const Frame& F, f3 out[5]) {
+    const int nT = g.nT, nP = g.nP, i = F.bi, j = F.bj;
+    f3 P[3][3];
+#pragma unroll
+    for (int dr = -1; dr <= 1; ++dr) {
+        int row = i + dr, shift = 0;
+        if (row < 0) { row = 0; shift = nT; }
+        if (row > nT - 1) { row = nT - 1; shift = nT; }
+#pragma unroll
+        for (int dc = -1; dc <= 1; ++dc) {
+            const int col = (j + dc + shift) & g.maskP;
+            const float2 m = map[row * nP + col];
+            int dj = col - j;
+            dj = ((dj + nT) & g.maskP) - nT;
+            const float dth = (float)(row - i) + m.x;
+            const float dph = (float)dj + m.y;
+            P[dr + 1][dc + 1] = disp_from_offsets(F, dth, dph, g.h);
+        }
+    }
+    // (theta, phi) = (-1/4, -1/4): rows i-1, i; cols j-1, j; fractions 3/4
+    out[0] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[0][0], P[0][1], 0.75f),
+                        slerp_disp(F.s0, F.c0, P[1][0], P[1][1], 0.75f), 0.75f);
+    out[1] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[1][0], P[1][1], 0.75f),
+                        slerp_disp(F.s0, F.c0, P[2][0], P[2][1], 0.75f), 0.25f);
+    out[2] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[0][1], P[0][2], 0.25f),
+                        slerp_disp(F.s0, F.c0, P[1][1], P[1][2], 0.25f), 0.75f);
+    out[3] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[1][1], P[1][2], 0.25f),
+                        slerp_disp(F.s0, F.c0, P[2][1], P[2][2], 0.25f), 0.25f);
+    out[4] = P[1][1];
 }
 
 __device__ __forceinline__ Frame cell_frame(const SbGrid& g, int i, int j) {

@@ -47,14 +47,16 @@ enum SbStage {
     STAGE_SOLVE,      // k_pcg: cooperative PCG
     STAGE_POST,       // k_post: forces, thickness, increments
     STAGE_ACCUM,      // k_accum: BIMOCQ accumulation + distortion
-    STAGE_REINIT1,    // k_reinit1..3: conditional map re-initialisation
-    STAGE_REINIT2,
-    STAGE_REINIT3,
+    STAGE_REINIT,     // k_reinit: conditional map re-initialisation (cooperative)
     STAGE_COUNT
 };
 
 cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbFields& f,
                          const struct SolverConfig& cfg, int cur, cudaStream_t s);
+// Occupancy queries and function attributes of the cooperative kernels, done
+// once before any stream capture.
+cudaError_t prepare_launches(const SbGrid& g, const struct SolverConfig& cfg);
+cudaError_t prepare_solve(const SbGrid& g, const struct SolverConfig& cfg);
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s);
 cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s);
 

@@ -17,8 +17,12 @@
 //   k_reinit{1,2,3} reInitializeMapping, correctCentered1/2 (2180-2280, 2509-2564)
 // van der Waals is identically zero in the reference (W1 = W2 = 0,
 // bubble.cu:2633-2638) and is folded out.
+#include <cooperative_groups.h>
+
 #include "sb_device.cuh"
 #include "sb_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace sb {
 
@@ -28,8 +32,6 @@ constexpr int kBlock = 128;
 constexpr float kEps = 1e-7f;  // bubble.cu:28
 
 __constant__ float kW5[5] = {0.125f, 0.125f, 0.125f, 0.125f, 0.5f};
-__constant__ float kDirT[5] = {-0.25f, 0.25f, -0.25f, 0.25f, 0.0f};  // theta offsets
-__constant__ float kDirP[5] = {-0.25f, -0.25f, 0.25f, 0.25f, 0.0f};  // phi offsets
 
 __device__ __forceinline__ Frame face_frame_uphi(const SbGrid& g, int i, int j) {
     Frame F;
@@ -145,20 +147,21 @@ k_bimocq(SbGrid g, SbPhys ph, SbFields f, int cur) {
         return;
     }
     const Frame F = cell_frame(g, i, j);
-    const float2* bwd = f.bwd[cur ^ 1];
     const float blend = ph.blend;
+    f3 d1s[5];
+    sample_map_multi5(g, f.bwd[cur ^ 1], F, d1s);
     float attrib = 0.0f;
 #pragma unroll 1
     for (int k = 0; k < 5; ++k) {
-        const Pos q = frame_pos(F, kDirT[k], kDirP[k]);
-        const f3 d1 = sample_map(g, bwd, F, q);
-        const Pos q1 = pos_from_disp(F, d1, g.invh, g.nT);
+        const Pos q1 = pos_from_disp(F, d1s[k], g.invh, g.nT);
         const f3 d2 = sample_map(g, f.bwdprev, F, q1);
         const Pos q2 = pos_from_disp(F, d2, g.invh, g.nT);
-        const float sDelta = sample_scalar(g, f.eta_delta, q1);
+        const SStencil s1 = scalar_stencil(g, q1);
+        const SStencil s2 = scalar_stencil(g, q2);
+        const float sDelta = gather(f.eta_delta, s1);
         attrib += (1.0f - blend) * kW5[k] *
-                  (sample_scalar(g, f.eta_initL, q2) + sDelta + sample_scalar(g, f.eta_deltaL, q2));
-        attrib += blend * kW5[k] * (sample_scalar(g, f.eta_init, q1) + sDelta);
+                  (gather(f.eta_initL, s2) + sDelta + gather(f.eta_deltaL, s2));
+        attrib += blend * kW5[k] * (gather(f.eta_init, s1) + sDelta);
     }
     f.eta_adv[idx] = fmaxf(0.0f, attrib);
 }
@@ -389,12 +392,13 @@ k_accum(SbGrid g, SbFields f, int cur) {
         const float2* fwd = f.fwd[cur ^ 1];
         const float2* bwd = f.bwd[cur ^ 1];
         float ed = f.eta_delta[idx], gd = f.gam_delta[idx];
-#pragma unroll 1
+        f3 ds[5];
+        sample_map_multi5(g, fwd, F, ds);
+#pragma unroll
         for (int k = 0; k < 5; ++k) {
-            const f3 d = sample_map(g, fwd, F, frame_pos(F, kDirT[k], kDirP[k]));
-            const Pos q = pos_from_disp(F, d, g.invh, g.nT);
-            ed += kW5[k] * sample_scalar(g, f.d_eta, q);
-            gd += kW5[k] * sample_scalar(g, f.d_gam, q);
+            const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
+            ed += kW5[k] * gather(f.d_eta, s);
+            gd += kW5[k] * gather(f.d_gam, s);
         }
         f.eta_delta[idx] = ed;
         f.gam_delta[idx] = gd;
@@ -423,24 +427,18 @@ __device__ __forceinline__ bool reinit_now(const SbDevStats* st) {
 }
 
 // correctCentered1: BIMOCQ error estimate through the forward map.
-__global__ void __launch_bounds__(kBlock)
-k_reinit1(SbGrid g, SbFields f, int cur) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= g.N || !reinit_now(f.stats)) return;
-    if (idx == 0) {
-        f.stats->reinit = 1;
-        f.stats->reinit_total += 1;
-    }
+__device__ __forceinline__ void reinit_error(const SbGrid& g, const SbFields& f, int cur, int idx) {
     const int i = idx >> g.logP, j = idx & g.maskP;
     const Frame F = cell_frame(g, i, j);
     const float2* fwd = f.fwd[cur ^ 1];
     float th = 0.0f, gm = 0.0f;
-#pragma unroll 1
+    f3 ds[5];
+    sample_map_multi5(g, fwd, F, ds);
+#pragma unroll
     for (int k = 0; k < 5; ++k) {
-        const f3 d = sample_map(g, fwd, F, frame_pos(F, kDirT[k], kDirP[k]));
-        const Pos q = pos_from_disp(F, d, g.invh, g.nT);
-        th += kW5[k] * sample_scalar(g, f.eta, q);
-        gm += kW5[k] * sample_scalar(g, f.gam, q);
+        const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
+        th += kW5[k] * gather(f.eta, s);
+        gm += kW5[k] * gather(f.gam, s);
     }
     f.err_eta[idx] = (th - f.eta_delta[idx] - f.eta_init[idx]) * 0.5f;
     f.err_gam[idx] = (gm - f.gam_delta[idx] - f.gam_init[idx]) * 0.5f;
@@ -455,21 +453,19 @@ __device__ __forceinline__ int nb_index(const SbGrid& g, int i, int j) {
 
 // correctCentered2: subtract the error pulled back through the backward map,
 // clamp to the 3x3 range of the uncorrected field, keep non-negative.  The
-// result goes to the *_adv buffers; k_reinit3 commits it.
-__global__ void __launch_bounds__(kBlock)
-k_reinit2(SbGrid g, SbFields f, int cur) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= g.N || !reinit_now(f.stats)) return;
+// result goes to the *_adv buffers and is committed in the next phase.
+__device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbFields& f, int cur, int idx) {
     const int i = idx >> g.logP, j = idx & g.maskP;
     const Frame F = cell_frame(g, i, j);
     const float2* bwd = f.bwd[cur ^ 1];
     float th = f.eta[idx], gm = f.gam[idx];
-#pragma unroll 1
+    f3 ds[5];
+    sample_map_multi5(g, bwd, F, ds);
+#pragma unroll
     for (int k = 0; k < 5; ++k) {
-        const f3 d = sample_map(g, bwd, F, frame_pos(F, kDirT[k], kDirP[k]));
-        const Pos q = pos_from_disp(F, d, g.invh, g.nT);
-        th -= kW5[k] * sample_scalar(g, f.err_eta, q);
-        gm -= kW5[k] * sample_scalar(g, f.err_gam, q);
+        const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
+        th -= kW5[k] * gather(f.err_eta, s);
+        gm -= kW5[k] * gather(f.err_gam, s);
     }
     float emin = f.eta[idx], emax = emin, gmin = f.gam[idx], gmx = gmin;
     for (int t = -1; t <= 1; ++t)
@@ -486,10 +482,7 @@ k_reinit2(SbGrid g, SbFields f, int cur) {
 }
 
 // Commit the correction, rotate the BIMOCQ buffers and reset the maps.
-__global__ void __launch_bounds__(kBlock)
-k_reinit3(SbGrid g, SbFields f, int cur) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= g.N || !reinit_now(f.stats)) return;
+__device__ __forceinline__ void reinit_commit(const SbFields& f, int cur, int idx) {
     const float e = f.eta_adv[idx], gm = f.gam_adv[idx];
     f.eta[idx] = e;
     f.gam[idx] = gm;
@@ -504,6 +497,28 @@ k_reinit3(SbGrid g, SbFields f, int cur) {
     f.bwdprev[idx] = f.bwd[cur ^ 1][idx];
     f.fwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
     f.bwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
+}
+
+// reInitializeMapping (kernel/bubble.cu:2509-2564) when the distortion
+// exceeds 4 cells (or when forced): one cooperative launch, three phases
+// separated by grid barriers.  Without a re-initialisation every block
+// returns at once (the decision is read from device memory, so no host
+// synchronisation is needed).
+__global__ void __launch_bounds__(kBlock)
+k_reinit(SbGrid g, SbFields f, int cur) {
+    if (!reinit_now(f.stats)) return;  // same value in every block
+    cg::grid_group grid = cg::this_grid();
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t0 == 0) {
+        f.stats->reinit = 1;
+        f.stats->reinit_total += 1;
+    }
+    for (int idx = t0; idx < g.N; idx += stride) reinit_error(g, f, cur, idx);
+    grid.sync();
+    for (int idx = t0; idx < g.N; idx += stride) reinit_correct(g, f, cur, idx);
+    grid.sync();
+    for (int idx = t0; idx < g.N; idx += stride) reinit_commit(f, cur, idx);
 }
 
 __global__ void k_reset_maps(SbGrid g, SbFields f) {
@@ -539,6 +554,21 @@ __global__ void k_mass(SbGrid g, SbFields f) {
 
 inline dim3 grid_for(const SbGrid& g) { return dim3((g.N + kBlock - 1) / kBlock); }
 
+// Co-resident grid of the cooperative re-initialisation kernel.
+int reinit_blocks() {
+    static int cache[16] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& b = cache[dev & 15];
+    if (b == 0) {
+        int sms = 0, per = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_reinit, kBlock, 0);
+        b = sms * (per > 0 ? per : 1);
+    }
+    return b;
+}
+
 }  // namespace
 
 cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbFields& f,
@@ -552,12 +582,22 @@ cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbF
         case STAGE_SOLVE: return launch_solve(g, ph, f, cfg, s);
         case STAGE_POST: k_post<<<grid, kBlock, 0, s>>>(g, ph, f); break;
         case STAGE_ACCUM: k_accum<<<grid, kBlock, 0, s>>>(g, f, cur); break;
-        case STAGE_REINIT1: k_reinit1<<<grid, kBlock, 0, s>>>(g, f, cur); break;
-        case STAGE_REINIT2: k_reinit2<<<grid, kBlock, 0, s>>>(g, f, cur); break;
-        case STAGE_REINIT3: k_reinit3<<<grid, kBlock, 0, s>>>(g, f, cur); break;
+        case STAGE_REINIT: {
+            SbGrid gg = g;
+            SbFields ff = f;
+            int cc = cur;
+            void* args[] = {&gg, &ff, &cc};
+            return cudaLaunchCooperativeKernel((const void*)k_reinit, dim3(reinit_blocks()),
+                                               dim3(kBlock), args, 0, s);
+        }
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+cudaError_t prepare_launches(const SbGrid& g, const SolverConfig& cfg) {
+    reinit_blocks();
+    return prepare_solve(g, cfg);
 }
 
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s) {

@@ -61,6 +61,30 @@ CASES = [
     (128, "c2", 0.001, 5, 0.5, 78, 0),
 ]
 
+# Under gravity the radius-1 film drains: by ~140 steps of c0 the top has
+# no film left (eta = 0), velocities there are NaN (the reference writes NaN
+# where both neighbouring thicknesses vanish, bubble.cu:1849-1853) and the
+# implicit system carries identity rows.  One step from such a state.
+BROKEN_CASES = [(64, "c0", 0.005, 160, 0.8, 1234), (64, "c0", 0.005, 260, 1.3, 1234)]
+
+
+@pytest.mark.parametrize("case", BROKEN_CASES, ids=lambda c: f"{c[0]}-{c[1]}-pre{c[3]}")
+def test_step_matches_oracle_on_broken_film(oracle, gpulib, case):
+    nT, recipe, dt, pre, t, seed = case
+    gb, ob = new_pair(oracle, nT, recipe, dt, pre, t, seed)
+    with gb:
+        assert np.isnan(ob.a["uth"]).any() and (ob.a["eta"] == 0).any()
+        st = ob.step()
+        gb.step(1, t, dt)
+        gs = gb.stats()
+        assert gs.broken_cells == st.broken_cells
+        assert gs.solver_converged == 1
+        for k in PHYS:
+            g, o = gb.download(k), ob.a[P.FIELD_MAP[k]]
+            np.testing.assert_array_equal(np.isnan(g), np.isnan(o), err_msg=k)
+            np.testing.assert_array_equal(g == 0, o == 0, err_msg=k)
+            assert P.rel_err(g, o) <= TOL_FIELD, (k, P.rel_err(g, o))
+
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[1]}-pre{c[3]}-force{c[6]}")
 def test_step_matches_oracle(oracle, gpulib, case):
