@@ -139,7 +139,7 @@ struct ArenaPlan {
     size_t fwd[2], bwd[2], bwdprev;
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
     size_t div, d_eta, d_gam, err_eta, err_gam;
-    size_t dmass, cE, cS, rhs, r0, x, dx, r, z, p, q, x64, partials, step, stats;
+    size_t dmass, cE, cS, rhs, r0, x, dx, r, z, p, q, x64, pcr, pcr_levels, partials, step, stats;
 };
 
 ArenaPlan plan_arena(const SbGrid& g, int partials) {
@@ -163,6 +163,10 @@ ArenaPlan plan_arena(const SbGrid& g, int partials) {
     a.r = a.L.take(N * F);
     a.z = a.L.take(N * F); a.p = a.L.take(N * F); a.q = a.L.take(N * F);
     a.x64 = a.L.take(N * 8);
+    int lg = 0;
+    while ((1 << lg) < g.nP) ++lg;
+    a.pcr = a.L.take((size_t)lg * N * 8);  // <= log2(nP) - 1 levels + final factors
+    a.pcr_levels = a.L.take((size_t)g.nT * 4);
     a.partials = a.L.take((size_t)partials * 8);
     a.step = a.L.take(sizeof(SbStepParams));
     a.stats = a.L.take(sizeof(SbDevStats) + 64);
@@ -358,6 +362,8 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.dmass = F32(a.dmass); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs); f.r0 = F32(a.r0);
     f.x = F32(a.x); f.dx = F32(a.dx); f.r = F32(a.r); f.z = F32(a.z); f.p = F32(a.p); f.q = F32(a.q);
     f.x64 = (double*)(A + a.x64);
+    f.pcr = (float2*)(A + a.pcr);
+    f.pcr_levels = (int*)(A + a.pcr_levels);
     f.partials = (double*)(A + a.partials);
     f.step = (SbStepParams*)(A + a.step);
     f.stats = (SbDevStats*)(A + a.stats);

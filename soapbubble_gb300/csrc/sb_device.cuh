@@ -112,8 +112,9 @@ __device__ __forceinline__ float dist_from_disp(f3 d, float invh) {
 // Spherical lerp between C + dA and C + dB, returned as a displacement.
 // Same great-circle interpolation as lerpCoords (kernel/bubble.cu:512-536):
 // slerp(A, B, a) = sin((1-a)W)/sin W A + sin(aW)/sin W B, written so that
-// nearby points keep full precision.
-__device__ SB_GEOM_INLINE f3 slerp_disp(float s0, float c0, f3 dA, f3 dB, float a) {
+// nearby points keep full precision: slerp - C = cA dA + cB dB + k C with
+// k = cA + cB - 1 = 2 sin((1-a)W/2) sin(aW/2) / cos(W/2).
+__device__ __noinline__ f3 slerp_disp_far(float s0, float c0, f3 dA, f3 dB, float a) {
     const f3 e = dB - dA;
     const float W = farc_of_chord(len3(e));
     const float b = 1.0f - a;
@@ -121,9 +122,47 @@ __device__ SB_GEOM_INLINE f3 slerp_disp(float s0, float c0, f3 dA, f3 dB, float 
     const float cA = b * fsinc(b * W) * isW;
     const float cB = a * fsinc(a * W) * isW;
     const float k = 0.5f * a * b * W * W * fsinc(0.5f * b * W) * fsinc(0.5f * a * W) /
-                    fcos_small(0.5f * W);  // cA + cB - 1
+                    fcos_small(0.5f * W);
     const f3 C = {s0, 0.0f, c0};
     return cA * dA + cB * dB + k * C;
+}
+
+// For chords up to 1/4 (W < 0.253) the coefficients are power series in
+// u = W^2 (from the squared chord c2: u = c2 + c2^2/12 + c2^3/90 + c2^4/560):
+//   cB / a = 1 + (1-a^2) u/6 + (1-a^2)(7-3a^2) u^2/360
+//              + (1-a^2)(3a^4-18a^2+31) u^3/15120,
+//   cA as cB with a -> 1-a,
+//   k / (p u / 2) = 1 + (1+p) u/12 + (p^2+3p+3) u^2/360
+//                   + (p^3+6p^2+17p+17) u^3/20160,   p = a (1-a);
+// the truncation is below 1e-9 relative.  Farther points take the exact
+// formula out of line.
+__device__ __forceinline__ f3 slerp_disp_inl(float s0, float c0, f3 dA, f3 dB, float a) {
+    const f3 e = dB - dA;
+    const float c2 = dot3(e, e);
+    if (c2 > 0.0625f) return slerp_disp_far(s0, c0, dA, dB, a);
+    const float u = c2 * fmaf(c2, fmaf(c2, fmaf(c2, 1.0f / 560.0f, 1.0f / 90.0f), 1.0f / 12.0f), 1.0f);
+    const float b = 1.0f - a;
+    const float a2 = a * a, b2 = b * b;
+    const float pa = fmaf(u, fmaf(u, fmaf(a2, fmaf(a2, 3.0f, -18.0f), 31.0f) * (1.0f / 15120.0f),
+                                  fmaf(a2, -3.0f, 7.0f) * (1.0f / 360.0f)),
+                          1.0f / 6.0f);
+    const float pb = fmaf(u, fmaf(u, fmaf(b2, fmaf(b2, 3.0f, -18.0f), 31.0f) * (1.0f / 15120.0f),
+                                  fmaf(b2, -3.0f, 7.0f) * (1.0f / 360.0f)),
+                          1.0f / 6.0f);
+    const float cB = a * fmaf(u * (1.0f - a2), pa, 1.0f);
+    const float cA = b * fmaf(u * (1.0f - b2), pb, 1.0f);
+    const float p = a * b;
+    const float pk = fmaf(u, fmaf(u, fmaf(p, fmaf(p, fmaf(p, 1.0f, 6.0f), 17.0f), 17.0f) *
+                                      (1.0f / 20160.0f),
+                                  fmaf(p, fmaf(p, 1.0f, 3.0f), 3.0f) * (1.0f / 360.0f)),
+                          (1.0f + p) * (1.0f / 12.0f));
+    const float k = 0.5f * p * u * fmaf(u, pk, 1.0f);
+    const f3 C = {s0, 0.0f, c0};
+    return cA * dA + cB * dB + k * C;
+}
+
+__device__ SB_GEOM_INLINE f3 slerp_disp(float s0, float c0, f3 dA, f3 dB, float a) {
+    return slerp_disp_inl(s0, c0, dA, dB, a);
 }
 
 // ---------------------------------------------------------------------------
@@ -450,14 +489,14 @@ __device__ __forceinline__ void sample_map_multi5(const SbGrid& g, const float2*
         }
     }
     // (theta, phi) = (-1/4, -1/4): rows i-1, i; cols j-1, j; fractions 3/4
-    out[0] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[0][0], P[0][1], 0.75f),
-                        slerp_disp(F.s0, F.c0, P[1][0], P[1][1], 0.75f), 0.75f);
-    out[1] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[1][0], P[1][1], 0.75f),
-                        slerp_disp(F.s0, F.c0, P[2][0], P[2][1], 0.75f), 0.25f);
-    out[2] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[0][1], P[0][2], 0.25f),
-                        slerp_disp(F.s0, F.c0, P[1][1], P[1][2], 0.25f), 0.75f);
-    out[3] = slerp_disp(F.s0, F.c0, slerp_disp(F.s0, F.c0, P[1][1], P[1][2], 0.25f),
-                        slerp_disp(F.s0, F.c0, P[2][1], P[2][2], 0.25f), 0.25f);
+    out[0] = slerp_disp_inl(F.s0, F.c0, slerp_disp_inl(F.s0, F.c0, P[0][0], P[0][1], 0.75f),
+                        slerp_disp_inl(F.s0, F.c0, P[1][0], P[1][1], 0.75f), 0.75f);
+    out[1] = slerp_disp_inl(F.s0, F.c0, slerp_disp_inl(F.s0, F.c0, P[1][0], P[1][1], 0.75f),
+                        slerp_disp_inl(F.s0, F.c0, P[2][0], P[2][1], 0.75f), 0.25f);
+    out[2] = slerp_disp_inl(F.s0, F.c0, slerp_disp_inl(F.s0, F.c0, P[0][1], P[0][2], 0.25f),
+                        slerp_disp_inl(F.s0, F.c0, P[1][1], P[1][2], 0.25f), 0.75f);
+    out[3] = slerp_disp_inl(F.s0, F.c0, slerp_disp_inl(F.s0, F.c0, P[1][1], P[1][2], 0.25f),
+                        slerp_disp_inl(F.s0, F.c0, P[2][1], P[2][2], 0.25f), 0.25f);
     out[4] = P[1][1];
 }
 

@@ -20,8 +20,22 @@ __device__ __noinline__ float slow_cos(float x) { return cosf(x); }
 __device__ __noinline__ float slow_arc(float x) { return 2.0f * asinf(fminf(x, 1.0f)); }
 __device__ __noinline__ float slow_atan2(float y, float x) { return atan2f(y, x); }
 
-// sin and cos; Taylor to x^11 / x^12 on |x| <= 0.8 (truncation < 1e-11).
+// sin and cos; Taylor to x^7 / x^8 on |x| <= 0.2 (truncation < 2e-12),
+// to x^11 / x^12 on |x| <= 0.8 (truncation < 1e-11).
 __device__ __forceinline__ void fsincos(float x, float* s, float* c) {
+    if (fabsf(x) <= 0.2f) {
+        const float x2 = x * x;
+        float ps = -1.9841269841e-4f;          // -1/7!
+        ps = fmaf(ps, x2, 8.3333333333e-3f);   //  1/5!
+        ps = fmaf(ps, x2, -1.6666666667e-1f);  // -1/3!
+        *s = fmaf(ps * x2, x, x);
+        float pc = 2.4801587302e-5f;           //  1/8!
+        pc = fmaf(pc, x2, -1.3888888889e-3f);  // -1/6!
+        pc = fmaf(pc, x2, 4.1666666667e-2f);   //  1/4!
+        pc = fmaf(pc, x2, -0.5f);
+        *c = fmaf(pc, x2, 1.0f);
+        return;
+    }
     if (fabsf(x) <= 0.8f) {
         const float x2 = x * x;
         float ps = -2.5052108385e-8f;          // -1/11!

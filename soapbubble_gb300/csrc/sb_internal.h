@@ -25,6 +25,8 @@ struct SbFields {
     float *dmass, *cE, *cS, *rhs, *r0;
     float *x, *dx, *r, *z, *p, *q;                 // solver vectors
     double *x64;                                   // mixed-precision iterate
+    float2 *pcr;                                   // phi-line factors, (log2 nPhi) x N
+    int *pcr_levels;                               // reduction levels per row
     double *partials;                              // per-block reduction slots
     SbStepParams* step;                            // device copy of step scalars
     SbDevStats* stats;

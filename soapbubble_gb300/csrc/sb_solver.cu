@@ -101,7 +101,13 @@ __device__ __forceinline__ A apply_A(const SbGrid& g, const SbFields& f, const T
 // z = M^-1 r on theta row i: Jacobi, or the exact periodic tridiagonal solve.
 // sm holds 4 * nP floats.  Adds this row's r.z and r.r to rz, rr.
 // PER = equations per thread (nP <= PER * kSolveBlock).
-template <bool MIXED, int PER>
+//
+// The row matrix does not change during a solve, so the first application
+// (BUILD) runs the full cyclic reduction and stores, per level, the two
+// elimination factors of every equation (f.pcr) and the number of levels the
+// row needed (f.pcr_levels); later applications only replay
+// D' = D + a D[j - s] + c D[j + s] with the stored factors.
+template <bool MIXED, int PER, bool BUILD>
 __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f,
                                                  const SolverConfig& cfg, int i, float* sm,
                                                  double& rz, double& rr) {
@@ -121,77 +127,145 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         }
         return;
     }
-    float* E = sm;            // excess: diagonal minus the phi couplings
-    float* L = sm + nP;       // |coupling to j - s|
-    float* U = sm + 2 * nP;   // |coupling to j + s|
-    float* D = sm + 3 * nP;   // right-hand side
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int j = threadIdx.x + k * kSolveBlock;
-        if (j < nP) {
-            const int c = row + j;
-            float ex = f.dmass[c];
-            if (i < nT - 1) ex += f.cS[c];
-            if (i > 0) ex += f.cS[c - nP];
-            E[j] = ex;
-            U[j] = f.cE[c];
-            L[j] = f.cE[row + ((j - 1) & mask)];
-            D[j] = f.r[c];
-        }
-    }
-    __syncthreads();
-    // Parallel cyclic reduction: after the step with stride s every
-    // equation couples j to j -/+ 2s (indices mod nP).  It stops early once
-    // every coupling is below 2^-26 of its excess (the row has decoupled to
-    // float precision); otherwise it ends with 2 x 2 solves of j, j + nP/2.
-    bool decoupled = false;
-    for (int s = 1; s <= nP / 4; s <<= 1) {
-        float nE[PER], nL[PER], nU[PER], nD[PER];
+    // factor storage of this row: level l at f.pcr[(l * nT + i) * nP + j]
+    const size_t lvl_stride = (size_t)nT * nP;
+    float2* fac = f.pcr + (size_t)row;
+    if (BUILD) {
+        float* E = sm;            // excess: diagonal minus the phi couplings
+        float* L = sm + nP;       // |coupling to j - s|
+        float* U = sm + 2 * nP;   // |coupling to j + s|
+        float* D = sm + 3 * nP;   // right-hand side
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int j = threadIdx.x + k * kSolveBlock;
             if (j < nP) {
-                const int jm = (j - s) & mask, jp = (j + s) & mask;
-                const float bm = E[jm] + L[jm] + U[jm];
-                const float bp = E[jp] + L[jp] + U[jp];
-                // fast division: the preconditioner stays a fixed operator
-                const float am = __fdividef(L[j], bm);
-                const float cp = __fdividef(U[j], bp);
-                nE[k] = E[j] + am * E[jm] + cp * E[jp];
-                nL[k] = am * L[jm];
-                nU[k] = cp * U[jp];
-                nD[k] = D[j] + am * D[jm] + cp * D[jp];
+                const int c = row + j;
+                float ex = f.dmass[c];
+                if (i < nT - 1) ex += f.cS[c];
+                if (i > 0) ex += f.cS[c - nP];
+                E[j] = ex;
+                U[j] = f.cE[c];
+                L[j] = f.cE[row + ((j - 1) & mask)];
+                D[j] = f.r[c];
             }
         }
         __syncthreads();
-        bool need = false;
+        // Parallel cyclic reduction: after the step with stride s every
+        // equation couples j to j -/+ 2s (indices mod nP).  It stops early
+        // once every coupling is below 2^-26 of its excess (the row has
+        // decoupled to float precision); otherwise it ends with 2 x 2
+        // solves of j and j + nP/2.
+        bool decoupled = false;
+        int levels = 0;
+        for (int s = 1; s <= nP / 4; s <<= 1) {
+            float nE[PER], nL[PER], nU[PER], nD[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int j = threadIdx.x + k * kSolveBlock;
+                if (j < nP) {
+                    const int jm = (j - s) & mask, jp = (j + s) & mask;
+                    const float bm = E[jm] + L[jm] + U[jm];
+                    const float bp = E[jp] + L[jp] + U[jp];
+                    // fast division: the preconditioner stays a fixed operator
+                    const float am = __fdividef(L[j], bm);
+                    const float cp = __fdividef(U[j], bp);
+                    fac[levels * lvl_stride + j] = make_float2(am, cp);
+                    nE[k] = E[j] + am * E[jm] + cp * E[jp];
+                    nL[k] = am * L[jm];
+                    nU[k] = cp * U[jp];
+                    nD[k] = D[j] + am * D[jm] + cp * D[jp];
+                }
+            }
+            __syncthreads();
+            bool need = false;
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int j = threadIdx.x + k * kSolveBlock;
+                if (j < nP) {
+                    E[j] = nE[k]; L[j] = nL[k]; U[j] = nU[k]; D[j] = nD[k];
+                    need |= (nL[k] + nU[k]) > 1.4901161e-8f * nE[k];
+                }
+            }
+            ++levels;
+            if (!__syncthreads_or(need)) {
+                decoupled = true;
+                break;
+            }
+        }
+        if (threadIdx.x == 0) f.pcr_levels[i] = decoupled ? levels : -levels;
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int j = threadIdx.x + k * kSolveBlock;
             if (j < nP) {
-                E[j] = nE[k]; L[j] = nL[k]; U[j] = nU[k]; D[j] = nD[k];
-                need |= (nL[k] + nU[k]) > 1.4901161e-8f * nE[k];
+                float c1, c2;
+                if (decoupled) {
+                    c1 = 1.0f / (E[j] + L[j] + U[j]);
+                    c2 = 0.0f;
+                } else {
+                    const int kk = (j + nP / 2) & mask;
+                    const float mj = L[j] + U[j], mk = L[kk] + U[kk];
+                    const float ej = E[j], ek = E[kk];
+                    const float idet = 1.0f / (ej * ek + ej * mk + mj * ek);
+                    c1 = (ek + mk) * idet;
+                    c2 = mj * idet;
+                }
+                fac[levels * lvl_stride + j] = make_float2(c1, c2);
+                const int kk = (j + nP / 2) & mask;
+                const float zj = c1 * D[j] + c2 * D[kk];
+                const int c = row + j;
+                const float rc = f.r[c];
+                f.z[c] = zj;
+                rz += MIXED ? (double)rc * (double)zj : (double)(rc * zj);
+                rr += MIXED ? (double)rc * (double)rc : (double)(rc * rc);
             }
         }
-        if (!__syncthreads_or(need)) {
-            decoupled = true;
-            break;
-        }
+        __syncthreads();
+        return;
     }
+    // replay with the stored factors; D ping-pongs between two buffers
+    float* D0 = sm;
+    float* D1 = sm + nP;
+    const int lv = f.pcr_levels[i];
+    const int levels = lv < 0 ? -lv : lv;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = threadIdx.x + k * kSolveBlock;
+        if (j < nP) D0[j] = f.r[row + j];
+    }
+    __syncthreads();
+    // the factors of level l + 1 are loaded while level l is reduced
+    float2 acn[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = threadIdx.x + k * kSolveBlock;
+        acn[k] = j < nP ? fac[j] : make_float2(0.0f, 0.0f);
+    }
+    int s = 1;
+    for (int l = 0; l < levels; ++l, s <<= 1) {
+        float* Din = (l & 1) ? D1 : D0;
+        float* Dout = (l & 1) ? D0 : D1;
+        float2 ac[PER];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            ac[k] = acn[k];
+            const int j = threadIdx.x + k * kSolveBlock;
+            if (j < nP) acn[k] = fac[(l + 1) * lvl_stride + j];
+        }
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int j = threadIdx.x + k * kSolveBlock;
+            if (j < nP)
+                Dout[j] = Din[j] + ac[k].x * Din[(j - s) & mask] + ac[k].y * Din[(j + s) & mask];
+        }
+        __syncthreads();
+    }
+    const float* Dn = (levels & 1) ? D1 : D0;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int j = threadIdx.x + k * kSolveBlock;
         if (j < nP) {
-            float zj;
-            if (decoupled) {
-                zj = D[j] / (E[j] + L[j] + U[j]);
-            } else {
-                const int kk = (j + nP / 2) & mask;
-                const float mj = L[j] + U[j], mk = L[kk] + U[kk];
-                const float ej = E[j], ek = E[kk];
-                const float det = ej * ek + ej * mk + mj * ek;
-                zj = (D[j] * (ek + mk) + mj * D[kk]) / det;
-            }
+            const float2 cc = acn[k];  // the final factors
+            const float zj = cc.x * Dn[j] + cc.y * Dn[(j + nP / 2) & mask];
             const int c = row + j;
             const float rc = f.r[c];
             f.z[c] = zj;
@@ -207,7 +281,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
 // on the fly, for the neighbouring rows it reads, so one grid barrier per
 // iteration is saved.
 template <bool MIXED, int PER>
-__global__ void __launch_bounds__(kSolveBlock, 3)
+__global__ void __launch_bounds__(kSolveBlock, 4)
 k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
     extern __shared__ float sm[];
     cg::grid_group grid = cg::this_grid();
@@ -231,7 +305,7 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
                 c2 += b * b;
             }
             __syncthreads();
-            precondition_row<MIXED, PER>(g, f, cfg, i, sm, a, b2);
+            precondition_row<MIXED, PER, true>(g, f, cfg, i, sm, a, b2);
         }
         block_partial3(a, b2, c2, partA);
     }
@@ -267,7 +341,7 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
             // restart CG from the refined iterate
             double a2 = 0, b2 = 0;
             for (int i = blockIdx.x; i < nT; i += G) {
-                precondition_row<MIXED, PER>(g, f, cfg, i, sm, a2, b2);
+                precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, a2, b2);
             }
             block_partial3(a2, b2, 0.0, partA);
             grid.sync();
@@ -315,7 +389,7 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
                 f.r[c] = f.r[c] - af * f.x[c];
             }
             __syncthreads();
-            precondition_row<MIXED, PER>(g, f, cfg, i, sm, rz2, rr2);
+            precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, rz2, rr2);
         }
         block_partial3(rz2, rr2, 0.0, partB);
         grid.sync();
@@ -328,35 +402,21 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
         pnew = t;
         ++it;
     }
-    // final increment, new gamma, and the true relative residual of the
-    // returned (FP32) gamma
+    // final increment and new gamma.  The reported residual is the FP64
+    // residual of the refined iterate checked above (mixed mode; it is held
+    // to 0.8 tol so that the FP32-rounded gamma also meets tol) or the
+    // recursive residual (plain mode).
     for (int i = blockIdx.x; i < nT; i += G)
         for (int j = threadIdx.x; j < nP; j += blockDim.x) {
             const int c = i * nP + j;
             const float dx = MIXED ? (float)f.x64[c] : f.dx[c];
             const float g0 = f.gam_adv[c];
-            const float xn = g0 + dx;
             f.dx[c] = dx;
-            f.x[c] = xn;
-            f.q[c] = xn - g0;  // stored increment, exact in FP32
+            f.x[c] = g0 + dx;
         }
-    grid.sync();
-    {
-        double a = 0;
-        for (int i = blockIdx.x; i < nT; i += G)
-            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                const int c = i * nP + j;
-                const double r = (double)f.r0[c] - apply_A<float, double>(g, f, f.q, c, i, j);
-                a += r * r;
-            }
-        block_partial3(a, 0.0, 0.0, partA);
-    }
-    grid.sync();
-    double res2, d1, d2;
-    all_sum3(partA, G, res2, d1, d2);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         f.stats->solver_iters = it;
-        f.stats->solver_rel_resid = sqrt(res2) / bnorm;
+        f.stats->solver_rel_resid = sqrt(rr) / bnorm;
         f.stats->solver_b_norm = bnorm;
         f.stats->solver_converged = conv ? 1 : 0;
     }
