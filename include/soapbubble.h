@@ -62,6 +62,8 @@ typedef struct {
     double solver_tol;    /* relative residual target (0 -> 1e-6) */
     int solver_max_iter;  /* (0 -> 1000) */
     int force_reinit;     /* 0: decide by distortion > 4; 1: never; 2: every step */
+    double nu_scale;      /* multiplies the air's kinematic viscosity in the drag
+                             coefficient Cr (0 -> 1) */
 } sb_params;
 
 /* Diagnostics of the most recent step (the reference prints these:
@@ -202,6 +204,49 @@ void* sb_stream(sb_bubble* b);
 
 /* Message for the last failing call on this thread. */
 const char* sb_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * Batches: an ensemble of bubbles (any mix of grid sizes on one device)
+ * stepped together, one kernel launch per stage for all members.
+ *
+ * The reference has no counterpart; it steps one Solver per process
+ * (Bubble::run, kernel/bubble.cu:2607-2704).  A batch step gives every
+ * member exactly the result of sb_step on that member alone: the kernels
+ * run the same per-cell code and the implicit solve keeps its own
+ * reductions, iteration count and stopping test per member.
+ *
+ * Members stay owned by the caller and must outlive the batch; while a
+ * batch exists, step its members only through it (sb_step on a member
+ * would desynchronise the batch's view of its double-buffered maps).
+ * Field I/O and statistics on members remain available after
+ * sb_batch_synchronize.  All members share one solver configuration, the
+ * first member's; the step time t and dt are common to all members.
+ * ------------------------------------------------------------------------ */
+typedef struct sb_batch sb_batch;
+
+/* Builds the batch's tables (per-member descriptors, cell tiles of 64, 128
+ * and 256 cells, solve-block ranges).  Synchronises the members' streams. */
+int sb_batch_create(sb_bubble* const* members, int n, sb_batch** out);
+int sb_batch_destroy(sb_batch* batch);
+
+/* n_steps steps of every member at time t_frame, step dt (seconds).
+ * Replays one captured CUDA graph per step on the batch's stream. */
+int sb_batch_step(sb_batch* batch, int n_steps, double t_frame, double dt);
+
+/* As sb_batch_step but launching stage by stage and adding each stage's
+ * device time (ms) to stage_ms[0 .. sb_stage_count()-1]; synchronises. */
+int sb_batch_step_timed(sb_batch* batch, int n_steps, double t_frame, double dt,
+                        double* stage_ms);
+
+/* Times one step per tile size (64, 128, 256 cells per block) and keeps the
+ * fastest for each stage; tile_sizes (optional, sb_stage_count() ints)
+ * receives the choice.  The tuning steps advance the members (3 steps). */
+int sb_batch_autotune(sb_batch* batch, double t_frame, double dt, int* tile_sizes);
+
+int sb_batch_synchronize(sb_batch* batch);
+
+/* CUDA stream of the batch (cudaStream_t). */
+void* sb_batch_stream(sb_batch* batch);
 
 #ifdef __cplusplus
 }

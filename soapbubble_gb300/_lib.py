@@ -29,6 +29,7 @@ class SbParams(C.Structure):
         ("blendCoeff", C.c_double), ("device", C.c_int),
         ("gs_scale", C.c_double), ("M_scale", C.c_double), ("solver_mode", C.c_int),
         ("solver_tol", C.c_double), ("solver_max_iter", C.c_int), ("force_reinit", C.c_int),
+        ("nu_scale", C.c_double),
     ]
 
 
@@ -97,10 +98,21 @@ def lib() -> C.CDLL:
     L.sb_stream.restype = C.c_void_p
     L.sb_last_error.argtypes = []
     L.sb_last_error.restype = C.c_char_p
+    ip = C.POINTER(C.c_int)
+    L.sb_batch_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]
+    L.sb_batch_destroy.argtypes = [H]
+    L.sb_batch_step.argtypes = [H, C.c_int, C.c_double, C.c_double]
+    L.sb_batch_step_timed.argtypes = [H, C.c_int, C.c_double, C.c_double, dp]
+    L.sb_batch_autotune.argtypes = [H, C.c_double, C.c_double, ip]
+    L.sb_batch_synchronize.argtypes = [H]
+    L.sb_batch_stream.argtypes = [H]
+    L.sb_batch_stream.restype = C.c_void_p
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
                  "sb_download_field", "sb_step", "sb_step_timed", "sb_upload_field_f32",
                  "sb_download_field_f32", "sb_synchronize", "sb_get_stats",
-                 "sb_update_mass", "sb_write_thickness_exr", "sb_run"):
+                 "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
+                 "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
+                 "sb_batch_autotune", "sb_batch_synchronize"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -117,4 +129,5 @@ EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_step_timed", "sb_stage_count", "sb_stage_name", "sb_upload_field_f32",
            "sb_download_field_f32", "sb_synchronize", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
            "sb_run", "sb_write_exr_gray", "sb_mass_integrals_noalloc", "sb_bytes_required",
-           "sb_stream", "sb_last_error"]
+           "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",
+           "sb_batch_step_timed", "sb_batch_autotune", "sb_batch_synchronize", "sb_batch_stream"]

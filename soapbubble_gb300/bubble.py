@@ -32,7 +32,8 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
                 Gamma_m: float = 1e-6, T: float = 298.15, blendCoeff: float = 0.5,
                 DT: Optional[float] = None, frames: int = 1, solver_mode: int = 0,
                 solver_tol: float = 1e-6, solver_max_iter: int = 1000, force_reinit: int = 0,
-                gs_scale: float = 0.0, M_scale: float = 0.0, device: int = 0) -> SbParams:
+                gs_scale: float = 0.0, M_scale: float = 0.0, nu_scale: float = 0.0,
+                device: int = 0) -> SbParams:
     p = default_params()
     p.nTheta, p.dt, p.radius, p.H, p.Gamma_m, p.T = nTheta, dt, radius, H, Gamma_m, T
     p.blendCoeff = blendCoeff
@@ -40,6 +41,7 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
     p.frames = frames
     p.solver_mode, p.solver_tol, p.solver_max_iter = solver_mode, solver_tol, solver_max_iter
     p.force_reinit, p.gs_scale, p.M_scale, p.device = force_reinit, gs_scale, M_scale, device
+    p.nu_scale = nu_scale
     return p
 
 
@@ -148,6 +150,57 @@ class GpuBubble:
 
     def stream(self) -> int:
         return lib().sb_stream(self.h)
+
+
+class GpuBatch:
+    """An ensemble of GpuBubbles stepped together (sb_batch_*): one kernel
+    launch per stage for all members, one CUDA graph per step.  The members
+    stay owned by the caller; step them only through the batch while it
+    exists, and synchronize() before reading their fields."""
+
+    def __init__(self, members):
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        h = C.c_void_p()
+        check(lib().sb_batch_create(arr, len(self.members), C.byref(h)), "sb_batch_create")
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib().sb_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def step(self, n: int, t: float, dt: float) -> None:
+        check(lib().sb_batch_step(self.h, n, t, dt), "sb_batch_step")
+
+    def step_timed(self, n: int, t: float, dt: float, stage_ms: np.ndarray) -> None:
+        assert stage_ms.dtype == np.float64 and stage_ms.size >= lib().sb_stage_count()
+        check(lib().sb_batch_step_timed(self.h, n, t, dt, _dp(stage_ms)), "sb_batch_step_timed")
+
+    def autotune(self, t: float, dt: float) -> list:
+        """Picks each stage's tile size (three tuning steps advance the
+        members); returns the chosen cells per block by stage."""
+        out = (C.c_int * lib().sb_stage_count())()
+        check(lib().sb_batch_autotune(self.h, t, dt, out), "sb_batch_autotune")
+        return list(out)
+
+    def synchronize(self) -> None:
+        check(lib().sb_batch_synchronize(self.h), "sb_batch_synchronize")
+
+    def stream(self) -> int:
+        return lib().sb_batch_stream(self.h)
 
 
 def stage_names() -> list:

@@ -95,7 +95,8 @@ void derive_phys(const sb_params& p, SbPhys& ph) {
     if (p.M_scale > 0) M *= p.M_scale;
     if (p.gs_scale > 0) gs *= p.gs_scale;
     ph.M = (float)M;
-    ph.Cr = (float)(kRhoA * std::sqrt(kNuA * p.radius / U) / (kRho * p.H));
+    const double nuA = kNuA * (p.nu_scale > 0 ? p.nu_scale : 1.0);
+    ph.Cr = (float)(kRhoA * std::sqrt(nuA * p.radius / U) / (kRho * p.H));
     ph.gs = (float)gs;
     ph.gmax = (float)(kSigmaA / sigma_r / p.Gamma_m);
     ph.blend = (float)p.blendCoeff;
@@ -216,11 +217,12 @@ float2* map_ptr(sb_bubble* b, sb_field w, int& comp) {
     }
 }
 
-int set_step_params(sb_bubble* b, double t, double dt_s) {
-    if (dt_s == b->last_dt && t == b->last_t) return SB_OK;
+// Writes the per-step scalars into the pinned slot and copies them to the
+// device on `stream`; the caller makes sure no earlier copy of the slot is
+// still in flight.
+int write_step_params(sb_bubble* b, double t, double dt_s, cudaStream_t stream) {
     const double dtn = dt_s * 1.0 / b->params.radius;  // dt U / r with U = 1
     SbStepParams* s = b->h_step;
-    SB_CHECK(cudaStreamSynchronize(b->stream));  // the pinned slot may be in flight
     s->dt = (float)dtn;
     s->invDt = (float)(1.0 / dtn);
     s->windg = (float)(3.0 - std::fabs(t - 3.0));
@@ -229,10 +231,16 @@ int set_step_params(sb_bubble* b, double t, double dt_s) {
     s->evapDt = (float)((double)b->ph.evap * dtn);
     s->gsdt = 0.f;
     s->pad = 0.f;
-    SB_CHECK(cudaMemcpyAsync(b->f.step, s, sizeof(SbStepParams), cudaMemcpyHostToDevice, b->stream));
+    SB_CHECK(cudaMemcpyAsync(b->f.step, s, sizeof(SbStepParams), cudaMemcpyHostToDevice, stream));
     b->last_dt = dt_s;
     b->last_t = t;
     return SB_OK;
+}
+
+int set_step_params(sb_bubble* b, double t, double dt_s) {
+    if (dt_s == b->last_dt && t == b->last_t) return SB_OK;
+    SB_CHECK(cudaStreamSynchronize(b->stream));  // the pinned slot may be in flight
+    return write_step_params(b, t, dt_s, b->stream);
 }
 
 int reset_bimocq(sb_bubble* b) {
@@ -759,5 +767,298 @@ int sb_write_exr_gray(const char* path, int width, int height, const float* img)
 void* sb_stream(sb_bubble* b) { return b ? (void*)b->stream : nullptr; }
 
 const char* sb_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many bubbles stepped together, one launch per stage.
+// ---------------------------------------------------------------------------
+
+struct sb_batch {
+    std::vector<sb_bubble*> m;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    char* arena = nullptr;
+    SbBubbleDesc* d_descs = nullptr;
+    int2* d_tiles[3] = {};
+    int ntiles[3] = {};
+    int* d_blk_bubble = nullptr;
+    int* d_first = nullptr;
+    int* d_nblk = nullptr;
+    double* d_partials = nullptr;
+    int* d_nactive = nullptr;
+    int G = 0;
+    int maxNP = 0;
+    SolverConfig solver;
+    int sel[STAGE_COUNT] = {1, 1, 1, 1, 1, 1, 1, 1};  // tile size index per stage
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev[STAGE_COUNT + 2] = {};
+    long long steps = 0;
+    long long launches = 0;
+    double last_t = -1e300, last_dt = -1;
+};
+
+namespace {
+
+const int kTileSizes[3] = {64, 128, 256};
+
+// Launches stage `st` of the batch (the solve and re-initialisation are
+// cooperative launches over the whole batch).
+cudaError_t batch_stage(sb_batch* B, int st) {
+    if (st == STAGE_SOLVE) {
+        SbBatchSolve bs;
+        bs.descs = B->d_descs;
+        bs.nb = (int)B->m.size();
+        bs.blk_bubble = B->d_blk_bubble;
+        bs.bub_first_blk = B->d_first;
+        bs.bub_nblk = B->d_nblk;
+        bs.partials = B->d_partials;
+        bs.nactive = B->d_nactive;
+        return launch_solve_batch(bs, B->G, B->maxNP, B->solver, B->stream);
+    }
+    if (st == STAGE_REINIT)
+        return launch_reinit_batch(B->d_descs, (int)B->m.size(), B->d_tiles[1], B->ntiles[1],
+                                   B->stream);
+    const int k = B->sel[st];
+    return launch_stage_batch(st, B->d_descs, B->d_tiles[k], B->ntiles[k], kTileSizes[k], B->stream);
+}
+
+cudaError_t batch_step_launches(sb_batch* B) {
+    for (int st = 0; st < STAGE_COUNT; ++st) {
+        cudaError_t e = batch_stage(B, st);
+        if (e != cudaSuccess) return e;
+    }
+    return launch_flip_batch(B->d_descs, (int)B->m.size(), B->stream);
+}
+
+int batch_set_params(sb_batch* B, double t, double dt) {
+    if (t == B->last_t && dt == B->last_dt) return SB_OK;
+    SB_CHECK(cudaStreamSynchronize(B->stream));  // pinned slots may be in flight
+    for (sb_bubble* b : B->m) {
+        int rc = write_step_params(b, t, dt, B->stream);
+        if (rc != SB_OK) return rc;
+    }
+    B->last_t = t;
+    B->last_dt = dt;
+    return SB_OK;
+}
+
+void batch_advance(sb_batch* B, int n) {
+    B->steps += n;
+    B->launches += (long long)n * (STAGE_COUNT + 1);
+    for (sb_bubble* b : B->m) {
+        b->steps += n;
+        b->launches += (long long)n * (STAGE_COUNT + 1);
+        b->cur ^= (n & 1);
+        b->last_t = -1e300;  // the bubble's own stream did not see the batch's copies
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
+    if (!out || !bubbles || n <= 0) return fail(SB_ERR_INVALID, "bad batch arguments");
+    *out = nullptr;
+    sb_batch* B = new sb_batch();
+    B->device = bubbles[0]->device;
+    B->solver = bubbles[0]->solver;
+    for (int k = 0; k < n; ++k) {
+        sb_bubble* b = bubbles[k];
+        if (!b || b->device != B->device) {
+            delete B;
+            return fail(SB_ERR_INVALID, "batch members must be valid bubbles on one device");
+        }
+        const SolverConfig& c = b->solver;
+        if (c.mode != B->solver.mode || c.max_iter != B->solver.max_iter ||
+            c.tol != B->solver.tol || c.precond != B->solver.precond) {
+            delete B;
+            return fail(SB_ERR_INVALID, "batch members must share one solver configuration");
+        }
+        B->m.push_back(b);
+        if (b->g.nP > B->maxNP) B->maxNP = b->g.nP;
+    }
+    cudaError_t e = cudaSetDevice(B->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
+    int Gmax = 0;
+    if (e == cudaSuccess) e = prepare_solve_batch(B->maxNP, B->solver, &Gmax);
+    if (e == cudaSuccess) reinit_batch_blocks();
+    if (e != cudaSuccess) {
+        int r = cuda_fail(e, "sb_batch_create");
+        sb_batch_destroy(B);
+        return r;
+    }
+    // solve blocks per bubble, proportional to rows, at least one each
+    long long rows = 0;
+    for (sb_bubble* b : B->m) rows += b->g.nT;
+    if (Gmax < n) {
+        sb_batch_destroy(B);
+        return fail(SB_ERR_INVALID, "too many bubbles for one batch solve");
+    }
+    std::vector<int> nblk(n), first(n);
+    int G = 0;
+    for (int k = 0; k < n; ++k) {
+        long long want = (long long)Gmax * B->m[k]->g.nT / rows;
+        nblk[k] = (int)std::max<long long>(1, std::min<long long>(want, B->m[k]->g.nT));
+        G += nblk[k];
+    }
+    while (G > Gmax) {
+        int big = 0;
+        for (int k = 1; k < n; ++k)
+            if (nblk[k] > nblk[big]) big = k;
+        --nblk[big];
+        --G;
+    }
+    std::vector<int> blk_bubble(G);
+    for (int k = 0, at = 0; k < n; ++k) {
+        first[k] = at;
+        for (int q = 0; q < nblk[k]; ++q) blk_bubble[at++] = k;
+    }
+    B->G = G;
+    // tiles for the three tile sizes
+    std::vector<int2> tiles[3];
+    for (int s = 0; s < 3; ++s) {
+        for (int k = 0; k < n; ++k)
+            for (int c = 0; c < B->m[k]->g.N; c += kTileSizes[s]) tiles[s].push_back(make_int2(k, c));
+        B->ntiles[s] = (int)tiles[s].size();
+    }
+    Layout L;
+    const size_t o_desc = L.take(sizeof(SbBubbleDesc) * n);
+    size_t o_tiles[3];
+    for (int s = 0; s < 3; ++s) o_tiles[s] = L.take(sizeof(int2) * tiles[s].size());
+    const size_t o_bb = L.take(sizeof(int) * G), o_first = L.take(sizeof(int) * n),
+                 o_nblk = L.take(sizeof(int) * n), o_part = L.take(sizeof(double) * 6 * G),
+                 o_act = L.take(sizeof(int) * 4);
+    e = cudaMalloc((void**)&B->arena, L.bytes);
+    if (e != cudaSuccess) {
+        int r = cuda_fail(e, "sb_batch_create allocation");
+        sb_batch_destroy(B);
+        return r;
+    }
+    char* A = B->arena;
+    B->d_descs = (SbBubbleDesc*)(A + o_desc);
+    for (int s = 0; s < 3; ++s) B->d_tiles[s] = (int2*)(A + o_tiles[s]);
+    B->d_blk_bubble = (int*)(A + o_bb);
+    B->d_first = (int*)(A + o_first);
+    B->d_nblk = (int*)(A + o_nblk);
+    B->d_partials = (double*)(A + o_part);
+    B->d_nactive = (int*)(A + o_act);
+    std::vector<SbBubbleDesc> descs(n);
+    for (int k = 0; k < n; ++k) {
+        sb_bubble* b = B->m[k];
+        descs[k].g = b->g;
+        descs[k].ph = b->ph;
+        descs[k].f = b->f;
+        descs[k].cur = b->cur;
+        descs[k].pad = 0;
+    }
+    // members may have work queued on their own streams
+    for (sb_bubble* b : B->m) e = e == cudaSuccess ? cudaStreamSynchronize(b->stream) : e;
+    if (e == cudaSuccess) e = cudaMemcpy(B->d_descs, descs.data(), sizeof(SbBubbleDesc) * n, cudaMemcpyHostToDevice);
+    for (int s = 0; s < 3 && e == cudaSuccess; ++s)
+        e = cudaMemcpy(B->d_tiles[s], tiles[s].data(), sizeof(int2) * tiles[s].size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(B->d_blk_bubble, blk_bubble.data(), sizeof(int) * G, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(B->d_first, first.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(B->d_nblk, nblk.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(B->d_nactive, 0, sizeof(int) * 4);
+    if (e != cudaSuccess) {
+        int r = cuda_fail(e, "sb_batch_create upload");
+        sb_batch_destroy(B);
+        return r;
+    }
+    *out = B;
+    return SB_OK;
+}
+
+int sb_batch_destroy(sb_batch* B) {
+    if (!B) return SB_OK;
+    cudaSetDevice(B->device);
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    if (B->graph) cudaGraphExecDestroy(B->graph);
+    for (cudaEvent_t e : B->ev)
+        if (e) cudaEventDestroy(e);
+    if (B->arena) cudaFree(B->arena);
+    if (B->stream) cudaStreamDestroy(B->stream);
+    delete B;
+    return SB_OK;
+}
+
+int sb_batch_step(sb_batch* B, int n_steps, double t_frame, double dt) {
+    if (!B) return fail(SB_ERR_INVALID, "null batch");
+    if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
+    SB_CHECK(cudaSetDevice(B->device));
+    int rc = batch_set_params(B, t_frame, dt);
+    if (rc != SB_OK) return rc;
+    if (!B->graph && n_steps > 0) {
+        cudaGraph_t graph = nullptr;
+        SB_CHECK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = batch_step_launches(B);
+        cudaError_t e2 = cudaStreamEndCapture(B->stream, &graph);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&B->graph, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
+    }
+    for (int s = 0; s < n_steps; ++s) SB_CHECK(cudaGraphLaunch(B->graph, B->stream));
+    batch_advance(B, n_steps);
+    return SB_OK;
+}
+
+int sb_batch_step_timed(sb_batch* B, int n_steps, double t_frame, double dt, double* stage_ms) {
+    if (!B || !stage_ms) return fail(SB_ERR_INVALID, "null argument");
+    SB_CHECK(cudaSetDevice(B->device));
+    int rc = batch_set_params(B, t_frame, dt);
+    if (rc != SB_OK) return rc;
+    if (!B->ev[0])
+        for (cudaEvent_t& e : B->ev) SB_CHECK(cudaEventCreate(&e));
+    for (int s = 0; s < n_steps; ++s) {
+        SB_CHECK(cudaEventRecord(B->ev[0], B->stream));
+        for (int st = 0; st < STAGE_COUNT; ++st) {
+            SB_CHECK(batch_stage(B, st));
+            SB_CHECK(cudaEventRecord(B->ev[st + 1], B->stream));
+        }
+        SB_CHECK(launch_flip_batch(B->d_descs, (int)B->m.size(), B->stream));
+        SB_CHECK(cudaEventSynchronize(B->ev[STAGE_COUNT]));
+        for (int st = 0; st < STAGE_COUNT; ++st) {
+            float ms = 0.f;
+            SB_CHECK(cudaEventElapsedTime(&ms, B->ev[st], B->ev[st + 1]));
+            stage_ms[st] += ms;
+        }
+        batch_advance(B, 1);
+    }
+    return SB_OK;
+}
+
+int sb_batch_autotune(sb_batch* B, double t_frame, double dt, int* tile_sizes) {
+    if (!B) return fail(SB_ERR_INVALID, "null batch");
+    double ms[3][STAGE_COUNT + 1] = {};
+    for (int k = 0; k < 3; ++k) {
+        for (int st = 0; st < STAGE_COUNT; ++st) B->sel[st] = k;
+        int rc = sb_batch_step_timed(B, 1, t_frame, dt, ms[k]);
+        if (rc != SB_OK) return rc;
+    }
+    for (int st = 0; st < STAGE_COUNT; ++st) {
+        int best = 1;
+        for (int k = 0; k < 3; ++k)
+            if (ms[k][st] < ms[best][st]) best = k;
+        B->sel[st] = best;
+        if (tile_sizes) tile_sizes[st] = kTileSizes[best];
+    }
+    if (B->graph) {
+        cudaGraphExecDestroy(B->graph);
+        B->graph = nullptr;
+    }
+    return SB_OK;
+}
+
+int sb_batch_synchronize(sb_batch* B) {
+    if (!B) return fail(SB_ERR_INVALID, "null batch");
+    SB_CHECK(cudaSetDevice(B->device));
+    SB_CHECK(cudaStreamSynchronize(B->stream));
+    return SB_OK;
+}
+
+void* sb_batch_stream(sb_batch* B) { return B ? (void*)B->stream : nullptr; }
 
 }  // extern "C"

@@ -32,6 +32,15 @@ struct SbFields {
     SbDevStats* stats;
 };
 
+// One bubble of a batch, as the batched kernels see it (device memory).
+struct SbBubbleDesc {
+    SbGrid g;
+    SbPhys ph;
+    SbFields f;
+    int cur;   // map parity, flipped on the device after every batch step
+    int pad;
+};
+
 struct SolverConfig {
     int mode;       // 0: plain FP32, 1: mixed precision (FP64 dots + refinement)
     int max_iter;
@@ -61,6 +70,30 @@ cudaError_t prepare_launches(const SbGrid& g, const struct SolverConfig& cfg);
 cudaError_t prepare_solve(const SbGrid& g, const struct SolverConfig& cfg);
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s);
 cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s);
+
+// Batched stages: one launch per stage over the tiles of every bubble.
+// tiles[k] = (bubble, first cell) of block k; `block` threads per tile.
+cudaError_t launch_stage_batch(int stage, const SbBubbleDesc* descs, const int2* tiles, int ntiles,
+                               int block, cudaStream_t s);
+cudaError_t launch_reinit_batch(const SbBubbleDesc* descs, int nb, const int2* tiles, int ntiles,
+                                cudaStream_t s);
+cudaError_t launch_flip_batch(SbBubbleDesc* descs, int nb, cudaStream_t s);
+int reinit_batch_blocks();
+
+// Batched implicit solve: every bubble's rows are owned by its own
+// contiguous range of blocks.
+struct SbBatchSolve {
+    const SbBubbleDesc* descs;
+    int nb;
+    const int* blk_bubble;     // [G] bubble of each block
+    const int* bub_first_blk;  // [nb]
+    const int* bub_nblk;       // [nb]
+    double* partials;          // [2 * 3 * G]
+    int* nactive;              // [3] bubbles still iterating (rotating counters)
+};
+cudaError_t prepare_solve_batch(int maxNP, const SolverConfig& cfg, int* blocks);
+cudaError_t launch_solve_batch(const SbBatchSolve& bs, int G, int maxNP, const SolverConfig& cfg,
+                               cudaStream_t s);
 
 // Implicit surfactant solve (sb_solver.cu).
 cudaError_t launch_solve(const SbGrid& g, const SbPhys& ph, const SbFields& f,

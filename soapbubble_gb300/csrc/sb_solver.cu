@@ -422,6 +422,213 @@ k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
     }
 }
 
+// Sum of the partials of blocks [first, first + nblk), same order in every
+// block of that range.
+__device__ __forceinline__ void range_sum3(const double* part, int first, int nblk, double& A,
+                                           double& B, double& C) {
+    __shared__ double res[3];
+    if (threadIdx.x < 32) {
+        double x = 0.0, y = 0.0, z = 0.0;
+        for (int k = threadIdx.x; k < nblk; k += 32) {
+            x += part[3 * (first + k) + 0];
+            y += part[3 * (first + k) + 1];
+            z += part[3 * (first + k) + 2];
+        }
+        x = warp_sum(x); y = warp_sum(y); z = warp_sum(z);
+        if (threadIdx.x == 0) { res[0] = x; res[1] = y; res[2] = z; }
+    }
+    __syncthreads();
+    A = res[0]; B = res[1]; C = res[2];
+    __syncthreads();
+}
+
+// Batched PCG: k_pcg for every bubble of a batch in one cooperative launch.
+// Block k works on bubble blk_bubble[k]; a bubble's blocks are a contiguous
+// range and reduce only their own partials, in the same order as k_pcg, so
+// a bubble that gets as many blocks as its own k_pcg launch would have
+// produces bit-identical results.  The loop runs in slots of two grid
+// barriers; in each slot a bubble either does one CG iteration (ITER), or
+// the mixed-precision true-residual check followed by the restart (CHECK),
+// or nothing (DONE).  These are the branches of k_pcg's loop in the same
+// order.  The number of bubbles not yet done is counted on rotating
+// counters one barrier ahead of its use, so every block agrees on when to
+// stop without an extra barrier.
+template <bool MIXED, int PER>
+__global__ void __launch_bounds__(kSolveBlock, 4)
+k_pcg_batch(SbBatchSolve bs, SolverConfig cfg) {
+    enum { ITER = 0, CHECK = 1, DONE = 2 };
+    extern __shared__ float sm[];
+    cg::grid_group grid = cg::this_grid();
+    const int G = gridDim.x;
+    const int bub = bs.blk_bubble[blockIdx.x];
+    const int first = bs.bub_first_blk[bub], nblk = bs.bub_nblk[bub];
+    const int lb = blockIdx.x - first;
+    const SbBubbleDesc& d = bs.descs[bub];
+    const SbGrid& g = d.g;
+    const SbFields& f = d.f;
+    const int nP = g.nP, nT = g.nT;
+    double* partA = bs.partials;
+    double* partB = bs.partials + 3 * G;
+    const bool lead = (lb == 0 && threadIdx.x == 0);
+    if (blockIdx.x == 0 && threadIdx.x < 3) bs.nactive[threadIdx.x] = 0;
+
+    // dx = 0, r = r0, z = M^-1 r (p_old = 0, beta = 0)
+    double rz = 0, rr = 0, bb = 0;
+    {
+        double a = 0, b2 = 0, c2 = 0;
+        for (int i = lb; i < nT; i += nblk) {
+            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                const int c = i * nP + j;
+                if (MIXED) f.x64[c] = 0.0;
+                else f.dx[c] = 0.0f;
+                f.r[c] = f.r0[c];
+                f.q[c] = 0.0f;  // p_old
+                const double bv = (double)f.rhs[c];
+                c2 += bv * bv;
+            }
+            __syncthreads();
+            precondition_row<MIXED, PER, true>(g, f, cfg, i, sm, a, b2);
+        }
+        block_partial3(a, b2, c2, partA);
+    }
+    grid.sync();
+    range_sum3(partA, first, nblk, rz, rr, bb);
+    const double bnorm = bb > 0.0 ? sqrt(bb) : 1.0;
+    const double tol2 = (MIXED ? 0.64 : 1.0) * cfg.tol * cfg.tol * bnorm * bnorm;
+    float* pold = f.q;
+    float* pnew = f.p;
+    float beta = 0.0f;
+    int it = 0;
+    bool conv = false;
+    // the loop head of k_pcg: iteration limit, NaN, target reached
+    auto next_state = [&]() -> int {
+        if (it >= cfg.max_iter || !(rr == rr)) return DONE;
+        if (rr <= tol2) {
+            if (!MIXED) { conv = true; return DONE; }
+            return CHECK;
+        }
+        return ITER;
+    };
+    int state = next_state();
+    if (state != DONE && lead) atomicAdd(&bs.nactive[0], 1);
+    for (int k = 0;; ++k) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) bs.nactive[(k + 2) % 3] = 0;
+        // first half: q = A p_new (ITER) or the true residual (CHECK)
+        double s1 = 0;
+        if (state == ITER) {
+            for (int i = lb; i < nT; i += nblk)
+                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                    const int c = i * nP + j;
+                    const int e = i * nP + ((j + 1) & g.maskP);
+                    const int w = i * nP + ((j - 1) & g.maskP);
+                    const float pc = f.z[c] + beta * pold[c];
+                    pnew[c] = pc;
+                    float qf = f.dmass[c] * pc + f.cE[c] * (pc - (f.z[e] + beta * pold[e])) +
+                               f.cE[w] * (pc - (f.z[w] + beta * pold[w]));
+                    if (i < nT - 1) {
+                        const int sc = c + nP;
+                        qf += f.cS[c] * (pc - (f.z[sc] + beta * pold[sc]));
+                    }
+                    if (i > 0) {
+                        const int nc = c - nP;
+                        qf += f.cS[nc] * (pc - (f.z[nc] + beta * pold[nc]));
+                    }
+                    f.x[c] = qf;  // q lives in x until the final phase
+                    s1 += MIXED ? (double)pc * (double)qf : (double)(pc * qf);
+                }
+        } else if (MIXED && state == CHECK) {
+            for (int i = lb; i < nT; i += nblk)
+                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                    const int c = i * nP + j;
+                    const double r = (double)f.r0[c] - apply_A<double, double>(g, f, f.x64, c, i, j);
+                    f.r[c] = (float)r;
+                    s1 += r * r;
+                }
+        }
+        block_partial3(s1, 0.0, 0.0, partA);
+        grid.sync();
+        if (bs.nactive[k % 3] == 0) break;  // same value in every block
+        double r1, d1, d2;
+        range_sum3(partA, first, nblk, r1, d1, d2);
+        // second half: update and precondition (ITER) or restart (CHECK)
+        double rz2 = 0, rr2 = 0;
+        if (state == ITER) {
+            if (!(r1 > 0.0)) {
+                state = DONE;  // breakdown: keep the current iterate
+            } else {
+                const double alpha = rz / r1;
+                const float af = (float)alpha;
+                for (int i = lb; i < nT; i += nblk) {
+                    for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+                        const int c = i * nP + j;
+                        const float pc = pnew[c];
+                        if (MIXED) f.x64[c] += alpha * (double)pc;
+                        else f.dx[c] += af * pc;
+                        f.r[c] = f.r[c] - af * f.x[c];
+                    }
+                    __syncthreads();
+                    precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, rz2, rr2);
+                }
+            }
+        } else if (state == CHECK) {
+            rr = r1;
+            if (rr <= tol2) {
+                conv = true;
+                state = DONE;
+            } else {
+                for (int i = lb; i < nT; i += nblk)
+                    precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, rz2, rr2);
+            }
+        }
+        block_partial3(rz2, rr2, 0.0, partB);
+        grid.sync();
+        double d3;
+        range_sum3(partB, first, nblk, rz2, rr2, d3);
+        if (state == ITER) {
+            beta = (float)(rz2 / rz);
+            rz = rz2;
+            rr = rr2;
+            float* t = pold;
+            pold = pnew;
+            pnew = t;
+            ++it;
+            state = next_state();
+        } else if (state == CHECK) {
+            // restarted from the refined iterate: the next slot iterates
+            rz = rz2;
+            rr = rr2;
+            beta = 0.0f;
+            state = ITER;
+        }
+        if (state != DONE && lead) atomicAdd(&bs.nactive[(k + 1) % 3], 1);
+    }
+    // final increment and new gamma, as k_pcg
+    for (int i = lb; i < nT; i += nblk)
+        for (int j = threadIdx.x; j < nP; j += blockDim.x) {
+            const int c = i * nP + j;
+            const float dx = MIXED ? (float)f.x64[c] : f.dx[c];
+            const float g0 = f.gam_adv[c];
+            f.dx[c] = dx;
+            f.x[c] = g0 + dx;
+        }
+    if (lead) {
+        f.stats->solver_iters = it;
+        f.stats->solver_rel_resid = sqrt(rr) / bnorm;
+        f.stats->solver_b_norm = bnorm;
+        f.stats->solver_converged = conv ? 1 : 0;
+    }
+}
+
+template <bool MIXED>
+const void* pcg_batch_kernel(int per) {
+    switch (per) {
+        case 1: return (const void*)k_pcg_batch<MIXED, 1>;
+        case 2: return (const void*)k_pcg_batch<MIXED, 2>;
+        case 4: return (const void*)k_pcg_batch<MIXED, 4>;
+        default: return (const void*)k_pcg_batch<MIXED, 8>;
+    }
+}
+
 template <bool MIXED>
 const void* pcg_kernel(int per) {
     switch (per) {
@@ -465,6 +672,34 @@ int solve_blocks(const SbGrid& g) {
 }  // namespace
 
 int solver_partials_needed(const SbGrid& g) { return 6 * solve_blocks(g); }
+
+cudaError_t prepare_solve_batch(int maxNP, const SolverConfig& cfg, int* blocks) {
+    if (maxNP > 8 * kSolveBlock) return cudaErrorInvalidValue;
+    const size_t smem = 4 * sizeof(float) * (size_t)maxNP;
+    const int per = per_of(maxNP);
+    const void* fn = cfg.mode == 1 ? pcg_batch_kernel<true>(per) : pcg_batch_kernel<false>(per);
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolveBlock, smem);
+    *blocks = sms * (occ > 0 ? occ : 1);
+    return e;
+}
+
+cudaError_t launch_solve_batch(const SbBatchSolve& bs, int G, int maxNP, const SolverConfig& cfg,
+                               cudaStream_t s) {
+    const size_t smem = 4 * sizeof(float) * (size_t)maxNP;
+    SbBatchSolve bb = bs;
+    SolverConfig cc = cfg;
+    void* args[] = {&bb, &cc};
+    const int per = per_of(maxNP);
+    const void* fn = cfg.mode == 1 ? pcg_batch_kernel<true>(per) : pcg_batch_kernel<false>(per);
+    return cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kSolveBlock), args, smem, s);
+}
 
 cudaError_t prepare_solve(const SbGrid& g, const SolverConfig& cfg) {
     if (g.nP > 8 * kSolveBlock) return cudaErrorInvalidValue;

@@ -52,15 +52,15 @@ __device__ __forceinline__ Pos pos_of(const Frame& F, const Trace& T, const SbGr
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock)
-k_advect_maps(SbGrid g, SbFields f, int cur) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                                          int idx) {
+    (void)ph;
+    (void)cur;
     if (idx == 0) {
         f.stats->distortion_bits = 0u;
         f.stats->reinit = 0;
         f.stats->broken_cells = 0;
     }
-    if (idx >= g.N) return;
     const int i = idx >> g.logP, j = idx & g.maskP;
     const float dt = f.step->dt;
     const Frame F = cell_frame(g, i, j);
@@ -115,10 +115,10 @@ __device__ __forceinline__ float advect_velocity(const SbGrid& g, const float* _
     return pu2.x * F.c0 - pu2.z * F.s0;             // e_theta = (c0, 0, -s0)
 }
 
-__global__ void __launch_bounds__(kBlock)
-k_velocity(SbGrid g, SbFields f) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= g.N) return;
+__device__ __forceinline__ void velocity_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                                          int idx) {
+    (void)ph;
+    (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
     const float dt = f.step->dt;
     {
@@ -137,10 +137,10 @@ k_velocity(SbGrid g, SbFields f) {
 
 // BIMOCQ thickness: compose the new backward map with the previous one and
 // blend the two reconstructions (MULTISAMPLE, 5 samples).
-__global__ void __launch_bounds__(kBlock)
-k_bimocq(SbGrid g, SbPhys ph, SbFields f, int cur) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= g.N) return;
+__device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                                          int idx) {
+    (void)ph;
+    (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
     if (f.eta[idx] == 0.0f) {
         f.eta_adv[idx] = 0.0f;
@@ -183,10 +183,10 @@ __device__ __forceinline__ bool is_broken(float gamma, float eta, float gmax) {
 // of its couplings moves into the neighbours' dmass, which keeps A
 // symmetric positive definite with the same solution as the reference's
 // identity row.
-__global__ void __launch_bounds__(kBlock)
-k_assemble(SbGrid g, SbPhys ph, SbFields f) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= g.N) return;
+__device__ __forceinline__ void assemble_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                                          int idx) {
+    (void)ph;
+    (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
     const int nP = g.nP, nT = g.nT;
     const float dt = f.step->dt, invDt = f.step->invDt;
@@ -308,10 +308,10 @@ __device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, floa
     return (ca ? gmax : xa) - (cb ? gmax : xb);
 }
 
-__global__ void __launch_bounds__(kBlock)
-k_post(SbGrid g, SbPhys ph, SbFields f) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= g.N) return;
+__device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                                          int idx) {
+    (void)ph;
+    (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
     const int nP = g.nP;
     const float dt = f.step->dt, invDt = f.step->invDt;
@@ -382,43 +382,84 @@ __device__ __forceinline__ float warp_max(float v) {
 
 // BIMOCQ change accumulation through the forward map, fused with the
 // forward/backward distortion estimate of the same maps.
-__global__ void __launch_bounds__(kBlock)
-k_accum(SbGrid g, SbFields f, int cur) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    float dist = 0.0f;
-    if (idx < g.N) {
-        const int i = idx >> g.logP, j = idx & g.maskP;
-        const Frame F = cell_frame(g, i, j);
-        const float2* fwd = f.fwd[cur ^ 1];
-        const float2* bwd = f.bwd[cur ^ 1];
-        float ed = f.eta_delta[idx], gd = f.gam_delta[idx];
-        f3 ds[5];
-        sample_map_multi5(g, fwd, F, ds);
+// returns the cell's distortion (0 outside the grid)
+__device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                                           int idx) {
+    (void)ph;
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const Frame F = cell_frame(g, i, j);
+    const float2* fwd = f.fwd[cur ^ 1];
+    const float2* bwd = f.bwd[cur ^ 1];
+    float ed = f.eta_delta[idx], gd = f.gam_delta[idx];
+    f3 ds[5];
+    sample_map_multi5(g, fwd, F, ds);
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
-            ed += kW5[k] * gather(f.d_eta, s);
-            gd += kW5[k] * gather(f.d_gam, s);
-        }
-        f.eta_delta[idx] = ed;
-        f.gam_delta[idx] = gd;
-        // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
-        float2 m = fwd[idx];
-        const float d1 = dist_from_disp(sample_map(g, bwd, F, frame_pos(F, m.x, m.y)), g.invh);
-        m = bwd[idx];
-        const float d2 = dist_from_disp(sample_map(g, fwd, F, frame_pos(F, m.x, m.y)), g.invh);
-        dist = fmaxf(fabsf(d1), fabsf(d2));
-        if (isnan(dist)) dist = 0.0f;
+    for (int k = 0; k < 5; ++k) {
+        const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
+        ed += kW5[k] * gather(f.d_eta, s);
+        gd += kW5[k] * gather(f.d_gam, s);
     }
-    __shared__ float smax[kBlock / 32];
+    f.eta_delta[idx] = ed;
+    f.gam_delta[idx] = gd;
+    // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
+    float2 m = fwd[idx];
+    const float d1 = dist_from_disp(sample_map(g, bwd, F, frame_pos(F, m.x, m.y)), g.invh);
+    m = bwd[idx];
+    const float d2 = dist_from_disp(sample_map(g, fwd, F, frame_pos(F, m.x, m.y)), g.invh);
+    const float dist = fmaxf(fabsf(d1), fabsf(d2));
+    return isnan(dist) ? 0.0f : dist;
+}
+
+// Block maximum of the distortion into the bubble's statistics (all
+// threads of the block belong to one bubble).
+__device__ __forceinline__ void block_max_distortion(float dist, SbDevStats* st) {
+    __shared__ float smax[32];
     dist = warp_max(dist);
     if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = dist;
     __syncthreads();
     if (threadIdx.x < 32) {
-        float v = threadIdx.x < kBlock / 32 ? smax[threadIdx.x] : 0.0f;
+        float v = threadIdx.x < (blockDim.x >> 5) ? smax[threadIdx.x] : 0.0f;
         v = warp_max(v);
-        if (threadIdx.x == 0) atomicMax(&f.stats->distortion_bits, __float_as_uint(v));
+        if (threadIdx.x == 0) atomicMax(&st->distortion_bits, __float_as_uint(v));
     }
+}
+
+// ---------------------------------------------------------------------------
+// Kernels: one bubble (parameters by value), or a batch of bubbles (one
+// descriptor per bubble, one 128..256-cell tile per block; a tile never
+// straddles two bubbles).
+#define SB_CELL_KERNELS(name)                                                          \
+    __global__ void __launch_bounds__(256) k_##name(SbGrid g, SbPhys ph, SbFields f, int cur) { \
+        const int idx = blockIdx.x * blockDim.x + threadIdx.x;                        \
+        if (idx < g.N) name##_cell(g, ph, f, cur, idx);                               \
+    }                                                                                  \
+    __global__ void __launch_bounds__(256) kb_##name(const SbBubbleDesc* __restrict__ descs, \
+                                                     const int2* __restrict__ tiles) {\
+        const int2 t = tiles[blockIdx.x];                                              \
+        const SbBubbleDesc& d = descs[t.x];                                            \
+        const int idx = t.y + threadIdx.x;                                             \
+        if (idx < d.g.N) name##_cell(d.g, d.ph, d.f, d.cur, idx);                     \
+    }
+
+SB_CELL_KERNELS(advect_maps)
+SB_CELL_KERNELS(velocity)
+SB_CELL_KERNELS(bimocq)
+SB_CELL_KERNELS(assemble)
+SB_CELL_KERNELS(post)
+
+__global__ void __launch_bounds__(256) k_accum(SbGrid g, SbPhys ph, SbFields f, int cur) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const float dist = idx < g.N ? accum_cell(g, ph, f, cur, idx) : 0.0f;
+    block_max_distortion(dist, f.stats);
+}
+
+__global__ void __launch_bounds__(256) kb_accum(const SbBubbleDesc* __restrict__ descs,
+                                                const int2* __restrict__ tiles) {
+    const int2 t = tiles[blockIdx.x];
+    const SbBubbleDesc& d = descs[t.x];
+    const int idx = t.y + threadIdx.x;
+    const float dist = idx < d.g.N ? accum_cell(d.g, d.ph, d.f, d.cur, idx) : 0.0f;
+    block_max_distortion(dist, d.f.stats);
 }
 
 __device__ __forceinline__ bool reinit_now(const SbDevStats* st) {
@@ -521,6 +562,57 @@ k_reinit(SbGrid g, SbFields f, int cur) {
     for (int idx = t0; idx < g.N; idx += stride) reinit_commit(f, cur, idx);
 }
 
+// Batched re-initialisation: the bubbles whose distortion exceeds the
+// threshold are corrected in three grid-synchronised phases over their
+// tiles.  Every block reads every bubble's decision, so all blocks agree on
+// whether any phase runs.
+__global__ void __launch_bounds__(kBlock)
+kb_reinit(const SbBubbleDesc* __restrict__ descs, int nb, const int2* __restrict__ tiles,
+          int ntiles) {
+    __shared__ int any;
+    if (threadIdx.x == 0) {
+        int a = 0;
+        for (int b = 0; b < nb; ++b) a |= reinit_now(descs[b].f.stats) ? 1 : 0;
+        any = a;
+    }
+    __syncthreads();
+    if (!any) return;
+    cg::grid_group grid = cg::this_grid();
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        const SbBubbleDesc& d = descs[tl.x];
+        if (!reinit_now(d.f.stats)) continue;
+        for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x) {
+            if (idx == 0) {
+                d.f.stats->reinit = 1;
+                d.f.stats->reinit_total += 1;
+            }
+            reinit_error(d.g, d.f, d.cur, idx);
+        }
+    }
+    grid.sync();
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        const SbBubbleDesc& d = descs[tl.x];
+        if (!reinit_now(d.f.stats)) continue;
+        for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
+            reinit_correct(d.g, d.f, d.cur, idx);
+    }
+    grid.sync();
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        const SbBubbleDesc& d = descs[tl.x];
+        if (!reinit_now(d.f.stats)) continue;
+        for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
+            reinit_commit(d.f, d.cur, idx);
+    }
+}
+
+__global__ void kb_flip(SbBubbleDesc* descs, int nb) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nb) descs[b].cur ^= 1;
+}
+
 __global__ void k_reset_maps(SbGrid g, SbFields f) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= g.N) return;
@@ -575,13 +667,13 @@ cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbF
                          const SolverConfig& cfg, int cur, cudaStream_t s) {
     const dim3 grid = grid_for(g);
     switch (stage) {
-        case STAGE_MAPS: k_advect_maps<<<grid, kBlock, 0, s>>>(g, f, cur); break;
-        case STAGE_VELOCITY: k_velocity<<<grid, kBlock, 0, s>>>(g, f); break;
+        case STAGE_MAPS: k_advect_maps<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
+        case STAGE_VELOCITY: k_velocity<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
         case STAGE_BIMOCQ: k_bimocq<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
-        case STAGE_ASSEMBLE: k_assemble<<<grid, kBlock, 0, s>>>(g, ph, f); break;
+        case STAGE_ASSEMBLE: k_assemble<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
         case STAGE_SOLVE: return launch_solve(g, ph, f, cfg, s);
-        case STAGE_POST: k_post<<<grid, kBlock, 0, s>>>(g, ph, f); break;
-        case STAGE_ACCUM: k_accum<<<grid, kBlock, 0, s>>>(g, f, cur); break;
+        case STAGE_POST: k_post<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
+        case STAGE_ACCUM: k_accum<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
         case STAGE_REINIT: {
             SbGrid gg = g;
             SbFields ff = f;
@@ -598,6 +690,50 @@ cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbF
 cudaError_t prepare_launches(const SbGrid& g, const SolverConfig& cfg) {
     reinit_blocks();
     return prepare_solve(g, cfg);
+}
+
+cudaError_t launch_stage_batch(int stage, const SbBubbleDesc* descs, const int2* tiles, int ntiles,
+                               int block, cudaStream_t s) {
+    switch (stage) {
+        case STAGE_MAPS: kb_advect_maps<<<ntiles, block, 0, s>>>(descs, tiles); break;
+        case STAGE_VELOCITY: kb_velocity<<<ntiles, block, 0, s>>>(descs, tiles); break;
+        case STAGE_BIMOCQ: kb_bimocq<<<ntiles, block, 0, s>>>(descs, tiles); break;
+        case STAGE_ASSEMBLE: kb_assemble<<<ntiles, block, 0, s>>>(descs, tiles); break;
+        case STAGE_POST: kb_post<<<ntiles, block, 0, s>>>(descs, tiles); break;
+        case STAGE_ACCUM: kb_accum<<<ntiles, block, 0, s>>>(descs, tiles); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+int reinit_batch_blocks() {
+    static int cache[16] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& b = cache[dev & 15];
+    if (b == 0) {
+        int sms = 0, per = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_reinit, kBlock, 0);
+        b = sms * (per > 0 ? per : 1);
+    }
+    return b;
+}
+
+cudaError_t launch_reinit_batch(const SbBubbleDesc* descs, int nb, const int2* tiles, int ntiles,
+                                cudaStream_t s) {
+    const SbBubbleDesc* dd = descs;
+    int nn = nb;
+    const int2* tt = tiles;
+    int nt = ntiles;
+    void* args[] = {&dd, &nn, &tt, &nt};
+    return cudaLaunchCooperativeKernel((const void*)kb_reinit, dim3(reinit_batch_blocks()),
+                                       dim3(kBlock), args, 0, s);
+}
+
+cudaError_t launch_flip_batch(SbBubbleDesc* descs, int nb, cudaStream_t s) {
+    kb_flip<<<(nb + 127) / 128, 128, 0, s>>>(descs, nb);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s) {

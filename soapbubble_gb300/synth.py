@@ -220,3 +220,33 @@ CONFIGS = {
 # Physical parameters shared by the configurations (config.txt keys, radius 1).
 PHYSICS = dict(radius=1.0, H=1e-6, U=1.0, c_m=0.5, Gamma_m=1e-6, T=298.15, Ds=0.0,
                rm=5e-9, blendCoeff=0.5)
+
+# The batched ensemble: 64 bubbles, nTheta uniform over ENSEMBLE_SIZES, the
+# thickness recipe, time step and solver of c0, 200 steps.
+ENSEMBLE = dict(members=64, steps=200, dt=0.005, recipe="c0", sizes=(64, 128, 256, 512),
+                spread=0.5)
+
+
+@dataclass
+class Member:
+    """One ensemble bubble: grid, field seed and the scale factors of its
+    gravity (gs_scale), air viscosity (nu_scale, through the drag
+    coefficient) and Marangoni coefficient (M_scale)."""
+    nTheta: int
+    seed: int
+    gs_scale: float
+    nu_scale: float
+    M_scale: float
+
+
+def ensemble(seed: int = 0, members: int = ENSEMBLE["members"], sizes=ENSEMBLE["sizes"],
+             spread: float = ENSEMBLE["spread"]) -> list:
+    """Seeded ensemble members: nTheta uniform over `sizes`, each physical
+    scale uniform in [1 - spread, 1 + spread], a field seed per member."""
+    rng = np.random.Generator(np.random.PCG64(sub_seed(seed, 0xE5)))
+    out = []
+    for k in range(members):
+        nT = int(sizes[int(rng.integers(len(sizes)))])
+        gs, nu, M = rng.uniform(1.0 - spread, 1.0 + spread, size=3)
+        out.append(Member(nT, sub_seed(seed, k), float(gs), float(nu), float(M)))
+    return out

@@ -1,0 +1,172 @@
+"""GPU checks of the batched ensemble (sb_batch_*): many bubbles of uneven
+grid size and coefficients stepped by one launch per stage.
+
+A member that gets as many solve blocks in the batch as its own solve
+launch uses (small batches) runs exactly the same arithmetic as sb_step on
+that member alone, so results are compared bit for bit.  In a large
+ensemble a member's implicit solve is spread over fewer blocks, which only
+changes the order of its FP64 dot-product sums; those runs are compared at
+1e-5 normwise relative error, the step's parity tolerance.
+"""
+import numpy as np
+import pytest
+
+import _parity as P
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("eta", "gamma", "u_theta", "u_phi", "eta_delta", "gamma_delta", "eta_init",
+          "gamma_init", "eta_delta_last", "fwd_t", "fwd_p", "bwd_t", "bwd_p", "bwdprev_t")
+
+
+def _member(nT, seed, recipe="c0", dt=0.005, scales=(1.0, 1.0, 1.0), **kw):
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    f = synth.make_fields(recipe, nT, seed)
+    gs, nu, M = scales
+    gb = GpuBubble(make_params(nT, dt, gs_scale=gs, nu_scale=nu, M_scale=M, **kw))
+    gb.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    return gb
+
+
+def _twins(specs, **kw):
+    """Two identical sets of bubbles: one for the batch, one stepped alone."""
+    a = [_member(*s, **kw) for s in specs]
+    b = [_member(*s, **kw) for s in specs]
+    return a, b
+
+
+def _schedule(nsteps, dt):
+    # the frame time changes every 5 steps, as in the frame loop
+    return [((k // 5) * 5 * dt, dt) for k in range(nsteps)]
+
+
+def _close(bubbles):
+    for g in bubbles:
+        g.close()
+
+
+SMALL = [(16, 11, "c0", 0.005, (1.4, 0.7, 1.2)),
+         (32, 12, "c0", 0.005, (0.6, 1.3, 0.8)),
+         (64, 13, "c1", 0.005, (1.0, 1.0, 1.0)),
+         (8, 14, "c0", 0.005, (1.2, 1.2, 0.5))]
+
+
+@pytest.mark.parametrize("solver_mode", [0, 1], ids=["mixed", "plain"])
+def test_batch_matches_members_stepped_alone(gpulib, solver_mode):
+    from soapbubble_gb300.bubble import GpuBatch
+    a, b = _twins(SMALL, solver_mode=solver_mode, solver_tol=1e-6)
+    try:
+        with GpuBatch(a) as batch:
+            for t, dt in _schedule(25, 0.005):
+                batch.step(1, t, dt)
+                for g in b:
+                    g.step(1, t, dt)
+            batch.synchronize()
+        for ga, gb in zip(a, b):
+            for name in FIELDS:
+                np.testing.assert_array_equal(ga.download(name), gb.download(name),
+                                              err_msg=f"nT={ga.nTheta} {name}")
+            sa, sb = ga.stats(), gb.stats()
+            assert sa.steps == sb.steps == 25
+            assert sa.reinits == sb.reinits
+            assert sa.solver_iters == sb.solver_iters
+            assert sa.solver_rel_resid == sb.solver_rel_resid
+            assert sa.solver_converged == sb.solver_converged == 1
+            assert sa.distortion == sb.distortion
+    finally:
+        _close(a + b)
+
+
+def test_batch_reinit_decided_per_member(gpulib):
+    """One member re-initialises every step (forced), the others never or by
+    their own distortion: each follows its own decision inside the shared
+    cooperative launch."""
+    from soapbubble_gb300.bubble import GpuBatch
+    specs = [(16, 21), (32, 22), (32, 23)]
+    forces = [2, 1, 0]
+    a = [_member(*s, force_reinit=f) for s, f in zip(specs, forces)]
+    b = [_member(*s, force_reinit=f) for s, f in zip(specs, forces)]
+    try:
+        with GpuBatch(a) as batch:
+            for t, dt in _schedule(12, 0.005):
+                batch.step(1, t, dt)
+                for g in b:
+                    g.step(1, t, dt)
+            batch.synchronize()
+        reinits = [g.stats().reinits for g in a]
+        assert reinits[0] == 12 and reinits[1] == 0
+        for ga, gb in zip(a, b):
+            assert ga.stats().reinits == gb.stats().reinits
+            for name in FIELDS:
+                np.testing.assert_array_equal(ga.download(name), gb.download(name), err_msg=name)
+    finally:
+        _close(a + b)
+
+
+def test_batch_timed_autotuned_and_graph_paths_agree(gpulib):
+    """The stage-by-stage path, the autotuner's tuning steps (every tile
+    size) and the captured graph with the tuned tiles give the results of
+    stepping the members alone."""
+    from soapbubble_gb300.bubble import GpuBatch, stage_names
+    a, b = _twins(SMALL[:3])
+    try:
+        with GpuBatch(a) as batch:
+            ms = np.zeros(16)
+            batch.step_timed(2, 0.0, 0.005, ms)
+            tiles = batch.autotune(0.0, 0.005)
+            batch.step(3, 0.025, 0.005)
+            batch.synchronize()
+            assert ms[:len(stage_names())].sum() > 0
+            assert all(t in (64, 128, 256) for t in tiles[:len(stage_names())])
+        for g in b:
+            g.step(5, 0.0, 0.005)
+            g.step(3, 0.025, 0.005)
+        for ga, gb in zip(a, b):
+            assert ga.stats().steps == gb.stats().steps == 8
+            for name in FIELDS:
+                np.testing.assert_array_equal(ga.download(name), gb.download(name), err_msg=name)
+    finally:
+        _close(a + b)
+
+
+def test_ensemble_matches_members_stepped_alone(gpulib):
+    """The 64-bubble ensemble (nTheta 64..512, seeded coefficients): a few
+    batched steps against each member stepped alone."""
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBatch
+    dt = synth.ENSEMBLE["dt"]
+    members = synth.ensemble(seed=4)
+    specs = [(m.nTheta, m.seed, "c0", dt, (m.gs_scale, m.nu_scale, m.M_scale)) for m in members]
+    a, b = _twins(specs)
+    try:
+        with GpuBatch(a) as batch:
+            for t, d in _schedule(6, dt):
+                batch.step(1, t, d)
+                for g in b:
+                    g.step(1, t, d)
+            batch.synchronize()
+        worst = 0.0
+        for ga, gb in zip(a, b):
+            sa = ga.stats()
+            assert sa.solver_converged == 1 and sa.solver_rel_resid <= 1e-6
+            assert sa.steps == 6
+            for name in ("eta", "gamma", "u_theta", "u_phi"):
+                e = P.rel_err(ga.download(name), gb.download(name))
+                worst = max(worst, e)
+                assert e <= 1e-5, (ga.nTheta, name, e)
+        print(f"worst normwise relative difference batch vs alone: {worst:.2e}")
+    finally:
+        _close(a + b)
+
+
+def test_batch_rejects_mixed_solver_settings(gpulib):
+    from soapbubble_gb300._lib import SoapBubbleError
+    from soapbubble_gb300.bubble import GpuBatch
+    a = _member(16, 1, solver_mode=0)
+    b = _member(16, 2, solver_mode=1)
+    try:
+        with pytest.raises(SoapBubbleError, match="solver"):
+            GpuBatch([a, b])
+    finally:
+        _close([a, b])

@@ -24,18 +24,25 @@ TOL_MAP_CELLS = 1e-4
 PHYS = ("eta", "gamma", "u_theta", "u_phi")
 
 
-def new_pair(oracle, nT, recipe, dt, pre, t, seed, force=0, solver_mode=0, tol=1e-10):
+def new_pair(oracle, nT, recipe, dt, pre, t, seed, force=0, solver_mode=0, tol=1e-10,
+             gs_scale=1.0, nu_scale=1.0, M_scale=1.0):
     from soapbubble_gb300 import synth
     from soapbubble_gb300.bubble import GpuBubble, make_params
     f = synth.make_fields(recipe, nT, seed)
     op = oracle.default_params(nT, dt_s=dt)
     op.t = t
     op.force_reinit = {0: -1, 1: 0, 2: 1}[force]
+    # the scale options: gravity and Marangoni linearly, the drag coefficient
+    # as the square root of the air viscosity
+    op.gs *= gs_scale
+    op.M *= M_scale
+    op.Cr *= np.sqrt(nu_scale)
     ob = oracle.OracleBubble(op, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
     for _ in range(pre):
         ob.step()
     gb = GpuBubble(make_params(nT, dt, solver_tol=tol, solver_max_iter=2000,
-                               force_reinit=force, solver_mode=solver_mode))
+                               force_reinit=force, solver_mode=solver_mode, gs_scale=gs_scale,
+                               nu_scale=nu_scale, M_scale=M_scale))
     P.sync_state(gb, ob)
     return gb, ob
 
@@ -99,6 +106,21 @@ def test_step_matches_oracle(oracle, gpulib, case):
         assert gs.reinit == st.reinit
         assert gs.distortion == pytest.approx(st.distortion, rel=1e-3, abs=1e-6)
         check_errors(P.compare(gb, ob))
+
+
+@pytest.mark.parametrize("scales", [(1.5, 0.5, 1.3), (0.5, 1.5, 0.6)])
+def test_scaled_coefficients_match_oracle(oracle, gpulib, scales):
+    """Per-bubble gravity, air viscosity and Marangoni scales (the batched
+    ensemble's per-member coefficients) reach the step as in the oracle."""
+    gs, nu, M = scales
+    gb, ob = new_pair(oracle, 64, "c0", 0.005, 5, 1.0, 555, gs_scale=gs, nu_scale=nu, M_scale=M)
+    with gb:
+        ob.step()
+        gb.step(1, 1.0, 0.005)
+        assert gb.stats().solver_converged == 1
+        err = P.compare(gb, ob, PHYS)
+        for k in PHYS:
+            assert err[k] <= TOL_FIELD, (k, err[k])
 
 
 def test_plain_fp32_solver_matches_oracle(oracle, gpulib):
