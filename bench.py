@@ -281,7 +281,7 @@ def run_ours(args):
     dom = names[k_dom]
     mean_iters = float(np.mean(iters)) if iters else 0.0
     alg = dict(ALG_BYTES_PER_CELL)
-    alg["k_pcg"] = PCG_BYTES_FIXED + PCG_BYTES_PER_ITER * mean_iters
+    alg["k_solve"] = PCG_BYTES_FIXED + PCG_BYTES_PER_ITER * mean_iters
     per_launch_bytes = alg[dom] * N
     avg_launch_s = stage_ms[k_dom] / 1e3 / kr
     achieved = per_launch_bytes / avg_launch_s / 1e9

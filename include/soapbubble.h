@@ -140,7 +140,15 @@ int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt);
  * times its phases with cudaEvent timers (kernel/solver.cu:261-279). */
 int sb_step_timed(sb_bubble* b, int n_steps, double t_frame, double dt, double* stage_ms);
 
-/* Number of kernel stages of one step, and the kernel name of a stage. */
+/* Picks, per stage, the tile size (64, 128 or 256 cells per block) with the
+ * shortest device time, from one timed step at each size; tile_sizes
+ * (optional, sb_stage_count() ints) receives the choice.  The three tuning
+ * steps advance the bubble like sb_step_timed.  Results do not depend on
+ * the tile sizes.  No counterpart in the reference. */
+int sb_autotune(sb_bubble* b, double t_frame, double dt, int* tile_sizes);
+
+/* Number of kernel stages of one step, and the kernel name of a stage.  A
+ * step launches one kernel per stage plus one that flips the map parity. */
 int sb_stage_count(void);
 const char* sb_stage_name(int stage);
 

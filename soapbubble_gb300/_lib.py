@@ -75,6 +75,7 @@ def lib() -> C.CDLL:
     L.sb_field_size.restype = C.c_size_t
     L.sb_step.argtypes = [H, C.c_int, C.c_double, C.c_double]
     L.sb_step_timed.argtypes = [H, C.c_int, C.c_double, C.c_double, dp]
+    L.sb_autotune.argtypes = [H, C.c_double, C.c_double, C.POINTER(C.c_int)]
     L.sb_stage_count.argtypes = []
     L.sb_stage_count.restype = C.c_int
     L.sb_stage_name.argtypes = [C.c_int]
@@ -108,7 +109,7 @@ def lib() -> C.CDLL:
     L.sb_batch_stream.argtypes = [H]
     L.sb_batch_stream.restype = C.c_void_p
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
-                 "sb_download_field", "sb_step", "sb_step_timed", "sb_upload_field_f32",
+                 "sb_download_field", "sb_step", "sb_step_timed", "sb_autotune", "sb_upload_field_f32",
                  "sb_download_field_f32", "sb_synchronize", "sb_get_stats",
                  "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
@@ -126,7 +127,7 @@ def check(code: int, what: str) -> None:
 # Every symbol include/soapbubble.h declares (checked by the CPU tests).
 EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_upload_field", "sb_download_field", "sb_field_size", "sb_step",
-           "sb_step_timed", "sb_stage_count", "sb_stage_name", "sb_upload_field_f32",
+           "sb_step_timed", "sb_autotune", "sb_stage_count", "sb_stage_name", "sb_upload_field_f32",
            "sb_download_field_f32", "sb_synchronize", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
            "sb_run", "sb_write_exr_gray", "sb_mass_integrals_noalloc", "sb_bytes_required",
            "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",

@@ -115,6 +115,13 @@ class GpuBubble:
         assert stage_ms.dtype == np.float64 and stage_ms.size >= lib().sb_stage_count()
         check(lib().sb_step_timed(self.h, n, t, dt, _dp(stage_ms)), "sb_step_timed")
 
+    def autotune(self, t: float, dt: float) -> list:
+        """sb_autotune: picks each stage's tile size (three tuning steps
+        advance the bubble); returns the chosen cells per block by stage."""
+        out = (C.c_int * lib().sb_stage_count())()
+        check(lib().sb_autotune(self.h, t, dt, out), "sb_autotune")
+        return list(out)
+
     def upload_f32(self, name: str, a: np.ndarray) -> None:
         """Asynchronous FP32 upload from a host buffer the caller keeps alive."""
         assert a.dtype == np.float32 and a.flags.c_contiguous

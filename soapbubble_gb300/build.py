@@ -24,6 +24,11 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 LIB_SOURCES = ["sb_step.cu", "sb_solver.cu", "sb_api.cu", "sb_exr.cpp", "sb_noalloc.cu"]
+# The implicit solve is compiled without multiply-add contraction: the solver
+# kernel is instantiated per row width of the largest system it serves, and
+# contraction choices may differ between instantiations, while a bubble must
+# get bit-identical results alone and inside any batch.
+EXTRA_FLAGS = {"sb_solver.cu": ["-fmad=false"]}
 CLI_SOURCES = ["sb_bubble.cpp", "sb_main.cpp"]
 
 
@@ -36,7 +41,8 @@ def nvcc() -> str:
 
 def _compile(src: str, extra=()) -> str:
     obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *EXTRA_FLAGS.get(src, []), *extra, "-c",
+           os.path.join(CSRC, src), "-o", obj]
     out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{out.stdout}\n{out.stderr}")
@@ -83,8 +89,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 def ptxas_report(src: str = "sb_step.cu") -> str:
     """Register / spill report of one translation unit (-Xptxas -v)."""
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-Xptxas", "-v", "-c", os.path.join(CSRC, src),
-           "-o", os.devnull]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *EXTRA_FLAGS.get(src, []), "-Xptxas", "-v", "-c",
+           os.path.join(CSRC, src), "-o", os.devnull]
     out = subprocess.run(cmd, capture_output=True, text=True)
     return out.stdout + out.stderr
 

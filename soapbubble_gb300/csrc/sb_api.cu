@@ -80,7 +80,9 @@ struct sb_bubble {
     SbStepParams* h_step = nullptr;  // pinned
     long long launches = 0;          // kernels launched by this handle
     cudaEvent_t ev[STAGE_COUNT + 1] = {};
-    cudaGraphExec_t graph[2] = {};   // one captured step per map parity
+    SbStepPlan plan{};                 // this bubble as a set of one
+    SbBubbleDesc desc{};               // host copy of the bubble's descriptor
+    cudaGraphExec_t graph = nullptr;   // one captured step
 };
 
 namespace {
@@ -140,10 +142,12 @@ struct ArenaPlan {
     size_t fwd[2], bwd[2], bwdprev;
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
     size_t div, d_eta, d_gam, err_eta, err_gam;
-    size_t dmass, cE, cS, rhs, r0, x, dx, r, z, p, q, x64, pcr, pcr_levels, partials, step, stats;
+    size_t dmass, cE, cS, rhs, r0, x, dx, r, z, p, q, xff, pcr, pcr_levels, step, stats;
+    size_t self, self_list, roff, done_at, cnt, rec, rowpart;  // the bubble's solve set
+    size_t tiles[3];                                           // its cell tiles
 };
 
-ArenaPlan plan_arena(const SbGrid& g, int partials) {
+ArenaPlan plan_arena(const SbGrid& g) {
     ArenaPlan a;
     const size_t N = (size_t)g.N, Nv = (size_t)g.Nv, F = sizeof(float);
     a.tables = a.L.take((size_t)(4 * g.nT + 2) * F);
@@ -163,12 +167,20 @@ ArenaPlan plan_arena(const SbGrid& g, int partials) {
     a.rhs = a.L.take(N * F); a.r0 = a.L.take(N * F); a.x = a.L.take(N * F); a.dx = a.L.take(N * F);
     a.r = a.L.take(N * F);
     a.z = a.L.take(N * F); a.p = a.L.take(N * F); a.q = a.L.take(N * F);
-    a.x64 = a.L.take(N * 8);
+    a.xff = a.L.take(N * 8);
     int lg = 0;
     while ((1 << lg) < g.nP) ++lg;
     a.pcr = a.L.take((size_t)lg * N * 8);  // <= log2(nP) - 1 levels + final factors
     a.pcr_levels = a.L.take((size_t)g.nT * 4);
-    a.partials = a.L.take((size_t)partials * 8);
+    a.self = a.L.take(sizeof(SbBubbleDesc));
+    a.self_list = a.L.take(sizeof(SbBubbleDesc*));
+    for (int k = 0; k < 3; ++k)
+        a.tiles[k] = a.L.take(sizeof(int2) * (size_t)((g.N + kTileSizes[k] - 1) / kTileSizes[k]));
+    a.roff = a.L.take(8);
+    a.done_at = a.L.take(4);
+    a.cnt = a.L.take(4);
+    a.rec = a.L.take(2 * sizeof(SbSolveRec));
+    a.rowpart = a.L.take((size_t)g.nT * 2 * 3 * sizeof(float2));
     a.step = a.L.take(sizeof(SbStepParams));
     a.stats = a.L.take(sizeof(SbDevStats) + 64);
     return a;
@@ -302,9 +314,7 @@ size_t sb_bytes_required(const sb_params* p) {
     g.nP = 2 * p->nTheta;
     g.N = g.nT * g.nP;
     g.Nv = (g.nT - 1) * g.nP;
-    // partial slots: 6 per block of the cooperative solve (blocks <= rows)
-    const int partials = 6 * g.nT;
-    return plan_arena(g, partials).L.bytes;
+    return plan_arena(g).L.bytes;
 }
 
 int sb_create(const sb_params* p, sb_bubble** out) {
@@ -333,8 +343,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     b->solver.precond = 1;
     b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
 
-    const int partials = 6 * g.nT;
-    ArenaPlan a = plan_arena(g, partials);
+    ArenaPlan a = plan_arena(g);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->arena, a.L.bytes);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_step, sizeof(SbStepParams));
@@ -369,16 +378,19 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.err_eta = F32(a.err_eta); f.err_gam = F32(a.err_gam);
     f.dmass = F32(a.dmass); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs); f.r0 = F32(a.r0);
     f.x = F32(a.x); f.dx = F32(a.dx); f.r = F32(a.r); f.z = F32(a.z); f.p = F32(a.p); f.q = F32(a.q);
-    f.x64 = (double*)(A + a.x64);
+    f.xff = (float2*)(A + a.xff);
     f.pcr = (float2*)(A + a.pcr);
     f.pcr_levels = (int*)(A + a.pcr_levels);
-    f.partials = (double*)(A + a.partials);
     f.step = (SbStepParams*)(A + a.step);
     f.stats = (SbDevStats*)(A + a.stats);
-    if (6 * 0 + solver_partials_needed(g) > partials) {
-        sb_destroy(b);
-        return fail(SB_ERR_INVALID, "solver partial buffer too small");
-    }
+    // the solve set of this bubble alone (rows 0 .. nT-1; the memset above
+    // leaves the row counter at zero)
+    f.self = (SbBubbleDesc*)(A + a.self);
+    f.roff = (int*)(A + a.roff);
+    f.done_at = (int*)(A + a.done_at);
+    f.cnt = (int*)(A + a.cnt);
+    f.rec = (SbSolveRec*)(A + a.rec);
+    f.rowpart = (float2*)(A + a.rowpart);
 
     // trigonometric tables in FP64, stored FP32
     std::vector<float> tab(4 * g.nT + 2);
@@ -433,8 +445,47 @@ int sb_create(const sb_params* p, sb_bubble** out) {
         if (e != cudaSuccess) rc = cuda_fail(e, "stats");
     }
     if (rc == SB_OK) {
-        e = prepare_launches(g, b->solver);
-        if (e != cudaSuccess) rc = cuda_fail(e, "prepare_launches");
+        // the bubble's own descriptor, and the launch plan of the bubble
+        // as a set of one
+        SbBubbleDesc d{};
+        d.g = g;
+        d.ph = b->ph;
+        d.f = f;
+        d.cur = 0;
+        const int roff[2] = {0, g.nT};
+        SbBubbleDesc** self_list = (SbBubbleDesc**)(A + a.self_list);
+        e = cudaMemcpy(f.self, &d, sizeof(d), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(f.roff, roff, sizeof(roff), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(self_list, &f.self, sizeof(f.self), cudaMemcpyHostToDevice);
+        SbStepPlan& P = b->plan;
+        P.descs = self_list;
+        P.nb = 1;
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+            std::vector<int2> tl;
+            for (int c = 0; c < g.N; c += kTileSizes[k]) tl.push_back(make_int2(0, c));
+            P.tiles[k] = (const int2*)(A + a.tiles[k]);
+            P.ntiles[k] = (int)tl.size();
+            e = cudaMemcpy((void*)P.tiles[k], tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice);
+        }
+        for (int st = 0; st < STAGE_COUNT; ++st) P.sel[st] = 1;
+        SbSolveSet& S = P.set;
+        S.descs = self_list;
+        S.nb = 1;
+        S.R = g.nT;
+        S.roff = f.roff;
+        S.rec = f.rec;
+        S.done_at = f.done_at;
+        S.cnt = f.cnt;
+        S.rowpart = f.rowpart;
+        P.maxNP = g.nP;
+        P.solver = b->solver;
+        b->desc = d;
+        P.one = &b->desc;
+        if (e != cudaSuccess) rc = cuda_fail(e, "step plan");
+    }
+    if (rc == SB_OK) {
+        e = prepare_plan(b->plan);
+        if (e != cudaSuccess) rc = cuda_fail(e, "prepare_plan");
     }
     if (rc == SB_OK) rc = set_step_params(b, 0.0, p->dt);
     if (rc == SB_OK) {
@@ -455,8 +506,7 @@ int sb_destroy(sb_bubble* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (cudaEvent_t e : b->ev)
         if (e) cudaEventDestroy(e);
-    for (cudaGraphExec_t gx : b->graph)
-        if (gx) cudaGraphExecDestroy(gx);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->arena) cudaFree(b->arena);
     if (b->h_step) cudaFreeHost(b->h_step);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -561,21 +611,76 @@ int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma, const
     return rc;
 }
 
-// One step of map parity `cur` captured as a CUDA graph (the per-step
-// scalars live in device memory, so the graph is replayed unchanged).
-static int capture_step(sb_bubble* b, int cur) {
+}  // extern "C"
+
+namespace {
+
+// One step of a plan captured as a CUDA graph.  The per-step scalars and
+// every bubble's map parity live in device memory, so the graph is replayed
+// unchanged step after step.
+int capture_plan(const SbStepPlan& P, cudaStream_t s, cudaGraphExec_t* out) {
     cudaGraph_t graph = nullptr;
-    SB_CHECK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaSuccess;
-    for (int st = 0; st < STAGE_COUNT && e == cudaSuccess; ++st)
-        e = launch_stage(st, b->g, b->ph, b->f, b->solver, cur, b->stream);
-    cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+    SB_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = launch_plan_step(P, s);
+    cudaError_t e2 = cudaStreamEndCapture(s, &graph);
     if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[cur], graph, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, graph, 0);
     if (graph) cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(e, "step graph capture");
     return SB_OK;
 }
+
+// One step launched stage by stage with events between the stages; adds
+// every stage's device time (ms) to stage_ms.  Synchronises.
+int timed_plan_step(const SbStepPlan& P, cudaStream_t s, cudaEvent_t* ev, double* stage_ms) {
+    if (!ev[0])
+        for (int k = 0; k <= STAGE_COUNT; ++k) SB_CHECK(cudaEventCreate(&ev[k]));
+    SB_CHECK(cudaEventRecord(ev[0], s));
+    for (int st = 0; st < STAGE_COUNT; ++st) {
+        SB_CHECK(launch_plan_stage(P, st, s));
+        SB_CHECK(cudaEventRecord(ev[st + 1], s));
+    }
+    SB_CHECK(launch_plan_flip(P, s));
+    SB_CHECK(cudaEventSynchronize(ev[STAGE_COUNT]));
+    for (int st = 0; st < STAGE_COUNT; ++st) {
+        float ms = 0.f;
+        SB_CHECK(cudaEventElapsedTime(&ms, ev[st], ev[st + 1]));
+        stage_ms[st] += ms;
+    }
+    return SB_OK;
+}
+
+// Tile-size autotuner: one timed step with every tile size, then the
+// fastest size of each stage.  The kernels compute the same values at every
+// tile size.  `step` runs one timed step (and keeps the handle's
+// bookkeeping).
+template <typename StepFn>
+int autotune_plan(SbStepPlan& P, StepFn step, int* tile_sizes) {
+    double ms[3][STAGE_COUNT + 1] = {};
+    for (int k = 0; k < 3; ++k) {
+        for (int st = 0; st < STAGE_COUNT; ++st) P.sel[st] = k;
+        int rc = step(ms[k]);
+        if (rc != SB_OK) return rc;
+    }
+    for (int st = 0; st < STAGE_COUNT; ++st) {
+        int best = 1;
+        for (int k = 0; k < 3; ++k)
+            if (ms[k][st] < ms[best][st]) best = k;
+        P.sel[st] = best;
+        if (tile_sizes) tile_sizes[st] = kTileSizes[best];
+    }
+    return SB_OK;
+}
+
+void bubble_advance(sb_bubble* b, int n) {
+    b->launches += (long long)n * (STAGE_COUNT + 1);
+    b->steps += n;
+    b->cur ^= (n & 1);
+}
+
+}  // namespace
+
+extern "C" {
 
 int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
@@ -583,16 +688,10 @@ int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt) {
     SB_CHECK(cudaSetDevice(b->device));
     int rc = set_step_params(b, t_frame, dt);
     if (rc != SB_OK) return rc;
-    for (int s = 0; s < n_steps; ++s) {
-        if (!b->graph[b->cur]) {
-            rc = capture_step(b, b->cur);
-            if (rc != SB_OK) return rc;
-        }
-        SB_CHECK(cudaGraphLaunch(b->graph[b->cur], b->stream));
-        b->launches += STAGE_COUNT;
-        b->cur ^= 1;
-        b->steps++;
-    }
+    if (n_steps > 0 && !b->graph && (rc = capture_plan(b->plan, b->stream, &b->graph)) != SB_OK)
+        return rc;
+    for (int s = 0; s < n_steps; ++s) SB_CHECK(cudaGraphLaunch(b->graph, b->stream));
+    bubble_advance(b, n_steps);
     return SB_OK;
 }
 
@@ -602,33 +701,36 @@ int sb_step_timed(sb_bubble* b, int n_steps, double t_frame, double dt, double* 
     SB_CHECK(cudaSetDevice(b->device));
     int rc = set_step_params(b, t_frame, dt);
     if (rc != SB_OK) return rc;
-    if (!b->ev[0]) {
-        for (cudaEvent_t& e : b->ev) SB_CHECK(cudaEventCreate(&e));
-    }
     for (int s = 0; s < n_steps; ++s) {
-        SB_CHECK(cudaEventRecord(b->ev[0], b->stream));
-        for (int st = 0; st < STAGE_COUNT; ++st) {
-            SB_CHECK(launch_stage(st, b->g, b->ph, b->f, b->solver, b->cur, b->stream));
-            SB_CHECK(cudaEventRecord(b->ev[st + 1], b->stream));
-        }
-        b->launches += STAGE_COUNT;
-        b->cur ^= 1;
-        b->steps++;
-        SB_CHECK(cudaEventSynchronize(b->ev[STAGE_COUNT]));
-        for (int st = 0; st < STAGE_COUNT; ++st) {
-            float ms = 0.f;
-            SB_CHECK(cudaEventElapsedTime(&ms, b->ev[st], b->ev[st + 1]));
-            stage_ms[st] += ms;
-        }
+        if ((rc = timed_plan_step(b->plan, b->stream, b->ev, stage_ms)) != SB_OK) return rc;
+        bubble_advance(b, 1);
     }
     return SB_OK;
+}
+
+int sb_autotune(sb_bubble* b, double t_frame, double dt, int* tile_sizes) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    if (!(dt > 0)) return fail(SB_ERR_INVALID, "bad dt");
+    SB_CHECK(cudaSetDevice(b->device));
+    int rc = set_step_params(b, t_frame, dt);
+    if (rc != SB_OK) return rc;
+    rc = autotune_plan(b->plan, [&](double* ms) {
+        int r = timed_plan_step(b->plan, b->stream, b->ev, ms);
+        if (r == SB_OK) bubble_advance(b, 1);
+        return r;
+    }, tile_sizes);
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return rc;
 }
 
 int sb_stage_count(void) { return STAGE_COUNT; }
 
 const char* sb_stage_name(int stage) {
     static const char* names[STAGE_COUNT] = {"k_advect_maps", "k_velocity", "k_bimocq",
-                                             "k_assemble", "k_pcg", "k_post", "k_accum",
+                                             "k_assemble", "k_solve", "k_post", "k_accum",
                                              "k_reinit"};
     return (stage >= 0 && stage < STAGE_COUNT) ? names[stage] : "";
 }
@@ -680,6 +782,8 @@ int sb_get_stats(sb_bubble* b, sb_stats* out) {
     out->launches = b->launches;
     out->mass_eta = st.mass_eta;
     out->mass_gamma = st.mass_gamma;
+    if (st.wait_faults)
+        return fail(SB_ERR_CUDA, "a bounded wait for a shared-memory copy in the implicit solve gave up");
     return SB_OK;
 }
 
@@ -779,57 +883,14 @@ struct sb_batch {
     int device = 0;
     cudaStream_t stream = nullptr;
     char* arena = nullptr;
-    SbBubbleDesc* d_descs = nullptr;
-    int2* d_tiles[3] = {};
-    int ntiles[3] = {};
-    int* d_blk_bubble = nullptr;
-    int* d_first = nullptr;
-    int* d_nblk = nullptr;
-    double* d_partials = nullptr;
-    int* d_nactive = nullptr;
-    int G = 0;
-    int maxNP = 0;
-    SolverConfig solver;
-    int sel[STAGE_COUNT] = {1, 1, 1, 1, 1, 1, 1, 1};  // tile size index per stage
+    SbStepPlan plan{};  // the members as one set: their own descriptors, tiles, solve set
     cudaGraphExec_t graph = nullptr;
-    cudaEvent_t ev[STAGE_COUNT + 2] = {};
+    cudaEvent_t ev[STAGE_COUNT + 1] = {};
     long long steps = 0;
-    long long launches = 0;
     double last_t = -1e300, last_dt = -1;
 };
 
 namespace {
-
-const int kTileSizes[3] = {64, 128, 256};
-
-// Launches stage `st` of the batch (the solve and re-initialisation are
-// cooperative launches over the whole batch).
-cudaError_t batch_stage(sb_batch* B, int st) {
-    if (st == STAGE_SOLVE) {
-        SbBatchSolve bs;
-        bs.descs = B->d_descs;
-        bs.nb = (int)B->m.size();
-        bs.blk_bubble = B->d_blk_bubble;
-        bs.bub_first_blk = B->d_first;
-        bs.bub_nblk = B->d_nblk;
-        bs.partials = B->d_partials;
-        bs.nactive = B->d_nactive;
-        return launch_solve_batch(bs, B->G, B->maxNP, B->solver, B->stream);
-    }
-    if (st == STAGE_REINIT)
-        return launch_reinit_batch(B->d_descs, (int)B->m.size(), B->d_tiles[1], B->ntiles[1],
-                                   B->stream);
-    const int k = B->sel[st];
-    return launch_stage_batch(st, B->d_descs, B->d_tiles[k], B->ntiles[k], kTileSizes[k], B->stream);
-}
-
-cudaError_t batch_step_launches(sb_batch* B) {
-    for (int st = 0; st < STAGE_COUNT; ++st) {
-        cudaError_t e = batch_stage(B, st);
-        if (e != cudaSuccess) return e;
-    }
-    return launch_flip_batch(B->d_descs, (int)B->m.size(), B->stream);
-}
 
 int batch_set_params(sb_batch* B, double t, double dt) {
     if (t == B->last_t && dt == B->last_dt) return SB_OK;
@@ -845,11 +906,8 @@ int batch_set_params(sb_batch* B, double t, double dt) {
 
 void batch_advance(sb_batch* B, int n) {
     B->steps += n;
-    B->launches += (long long)n * (STAGE_COUNT + 1);
     for (sb_bubble* b : B->m) {
-        b->steps += n;
-        b->launches += (long long)n * (STAGE_COUNT + 1);
-        b->cur ^= (n & 1);
+        bubble_advance(b, n);
         b->last_t = -1e300;  // the bubble's own stream did not see the batch's copies
     }
 }
@@ -863,7 +921,8 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     *out = nullptr;
     sb_batch* B = new sb_batch();
     B->device = bubbles[0]->device;
-    B->solver = bubbles[0]->solver;
+    SbStepPlan& P = B->plan;
+    P.solver = bubbles[0]->solver;
     for (int k = 0; k < n; ++k) {
         sb_bubble* b = bubbles[k];
         if (!b || b->device != B->device) {
@@ -871,97 +930,85 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
             return fail(SB_ERR_INVALID, "batch members must be valid bubbles on one device");
         }
         const SolverConfig& c = b->solver;
-        if (c.mode != B->solver.mode || c.max_iter != B->solver.max_iter ||
-            c.tol != B->solver.tol || c.precond != B->solver.precond) {
+        if (c.mode != P.solver.mode || c.max_iter != P.solver.max_iter ||
+            c.tol != P.solver.tol || c.precond != P.solver.precond) {
             delete B;
             return fail(SB_ERR_INVALID, "batch members must share one solver configuration");
         }
         B->m.push_back(b);
-        if (b->g.nP > B->maxNP) B->maxNP = b->g.nP;
+        if (b->g.nP > P.maxNP) P.maxNP = b->g.nP;
+    }
+    // the row list of the solve: every member's theta rows, member by member
+    std::vector<int> roff(n + 1, 0);
+    unsigned long long weight = 0;
+    for (int k = 0; k < n; ++k) {
+        const int nT = B->m[k]->g.nT;
+        roff[k + 1] = roff[k] + nT;
+        weight += (unsigned long long)nT * (2ull * nT + 256ull);
+    }
+    const int R = roff[n];
+    if (n > 1024 || weight >= (1ull << 32)) {
+        delete B;
+        return fail(SB_ERR_INVALID, "a batch holds at most 1024 members of bounded total size");
     }
     cudaError_t e = cudaSetDevice(B->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
-    int Gmax = 0;
-    if (e == cudaSuccess) e = prepare_solve_batch(B->maxNP, B->solver, &Gmax);
-    if (e == cudaSuccess) reinit_batch_blocks();
+    if (e == cudaSuccess) e = prepare_plan(P);
     if (e != cudaSuccess) {
         int r = cuda_fail(e, "sb_batch_create");
         sb_batch_destroy(B);
         return r;
     }
-    // solve blocks per bubble, proportional to rows, at least one each
-    long long rows = 0;
-    for (sb_bubble* b : B->m) rows += b->g.nT;
-    if (Gmax < n) {
-        sb_batch_destroy(B);
-        return fail(SB_ERR_INVALID, "too many bubbles for one batch solve");
-    }
-    std::vector<int> nblk(n), first(n);
-    int G = 0;
-    for (int k = 0; k < n; ++k) {
-        long long want = (long long)Gmax * B->m[k]->g.nT / rows;
-        nblk[k] = (int)std::max<long long>(1, std::min<long long>(want, B->m[k]->g.nT));
-        G += nblk[k];
-    }
-    while (G > Gmax) {
-        int big = 0;
-        for (int k = 1; k < n; ++k)
-            if (nblk[k] > nblk[big]) big = k;
-        --nblk[big];
-        --G;
-    }
-    std::vector<int> blk_bubble(G);
-    for (int k = 0, at = 0; k < n; ++k) {
-        first[k] = at;
-        for (int q = 0; q < nblk[k]; ++q) blk_bubble[at++] = k;
-    }
-    B->G = G;
     // tiles for the three tile sizes
     std::vector<int2> tiles[3];
-    for (int s = 0; s < 3; ++s) {
+    for (int s = 0; s < 3; ++s)
         for (int k = 0; k < n; ++k)
             for (int c = 0; c < B->m[k]->g.N; c += kTileSizes[s]) tiles[s].push_back(make_int2(k, c));
-        B->ntiles[s] = (int)tiles[s].size();
-    }
     Layout L;
-    const size_t o_desc = L.take(sizeof(SbBubbleDesc) * n);
+    const size_t o_desc = L.take(sizeof(SbBubbleDesc*) * n);
     size_t o_tiles[3];
     for (int s = 0; s < 3; ++s) o_tiles[s] = L.take(sizeof(int2) * tiles[s].size());
-    const size_t o_bb = L.take(sizeof(int) * G), o_first = L.take(sizeof(int) * n),
-                 o_nblk = L.take(sizeof(int) * n), o_part = L.take(sizeof(double) * 6 * G),
-                 o_act = L.take(sizeof(int) * 4);
+    const size_t o_roff = L.take(sizeof(int) * (n + 1)),
+                 o_rec = L.take(sizeof(SbSolveRec) * 2 * n), o_done = L.take(sizeof(int) * n),
+                 o_cnt = L.take(sizeof(int) * n), o_part = L.take(sizeof(float2) * 2 * 3 * R);
     e = cudaMalloc((void**)&B->arena, L.bytes);
+    if (e == cudaSuccess) e = cudaMemset(B->arena, 0, L.bytes);
     if (e != cudaSuccess) {
         int r = cuda_fail(e, "sb_batch_create allocation");
         sb_batch_destroy(B);
         return r;
     }
     char* A = B->arena;
-    B->d_descs = (SbBubbleDesc*)(A + o_desc);
-    for (int s = 0; s < 3; ++s) B->d_tiles[s] = (int2*)(A + o_tiles[s]);
-    B->d_blk_bubble = (int*)(A + o_bb);
-    B->d_first = (int*)(A + o_first);
-    B->d_nblk = (int*)(A + o_nblk);
-    B->d_partials = (double*)(A + o_part);
-    B->d_nactive = (int*)(A + o_act);
-    std::vector<SbBubbleDesc> descs(n);
-    for (int k = 0; k < n; ++k) {
-        sb_bubble* b = B->m[k];
-        descs[k].g = b->g;
-        descs[k].ph = b->ph;
-        descs[k].f = b->f;
-        descs[k].cur = b->cur;
-        descs[k].pad = 0;
+    // the members' own descriptors: a member keeps one map parity whether it
+    // is stepped alone or here
+    std::vector<SbBubbleDesc*> descs(n);
+    for (int k = 0; k < n; ++k) descs[k] = B->m[k]->f.self;
+    P.descs = (SbBubbleDesc* const*)(A + o_desc);
+    P.nb = n;
+    for (int s = 0; s < 3; ++s) {
+        P.tiles[s] = (const int2*)(A + o_tiles[s]);
+        P.ntiles[s] = (int)tiles[s].size();
     }
+    for (int st = 0; st < STAGE_COUNT; ++st) P.sel[st] = 1;
+    P.one = nullptr;
+    SbSolveSet& S = P.set;
+    S.descs = P.descs;
+    S.nb = n;
+    S.R = R;
+    S.roff = (const int*)(A + o_roff);
+    S.rec = (SbSolveRec*)(A + o_rec);
+    S.done_at = (int*)(A + o_done);
+    S.cnt = (int*)(A + o_cnt);
+    S.rowpart = (float2*)(A + o_part);
     // members may have work queued on their own streams
     for (sb_bubble* b : B->m) e = e == cudaSuccess ? cudaStreamSynchronize(b->stream) : e;
-    if (e == cudaSuccess) e = cudaMemcpy(B->d_descs, descs.data(), sizeof(SbBubbleDesc) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy((void*)P.descs, descs.data(), sizeof(SbBubbleDesc*) * n, cudaMemcpyHostToDevice);
     for (int s = 0; s < 3 && e == cudaSuccess; ++s)
-        e = cudaMemcpy(B->d_tiles[s], tiles[s].data(), sizeof(int2) * tiles[s].size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(B->d_blk_bubble, blk_bubble.data(), sizeof(int) * G, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(B->d_first, first.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(B->d_nblk, nblk.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(B->d_nactive, 0, sizeof(int) * 4);
+        e = cudaMemcpy((void*)P.tiles[s], tiles[s].data(), sizeof(int2) * tiles[s].size(),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy((void*)S.roff, roff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         int r = cuda_fail(e, "sb_batch_create upload");
         sb_batch_destroy(B);
@@ -990,16 +1037,8 @@ int sb_batch_step(sb_batch* B, int n_steps, double t_frame, double dt) {
     SB_CHECK(cudaSetDevice(B->device));
     int rc = batch_set_params(B, t_frame, dt);
     if (rc != SB_OK) return rc;
-    if (!B->graph && n_steps > 0) {
-        cudaGraph_t graph = nullptr;
-        SB_CHECK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = batch_step_launches(B);
-        cudaError_t e2 = cudaStreamEndCapture(B->stream, &graph);
-        if (e == cudaSuccess) e = e2;
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&B->graph, graph, 0);
-        if (graph) cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
-    }
+    if (n_steps > 0 && !B->graph && (rc = capture_plan(B->plan, B->stream, &B->graph)) != SB_OK)
+        return rc;
     for (int s = 0; s < n_steps; ++s) SB_CHECK(cudaGraphLaunch(B->graph, B->stream));
     batch_advance(B, n_steps);
     return SB_OK;
@@ -1007,24 +1046,12 @@ int sb_batch_step(sb_batch* B, int n_steps, double t_frame, double dt) {
 
 int sb_batch_step_timed(sb_batch* B, int n_steps, double t_frame, double dt, double* stage_ms) {
     if (!B || !stage_ms) return fail(SB_ERR_INVALID, "null argument");
+    if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
     SB_CHECK(cudaSetDevice(B->device));
     int rc = batch_set_params(B, t_frame, dt);
     if (rc != SB_OK) return rc;
-    if (!B->ev[0])
-        for (cudaEvent_t& e : B->ev) SB_CHECK(cudaEventCreate(&e));
     for (int s = 0; s < n_steps; ++s) {
-        SB_CHECK(cudaEventRecord(B->ev[0], B->stream));
-        for (int st = 0; st < STAGE_COUNT; ++st) {
-            SB_CHECK(batch_stage(B, st));
-            SB_CHECK(cudaEventRecord(B->ev[st + 1], B->stream));
-        }
-        SB_CHECK(launch_flip_batch(B->d_descs, (int)B->m.size(), B->stream));
-        SB_CHECK(cudaEventSynchronize(B->ev[STAGE_COUNT]));
-        for (int st = 0; st < STAGE_COUNT; ++st) {
-            float ms = 0.f;
-            SB_CHECK(cudaEventElapsedTime(&ms, B->ev[st], B->ev[st + 1]));
-            stage_ms[st] += ms;
-        }
+        if ((rc = timed_plan_step(B->plan, B->stream, B->ev, stage_ms)) != SB_OK) return rc;
         batch_advance(B, 1);
     }
     return SB_OK;
@@ -1032,24 +1059,20 @@ int sb_batch_step_timed(sb_batch* B, int n_steps, double t_frame, double dt, dou
 
 int sb_batch_autotune(sb_batch* B, double t_frame, double dt, int* tile_sizes) {
     if (!B) return fail(SB_ERR_INVALID, "null batch");
-    double ms[3][STAGE_COUNT + 1] = {};
-    for (int k = 0; k < 3; ++k) {
-        for (int st = 0; st < STAGE_COUNT; ++st) B->sel[st] = k;
-        int rc = sb_batch_step_timed(B, 1, t_frame, dt, ms[k]);
-        if (rc != SB_OK) return rc;
-    }
-    for (int st = 0; st < STAGE_COUNT; ++st) {
-        int best = 1;
-        for (int k = 0; k < 3; ++k)
-            if (ms[k][st] < ms[best][st]) best = k;
-        B->sel[st] = best;
-        if (tile_sizes) tile_sizes[st] = kTileSizes[best];
-    }
+    if (!(dt > 0)) return fail(SB_ERR_INVALID, "bad dt");
+    SB_CHECK(cudaSetDevice(B->device));
+    int rc = batch_set_params(B, t_frame, dt);
+    if (rc != SB_OK) return rc;
+    rc = autotune_plan(B->plan, [&](double* ms) {
+        int r = timed_plan_step(B->plan, B->stream, B->ev, ms);
+        if (r == SB_OK) batch_advance(B, 1);
+        return r;
+    }, tile_sizes);
     if (B->graph) {
         cudaGraphExecDestroy(B->graph);
         B->graph = nullptr;
     }
-    return SB_OK;
+    return rc;
 }
 
 int sb_batch_synchronize(sb_batch* B) {

@@ -6,6 +6,9 @@
 
 namespace sb {
 
+struct SbBubbleDesc;
+struct SbSolveRec;
+
 // Every device array of one bubble.  Fields are FP32, row-major [theta][phi]
 // with row stride nPhi; u_theta has nTheta-1 rows.  "A" buffers hold the
 // state between steps, "adv" buffers the advected intermediate state.
@@ -24,20 +27,26 @@ struct SbFields {
     // analytically; rhs = b (for the norm only)
     float *dmass, *cE, *cS, *rhs, *r0;
     float *x, *dx, *r, *z, *p, *q;                 // solver vectors
-    double *x64;                                   // mixed-precision iterate
+    float2 *xff;                                   // mixed-precision iterate (float-float)
     float2 *pcr;                                   // phi-line factors, (log2 nPhi) x N
     int *pcr_levels;                               // reduction levels per row
-    double *partials;                              // per-block reduction slots
+    // the bubble's own solve set (one system): its device descriptor and
+    // the solver's per-row and per-system scratch (see SbSolveSet)
+    SbBubbleDesc* self;
+    int *roff, *done_at, *cnt;
+    SbSolveRec* rec;
+    float2* rowpart;
     SbStepParams* step;                            // device copy of step scalars
     SbDevStats* stats;
 };
 
-// One bubble of a batch, as the batched kernels see it (device memory).
+// One bubble as the kernels see it (device memory, one per bubble, shared
+// by every set that steps the bubble).
 struct SbBubbleDesc {
     SbGrid g;
     SbPhys ph;
     SbFields f;
-    int cur;   // map parity, flipped on the device after every batch step
+    int cur;   // map parity, flipped on the device at the end of every step
     int pad;
 };
 
@@ -46,58 +55,85 @@ struct SolverConfig {
     int max_iter;
     double tol;     // relative residual ||b - A x|| / ||b||
     int precond;    // 0: Jacobi, 1: exact phi-line (periodic tridiagonal per row)
+    int ring;       // factor levels staged in shared memory at once (set at launch)
 };
 
 // Step stages in launch order (sb_step.cu, sb_solver.cu).  `cur` selects the
-// map ping-pong buffers.  Each stage is one kernel launch.
+// map ping-pong buffers.  Each stage is one kernel launch; a step ends with a
+// flip of every bubble's map parity (one more launch).
 enum SbStage {
     STAGE_MAPS = 0,   // k_advect_maps: characteristic maps, gamma, air flow
     STAGE_VELOCITY,   // k_velocity: u_theta / u_phi self-advection
     STAGE_BIMOCQ,     // k_bimocq: thickness through the composed maps
     STAGE_ASSEMBLE,   // k_assemble: implicit surfactant system
-    STAGE_SOLVE,      // k_pcg: cooperative PCG
+    STAGE_SOLVE,      // k_solve: cooperative PCG
     STAGE_POST,       // k_post: forces, thickness, increments
     STAGE_ACCUM,      // k_accum: BIMOCQ accumulation + distortion
     STAGE_REINIT,     // k_reinit: conditional map re-initialisation (cooperative)
     STAGE_COUNT
 };
 
-cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbFields& f,
-                         const struct SolverConfig& cfg, int cur, cudaStream_t s);
-// Occupancy queries and function attributes of the cooperative kernels, done
-// once before any stream capture.
-cudaError_t prepare_launches(const SbGrid& g, const struct SolverConfig& cfg);
-cudaError_t prepare_solve(const SbGrid& g, const struct SolverConfig& cfg);
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s);
 cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s);
 
-// Batched stages: one launch per stage over the tiles of every bubble.
-// tiles[k] = (bubble, first cell) of block k; `block` threads per tile.
-cudaError_t launch_stage_batch(int stage, const SbBubbleDesc* descs, const int2* tiles, int ntiles,
-                               int block, cudaStream_t s);
-cudaError_t launch_reinit_batch(const SbBubbleDesc* descs, int nb, const int2* tiles, int ntiles,
-                                cudaStream_t s);
-cudaError_t launch_flip_batch(SbBubbleDesc* descs, int nb, cudaStream_t s);
-int reinit_batch_blocks();
-
-// Batched implicit solve: every bubble's rows are owned by its own
-// contiguous range of blocks.
-struct SbBatchSolve {
-    const SbBubbleDesc* descs;
-    int nb;
-    const int* blk_bubble;     // [G] bubble of each block
-    const int* bub_first_blk;  // [nb]
-    const int* bub_nblk;       // [nb]
-    double* partials;          // [2 * 3 * G]
-    int* nactive;              // [3] bubbles still iterating (rotating counters)
+// Scalars of one system of a solve, written by the block that completes the
+// system's last row in a phase and read in the next phase (double buffered).
+struct SbSolveRec {
+    double rz, rr, bnorm, tol2, alpha;
+    float beta;
+    int state;  // iterate, or check the true residual / restart (mixed mode)
+    int it;
+    int conv;
 };
-cudaError_t prepare_solve_batch(int maxNP, const SolverConfig& cfg, int* blocks);
-cudaError_t launch_solve_batch(const SbBatchSolve& bs, int G, int maxNP, const SolverConfig& cfg,
-                               cudaStream_t s);
 
-// Implicit surfactant solve (sb_solver.cu).
-cudaError_t launch_solve(const SbGrid& g, const SbPhys& ph, const SbFields& f,
-                         const SolverConfig& cfg, cudaStream_t s);
-int solver_partials_needed(const SbGrid& g);
+// A set of implicit systems solved by one cooperative launch: the system of
+// one bubble, or the systems of every bubble of a batch (at most 1024, with
+// sum over systems of nT (2 nT + 256) below 2^32).  Device arrays.
+struct SbSolveSet {
+    SbBubbleDesc* const* descs;  // [nb] device pointers to each bubble's descriptor
+    int nb;
+    int R;                      // theta rows of all systems
+    const int* roff;            // [nb + 1] first row of each system in the row list
+    SbSolveRec* rec;            // [2 * nb]
+    int* done_at;               // [nb] first phase in which the system is finished
+    int* cnt;                   // [nb] rows completed in the current phase (0 between launches)
+    float2* rowpart;            // [2][3 * R] float-float partial sums of every row, by phase parity
+};
+
+// Implicit surfactant solve (sb_solver.cu).  prepare_solve sets the kernel
+// attributes for rows of up to maxNP columns and returns the co-resident
+// block count; call it before any stream capture.
+cudaError_t prepare_solve(int maxNP, const SolverConfig& cfg, int* max_blocks);
+cudaError_t launch_solve(const SbSolveSet& set, int maxNP, const SolverConfig& cfg,
+                         cudaStream_t s);
+// The same solve for a set of one system, with the descriptor passed as
+// kernel parameters (bit-identical results).
+cudaError_t launch_solve_one(const SbGrid& g, const SbFields& f, const SbSolveSet& set,
+                             const SolverConfig& cfg, cudaStream_t s);
+
+// Cells per block of the three tile sizes the stage kernels can use.
+extern const int kTileSizes[3];
+
+// Everything one step launches over a set of bubbles (one bubble, or every
+// bubble of a batch; sb_step.cu).  Device arrays: descs[k] points to bubble
+// k's own descriptor, so a bubble has one map parity whichever set steps it.
+struct SbStepPlan {
+    SbBubbleDesc* const* descs;  // [nb]
+    int nb;
+    const int2* tiles[3];        // (bubble, first cell) of every tile, per tile size
+    int ntiles[3];
+    int sel[STAGE_COUNT];        // tile size (index into kTileSizes) of every stage
+    SbSolveSet set;              // every bubble's implicit system
+    int maxNP;                   // widest grid of the set
+    SolverConfig solver;
+    const SbBubbleDesc* one;     // host copy of the descriptor of a set of one bubble, else null
+};
+
+// Occupancy queries and kernel attributes; call before any stream capture.
+cudaError_t prepare_plan(const SbStepPlan& P);
+// One stage of a step, the map-parity flip that ends a step, or the whole step.
+cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s);
+cudaError_t launch_plan_flip(const SbStepPlan& P, cudaStream_t s);
+cudaError_t launch_plan_step(const SbStepPlan& P, cudaStream_t s);
 
 }  // namespace sb

@@ -5,11 +5,16 @@
 // is the increment dx = gamma_new - gamma_adv, starting from dx = 0, which is
 // the same iteration with the large common part removed.
 //
-// One cooperative launch runs the whole solve.  Each block owns whole theta
-// rows; phases are separated by grid-wide barriers; dot products are summed
-// per block and then by every block in the same block order, so every block
-// sees bit-identical scalars and takes the same loop decisions (the
-// iteration count is bounded by max_iter).
+// One cooperative launch solves a set of systems: the one system of a
+// bubble, or the systems of every bubble of a batch.  The theta rows of all
+// systems form one list that is dealt to the blocks round robin; a phase
+// (separated from the next by a grid barrier) visits the rows of the
+// systems still iterating, so a system that needs more iterations than the
+// others is spread over the whole GPU.  Every row publishes its partial dot
+// products; the block that completes the last row of a system in a phase
+// sums that system's row partials in row order and advances the system's
+// scalars.  Scalars therefore do not depend on how rows are distributed:
+// a bubble solved alone and inside a batch gives bit-identical results.
 //
 // Preconditioner: exact solve of each theta row's periodic tridiagonal block
 // (phi couplings; the theta couplings stay on its diagonal).  Near the poles
@@ -27,6 +32,10 @@
 // relative residual target holds).
 #include <cooperative_groups.h>
 
+#include <algorithm>
+#include <climits>
+
+#include "sb_ff.cuh"
 #include "sb_internal.h"
 
 namespace cg = cooperative_groups;
@@ -36,71 +45,138 @@ namespace sb {
 namespace {
 
 constexpr int kSolveBlock = 256;
+constexpr int kWarps = kSolveBlock / 32;  // row partials per row: one per warp
+constexpr int kMaxRing = 12;          // >= log2(nP) for every supported nP
+constexpr int kWaitPolls = 1 << 22;   // mbarrier polls before a copy counts as lost
+constexpr int kMaxSystems = 1024;     // systems of one solve set
+constexpr int kRowChunk = 16;         // rows a block publishes at a time
+enum { ST_ITER = 0, ST_CHECK = 1 };
 
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Block partial sums of three values into part[3 * blockIdx.x + k].
-__device__ __forceinline__ void block_partial3(double a, double b, double c, double* part) {
-    __shared__ double sm[3][kSolveBlock / 32];
-    a = warp_sum(a);
-    b = warp_sum(b);
-    c = warp_sum(c);
+// Block sums of three float-float values, returned to every thread.  Fixed
+// order (lanes by shuffle tree, then the warps in order), so equal inputs
+// give equal sums in every block.
+__device__ __forceinline__ void block_sum3(ff& a, ff& b, ff& c) {
+    __shared__ ff part[3][kSolveBlock / 32];
+    a = ff_warp_sum(a);
+    b = ff_warp_sum(b);
+    c = ff_warp_sum(c);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) { sm[0][w] = a; sm[1][w] = b; sm[2][w] = c; }
+    if (l == 0) { part[0][w] = a; part[1][w] = b; part[2][w] = c; }
     __syncthreads();
-    if (w == 0) {
-        double x = l < kSolveBlock / 32 ? sm[0][l] : 0.0;
-        double y = l < kSolveBlock / 32 ? sm[1][l] : 0.0;
-        double z = l < kSolveBlock / 32 ? sm[2][l] : 0.0;
-        x = warp_sum(x); y = warp_sum(y); z = warp_sum(z);
-        if (l == 0) {
-            part[3 * blockIdx.x + 0] = x;
-            part[3 * blockIdx.x + 1] = y;
-            part[3 * blockIdx.x + 2] = z;
-        }
+    ff x = ff_zero(), y = ff_zero(), z = ff_zero();
+#pragma unroll
+    for (int k = 0; k < kSolveBlock / 32; ++k) {
+        x = ff_add(x, part[0][k]);
+        y = ff_add(y, part[1][k]);
+        z = ff_add(z, part[2][k]);
+    }
+    __syncthreads();
+    a = x; b = y; c = z;
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory staging of the stored cyclic-reduction factors.  Each
+// (level, row) factor slice is nP contiguous float2 in global memory; one
+// thread copies it into one of K ring slots with a bulk asynchronous copy
+// (cp.async.bulk, completion counted on the slot's mbarrier), so the levels
+// of a row arrive together instead of one dependent load per level.
+struct Ring {
+    float2* buf;    // K slots of nP float2 at the start of dynamic shared memory
+    uint32_t bar;   // shared address of K mbarriers, 8 bytes apart
+    int K;
+    unsigned seq;   // slices issued (and waited for) by this block so far
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void ring_init(Ring& R, uint64_t* bars, float* sm, int K) {
+    R.buf = reinterpret_cast<float2*>(sm);
+    R.bar = smem_u32(bars);
+    R.K = K;
+    R.seq = 0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < K; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(R.bar + 8 * s) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 }
 
-// Sum of all blocks' partials, same order in every block.
-__device__ __forceinline__ void all_sum3(const double* part, int G, double& A, double& B,
-                                         double& C) {
-    __shared__ double res[3];
-    if (threadIdx.x < 32) {
-        double x = 0.0, y = 0.0, z = 0.0;
-        for (int k = threadIdx.x; k < G; k += 32) {
-            x += part[3 * k + 0];
-            y += part[3 * k + 1];
-            z += part[3 * k + 2];
-        }
-        x = warp_sum(x); y = warp_sum(y); z = warp_sum(z);
-        if (threadIdx.x == 0) { res[0] = x; res[1] = y; res[2] = z; }
-    }
-    __syncthreads();
-    A = res[0]; B = res[1]; C = res[2];
-    __syncthreads();
+// Thread 0: start copying the slice `src` (n float2) into the slot of seq.
+__device__ __forceinline__ void ring_issue(const Ring& R, unsigned seq, const float2* src, int n) {
+    if (threadIdx.x != 0) return;
+    const unsigned s = seq % (unsigned)R.K;
+    const uint32_t bar = R.bar + 8 * s;
+    const uint32_t dst = smem_u32(R.buf + (size_t)s * n);
+    const uint32_t bytes = (uint32_t)n * 8u;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
 }
 
-// (A v)_c for a cell c = (i, j); T is float or double.
-template <typename T, typename A>
-__device__ __forceinline__ A apply_A(const SbGrid& g, const SbFields& f, const T* __restrict__ v,
-                                     int c, int i, int j) {
+// Every thread: wait (bounded) until the slice of seq has landed; returns
+// its slot.  A wait that gives up is counted in the stats, and the solve is
+// then reported as failed instead of hanging.
+__device__ __forceinline__ const float2* ring_wait(const Ring& R, unsigned seq, int n,
+                                                   SbDevStats* st) {
+    const unsigned s = seq % (unsigned)R.K;
+    const uint32_t bar = R.bar + 8 * s;
+    const uint32_t parity = (seq / (unsigned)R.K) & 1u;
+    for (int k = 0;; ++k) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) break;
+        if (k >= kWaitPolls) {
+            if (threadIdx.x == 0) atomicAdd(&st->wait_faults, 1);
+            break;
+        }
+    }
+    return R.buf + (size_t)s * n;
+}
+
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ ff ld_ff(const float2* v, int c) {
+    const float2 t = v[c];
+    return {t.x, t.y};
+}
+
+// (A x)_c in float-float for the float-float iterate x at cell c = (i, j).
+__device__ __forceinline__ ff apply_A_ff(const SbGrid& g, const SbFields& f, const float2* x, int c,
+                                         int i, int j) {
     const int nP = g.nP;
     const int e = i * nP + ((j + 1) & g.maskP);
     const int w = i * nP + ((j - 1) & g.maskP);
-    const A vc = (A)v[c];
-    A s = (A)f.dmass[c] * vc + (A)f.cE[c] * (vc - (A)v[e]) + (A)f.cE[w] * (vc - (A)v[w]);
-    if (i < g.nT - 1) s += (A)f.cS[c] * (vc - (A)v[c + nP]);
-    if (i > 0) s += (A)f.cS[c - nP] * (vc - (A)v[c - nP]);
+    const ff xc = ld_ff(x, c);
+    ff s = ff_mul_f(xc, f.dmass[c]);
+    s = ff_add(s, ff_mul_f(ff_add(xc, ff_neg(ld_ff(x, e))), f.cE[c]));
+    s = ff_add(s, ff_mul_f(ff_add(xc, ff_neg(ld_ff(x, w))), f.cE[w]));
+    if (i < g.nT - 1) s = ff_add(s, ff_mul_f(ff_add(xc, ff_neg(ld_ff(x, c + nP))), f.cS[c]));
+    if (i > 0) s = ff_add(s, ff_mul_f(ff_add(xc, ff_neg(ld_ff(x, c - nP))), f.cS[c - nP]));
     return s;
 }
 
+// Dot-product terms: exact products in mixed mode, float products in plain
+// mode, accumulated in float-float.
+template <bool MIXED>
+__device__ __forceinline__ ff acc(ff s, float a, float b) {
+    return MIXED ? ff_add_prod(s, a, b) : ff_add_f(s, __fmul_rn(a, b));
+}
+
+// Column of element k of this thread in a row.
+__device__ __forceinline__ int col_of(int k) { return threadIdx.x + k * kSolveBlock; }
+
 // z = M^-1 r on theta row i: Jacobi, or the exact periodic tridiagonal solve.
-// sm holds 4 * nP floats.  Adds this row's r.z and r.r to rz, rr.
-// PER = equations per thread (nP <= PER * kSolveBlock).
+// rv[k] holds r at column col_of(k) (this thread's elements).  Adds the
+// row's r.z and r.r to rz, rr.  PER = equations per thread
+// (nP <= PER * kSolveBlock).
 //
 // The row matrix does not change during a solve, so the first application
 // (BUILD) runs the full cyclic reduction and stores, per level, the two
@@ -110,20 +186,25 @@ __device__ __forceinline__ A apply_A(const SbGrid& g, const SbFields& f, const T
 template <bool MIXED, int PER, bool BUILD>
 __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f,
                                                  const SolverConfig& cfg, int i, float* sm,
-                                                 double& rz, double& rr) {
+                                                 Ring& R, const float (&rv)[PER], ff& rz,
+                                                 ff& rr) {
     const int nP = g.nP, nT = g.nT, mask = g.maskP;
     const int row = i * nP;
     if (cfg.precond == 0) {
-        for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-            const int c = row + j;
-            float dg = f.dmass[c] + f.cE[c] + f.cE[row + ((j - 1) & mask)];
-            if (i < nT - 1) dg += f.cS[c];
-            if (i > 0) dg += f.cS[c - nP];
-            const float rc = f.r[c];
-            const float zc = rc / dg;
-            f.z[c] = zc;
-            rz += MIXED ? (double)rc * (double)zc : (double)(rc * zc);
-            rr += MIXED ? (double)rc * (double)rc : (double)(rc * rc);
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int j = col_of(k);
+            if (j < nP) {
+                const int c = row + j;
+                float dg = f.dmass[c] + f.cE[c] + f.cE[row + ((j - 1) & mask)];
+                if (i < nT - 1) dg += f.cS[c];
+                if (i > 0) dg += f.cS[c - nP];
+                const float rc = rv[k];
+                const float zc = rc / dg;
+                f.z[c] = zc;
+                rz = acc<MIXED>(rz, rc, zc);
+                rr = acc<MIXED>(rr, rc, rc);
+            }
         }
         return;
     }
@@ -137,7 +218,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         float* D = sm + 3 * nP;   // right-hand side
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
-            const int j = threadIdx.x + k * kSolveBlock;
+            const int j = col_of(k);
             if (j < nP) {
                 const int c = row + j;
                 float ex = f.dmass[c];
@@ -146,7 +227,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
                 E[j] = ex;
                 U[j] = f.cE[c];
                 L[j] = f.cE[row + ((j - 1) & mask)];
-                D[j] = f.r[c];
+                D[j] = rv[k];
             }
         }
         __syncthreads();
@@ -161,7 +242,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
             float nE[PER], nL[PER], nU[PER], nD[PER];
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
-                const int j = threadIdx.x + k * kSolveBlock;
+                const int j = col_of(k);
                 if (j < nP) {
                     const int jm = (j - s) & mask, jp = (j + s) & mask;
                     const float bm = E[jm] + L[jm] + U[jm];
@@ -180,7 +261,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
             bool need = false;
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
-                const int j = threadIdx.x + k * kSolveBlock;
+                const int j = col_of(k);
                 if (j < nP) {
                     E[j] = nE[k]; L[j] = nL[k]; U[j] = nU[k]; D[j] = nD[k];
                     need |= (nL[k] + nU[k]) > 1.4901161e-8f * nE[k];
@@ -195,7 +276,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         if (threadIdx.x == 0) f.pcr_levels[i] = decoupled ? levels : -levels;
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
-            const int j = threadIdx.x + k * kSolveBlock;
+            const int j = col_of(k);
             if (j < nP) {
                 float c1, c2;
                 if (decoupled) {
@@ -212,430 +293,648 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
                 fac[levels * lvl_stride + j] = make_float2(c1, c2);
                 const int kk = (j + nP / 2) & mask;
                 const float zj = c1 * D[j] + c2 * D[kk];
-                const int c = row + j;
-                const float rc = f.r[c];
-                f.z[c] = zj;
-                rz += MIXED ? (double)rc * (double)zj : (double)(rc * zj);
-                rr += MIXED ? (double)rc * (double)rc : (double)(rc * rc);
+                const float rc = rv[k];
+                f.z[row + j] = zj;
+                rz = acc<MIXED>(rz, rc, zj);
+                rr = acc<MIXED>(rr, rc, rc);
             }
         }
+        // the factors written here (global) and the E, L, U, D arrays
+        // (shared, where the ring slots will land) are next touched by bulk
+        // asynchronous copies: order these generic writes before them
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         return;
     }
-    // replay with the stored factors; D ping-pongs between two buffers
-    float* D0 = sm;
-    float* D1 = sm + nP;
+    // replay with the stored factors: the row's slices stream into the
+    // shared-memory ring (all of them at once when the ring is deep enough);
+    // D ping-pongs between two buffers behind the ring
+    float* D0 = sm + 2 * R.K * nP;
+    float* D1 = D0 + nP;
     const int lv = f.pcr_levels[i];
     const int levels = lv < 0 ? -lv : lv;
+    const int nbuf = levels + 1;  // reduction levels + final factors
+    const unsigned base = R.seq;
+    for (int l = 0; l < nbuf && l < R.K; ++l) ring_issue(R, base + l, fac + l * lvl_stride, nP);
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = threadIdx.x + k * kSolveBlock;
-        if (j < nP) D0[j] = f.r[row + j];
+        const int j = col_of(k);
+        if (j < nP) D0[j] = rv[k];
     }
     __syncthreads();
-    // the factors of level l + 1 are loaded while level l is reduced
-    float2 acn[PER];
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int j = threadIdx.x + k * kSolveBlock;
-        acn[k] = j < nP ? fac[j] : make_float2(0.0f, 0.0f);
-    }
     int s = 1;
     for (int l = 0; l < levels; ++l, s <<= 1) {
-        float* Din = (l & 1) ? D1 : D0;
+        const float2* ac = ring_wait(R, base + l, nP, f.stats);
+        const float* Din = (l & 1) ? D1 : D0;
         float* Dout = (l & 1) ? D0 : D1;
-        float2 ac[PER];
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
-            ac[k] = acn[k];
-            const int j = threadIdx.x + k * kSolveBlock;
-            if (j < nP) acn[k] = fac[(l + 1) * lvl_stride + j];
-        }
-#pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int j = threadIdx.x + k * kSolveBlock;
-            if (j < nP)
-                Dout[j] = Din[j] + ac[k].x * Din[(j - s) & mask] + ac[k].y * Din[(j + s) & mask];
+            const int j = col_of(k);
+            if (j < nP) {
+                const float2 c = ac[j];
+                Dout[j] = Din[j] + c.x * Din[(j - s) & mask] + c.y * Din[(j + s) & mask];
+            }
         }
         __syncthreads();
+        // slot of level l is free again
+        if (l + R.K < nbuf) ring_issue(R, base + l + R.K, fac + (l + R.K) * lvl_stride, nP);
     }
+    const float2* fin = ring_wait(R, base + levels, nP, f.stats);
     const float* Dn = (levels & 1) ? D1 : D0;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = threadIdx.x + k * kSolveBlock;
+        const int j = col_of(k);
         if (j < nP) {
-            const float2 cc = acn[k];  // the final factors
+            const float2 cc = fin[j];
             const float zj = cc.x * Dn[j] + cc.y * Dn[(j + nP / 2) & mask];
+            const float rc = rv[k];
+            f.z[row + j] = zj;
+            rz = acc<MIXED>(rz, rc, zj);
+            rr = acc<MIXED>(rr, rc, rc);
+        }
+    }
+    __syncthreads();
+    R.seq = base + nbuf;
+}
+
+// ---------------------------------------------------------------------------
+// Row bodies.  Every thread handles the columns col_of(0 .. PER-1) of a theta
+// row, one column after the other (measured faster than issuing all loads
+// of a thread's columns first, which costs registers).  Dot-product terms
+// are accumulated in column order.
+
+// dx = 0, r = r0, p_old = 0; rv = r; adds |rhs|^2 to bb.
+template <bool MIXED, int PER>
+__device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int i,
+                                         float (&rv)[PER], ff& bb) {
+    const int nP = g.nP, row = i * nP;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        rv[k] = 0.0f;
+        if (j < nP) {
             const int c = row + j;
-            const float rc = f.r[c];
-            f.z[c] = zj;
-            rz += MIXED ? (double)rc * (double)zj : (double)(rc * zj);
-            rr += MIXED ? (double)rc * (double)rc : (double)(rc * rc);
+            rv[k] = f.r0[c];
+            const float rhs = f.rhs[c];
+            if (MIXED) f.xff[c] = make_float2(0.0f, 0.0f);
+            else f.dx[c] = 0.0f;
+            f.r[c] = rv[k];
+            f.q[c] = 0.0f;
+            bb = ff_add_prod(bb, rhs, rhs);
         }
     }
+}
+
+// p_new = z + beta p_old on the row and, on the fly, on the neighbours it
+// reads (so no barrier is needed between forming p and using it); q = A p_new
+// is kept in f.x.  Returns the row's p.q.
+template <bool MIXED, int PER>
+__device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i, float beta,
+                                           const float* __restrict__ pold,
+                                           float* __restrict__ pnew) {
+    const int nP = g.nP, nT = g.nT, row = i * nP;
+    const float* __restrict__ z = f.z;
+    ff pq = ff_zero();
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        if (j < nP) {
+            const int c = row + j;
+            const int e = row + ((j + 1) & g.maskP);
+            const int w = row + ((j - 1) & g.maskP);
+            const float pc = z[c] + beta * pold[c];
+            float qf = f.dmass[c] * pc + f.cE[c] * (pc - (z[e] + beta * pold[e])) +
+                       f.cE[w] * (pc - (z[w] + beta * pold[w]));
+            if (i < nT - 1) {
+                const int sc = c + nP;
+                qf += f.cS[c] * (pc - (z[sc] + beta * pold[sc]));
+            }
+            if (i > 0) {
+                const int nc = c - nP;
+                qf += f.cS[nc] * (pc - (z[nc] + beta * pold[nc]));
+            }
+            pnew[c] = pc;
+            f.x[c] = qf;
+            pq = acc<MIXED>(pq, pc, qf);
+        }
+    }
+    return pq;
+}
+
+// True residual r = r0 - A x of the float-float iterate (mixed mode),
+// carried in float-float; stores it (rounded) in f.r and returns the row's
+// |r|^2.
+template <int PER>
+__device__ __forceinline__ ff row_true_residual(const SbGrid& g, const SbFields& f, int i) {
+    const int nP = g.nP, row = i * nP;
+    ff a = ff_zero();
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        if (j < nP) {
+            const int c = row + j;
+            const ff r = ff_add_f(ff_neg(apply_A_ff(g, f, f.xff, c, i, j)), f.r0[c]);
+            f.r[c] = ff_to_f(r);
+            // r^2 = hi^2 + 2 hi lo (+ lo^2, below the float-float precision)
+            a = ff_add_f(ff_add_prod(a, r.hi, r.hi), __fmul_rn(2.0f, __fmul_rn(r.hi, r.lo)));
+        }
+    }
+    return a;
+}
+
+// x += alpha p_new, r -= alpha q; rv = the new r.
+template <bool MIXED, int PER>
+__device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, int i, double alpha,
+                                           const float* __restrict__ pnew, float (&rv)[PER]) {
+    const int nP = g.nP, row = i * nP;
+    const float af = (float)alpha;
+    const ff a2 = ff_from_d(alpha);
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        rv[k] = 0.0f;
+        if (j < nP) {
+            const int c = row + j;
+            const float pc = pnew[c];
+            if (MIXED) {
+                const ff x = ff_add(ld_ff(f.xff, c), ff_mul_f(a2, pc));
+                f.xff[c] = make_float2(x.hi, x.lo);
+            } else {
+                f.dx[c] += af * pc;
+            }
+            rv[k] = f.r[c] - af * f.x[c];
+            f.r[c] = rv[k];
+        }
+    }
+}
+
+// rv = r (restart from the refined iterate's residual).
+template <int PER>
+__device__ __forceinline__ void row_load_r(const SbGrid& g, const SbFields& f, int i,
+                                           float (&rv)[PER]) {
+    const int nP = g.nP, row = i * nP;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        rv[k] = j < nP ? f.r[row + j] : 0.0f;
+    }
+}
+
+// The increment and the new gamma: dx, x = gamma_adv + dx.
+template <bool MIXED, int PER>
+__device__ __forceinline__ void row_final(const SbGrid& g, const SbFields& f, int i) {
+    const int nP = g.nP, row = i * nP;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        if (j < nP) {
+            const int c = row + j;
+            const float dx = MIXED ? ff_to_f(ld_ff(f.xff, c)) : f.dx[c];
+            f.dx[c] = dx;
+            f.x[c] = f.gam_adv[c] + dx;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-system scalars.  Records are read with L2 loads (__ldcg): they are
+// written by other blocks between phases.
+__device__ __forceinline__ SbSolveRec load_rec(const SbSolveRec* p) {
+    SbSolveRec r;
+    r.rz = __ldcg(&p->rz);
+    r.rr = __ldcg(&p->rr);
+    r.bnorm = __ldcg(&p->bnorm);
+    r.tol2 = __ldcg(&p->tol2);
+    r.alpha = __ldcg(&p->alpha);
+    r.beta = __ldcg(&p->beta);
+    r.state = __ldcg(&p->state);
+    r.it = __ldcg(&p->it);
+    r.conv = __ldcg(&p->conv);
+    return r;
+}
+
+// Final statistics of a system that leaves the solve.
+__device__ __forceinline__ void write_stats(SbDevStats* st, const SbSolveRec& rc) {
+    st->solver_iters = rc.it;
+    st->solver_rel_resid = sqrt(rc.rr) / rc.bnorm;
+    st->solver_b_norm = rc.bnorm;
+    st->solver_converged = rc.conv;
+}
+
+// The loop head of CG: iteration limit, NaN, target reached (mixed mode
+// then checks the true residual first).  Returns true when the system is
+// finished.
+template <bool MIXED>
+__device__ __forceinline__ bool loop_head(SbSolveRec& rc, const SolverConfig& cfg) {
+    if (rc.it >= cfg.max_iter || !(rc.rr == rc.rr)) return true;
+    if (rc.rr <= rc.tol2) {
+        if (!MIXED) {
+            rc.conv = 1;
+            return true;
+        }
+        rc.state = ST_CHECK;
+        return false;
+    }
+    rc.state = ST_ITER;
+    return false;
+}
+
+// Advances a system's scalars past phase p with its summed row partials
+// (A, B, C); returns true when the system is finished.
+//   p = 0 (set-up): A = r.z, B = r.r, C = |b|^2
+//   odd p:  iterate -> A = p.q;   check -> A = |r_true|^2
+//   even p: iterate -> A = r.z, B = r.r (after the update); restart -> same
+// Every path that advances a system (one block for a batch, every block
+// for a single system) runs this same function on the same sums.
+template <bool MIXED>
+__device__ __forceinline__ bool transition(SbSolveRec& rc, int p, double A, double B, double C,
+                                           const SolverConfig& cfg) {
+    if (p == 0) {
+        rc.bnorm = C > 0.0 ? sqrt(C) : 1.0;
+        // the FP64 iterate is driven to 0.8 tol so that the returned FP32
+        // gamma (whose rounding adds up to a few percent) still meets tol
+        rc.tol2 = (MIXED ? 0.64 : 1.0) * cfg.tol * cfg.tol * rc.bnorm * rc.bnorm;
+        rc.rz = A;
+        rc.rr = B;
+        rc.alpha = 0.0;
+        rc.beta = 0.0f;
+        rc.it = 0;
+        rc.conv = 0;
+        rc.state = ST_ITER;
+        return loop_head<MIXED>(rc, cfg);
+    }
+    if (p & 1) {
+        if (rc.state == ST_ITER) {
+            if (!(A > 0.0)) return true;  // breakdown: keep the current iterate
+            rc.alpha = rc.rz / A;
+            return false;
+        }
+        rc.rr = A;
+        if (rc.rr <= rc.tol2) {
+            rc.conv = 1;
+            return true;
+        }
+        return false;  // restart from the refined iterate
+    }
+    if (rc.state == ST_ITER) {
+        rc.beta = (float)(A / rc.rz);
+        rc.rz = A;
+        rc.rr = B;
+        ++rc.it;
+        return loop_head<MIXED>(rc, cfg);
+    }
+    rc.rz = A;
+    rc.rr = B;
+    rc.beta = 0.0f;
+    rc.state = ST_ITER;
+    return false;
+}
+
+// Thread 0 of the block that completed system b's last row in phase p
+// (sets of several systems): advance the system and publish its scalars
+// for phase p + 1, or retire it (from phase p + 1 on no block visits its
+// rows).
+template <bool MIXED>
+__device__ __forceinline__ void advance(const SbSolveSet& S, int b, int p, double A, double B,
+                                        double C, const SolverConfig& cfg) {
+    SbSolveRec rc = load_rec(S.rec + (p & 1) * S.nb + b);
+    if (transition<MIXED>(rc, p, A, B, C, cfg)) {
+        write_stats(S.descs[b]->f.stats, rc);
+        S.done_at[b] = p + 1;
+    } else {
+        S.rec[((p + 1) & 1) * S.nb + b] = rc;
+        if (p == 0) S.done_at[b] = INT_MAX;
+    }
+    S.cnt[b] = 0;
+}
+
+// Sum of system b's row partials in row order (the same in every block).
+__device__ __forceinline__ void system_sum3(const SbSolveSet& S, int b, int nT, int parity,
+                                            double& A, double& B, double& C) {
+    const float2* p = S.rowpart + 3 * ((size_t)parity * S.R + S.roff[b]);
+    ff x = ff_zero(), y = ff_zero(), z = ff_zero();
+#pragma unroll 4
+    for (int i = threadIdx.x; i < nT; i += kSolveBlock) {
+        const float2 u = __ldcg(p + 3 * i), v = __ldcg(p + 3 * i + 1), w = __ldcg(p + 3 * i + 2);
+        x = ff_add(x, {u.x, u.y});
+        y = ff_add(y, {v.x, v.y});
+        z = ff_add(z, {w.x, w.y});
+    }
+    block_sum3(x, y, z);
+    A = ff_to_d(x);
+    B = ff_to_d(y);
+    C = ff_to_d(z);
+}
+
+// Rows [i, i + n) of system b were computed by this block; warp w left its
+// share of row i + k in s_part[k][w].  Folds every row's warp shares in warp
+// order into the row's partial, publishes the partials and counts the rows.
+// Returns (in every thread) whether these were the system's last rows.
+__device__ __forceinline__ bool publish_rows(const SbSolveSet& S, int b, int nT, int i, int n,
+                                             int parity, bool count, ff (*s_part)[kWarps][3],
+                                             int* s_last) {
+    __syncthreads();
+    if (threadIdx.x < n) {
+        ff x = ff_zero(), y = ff_zero(), z = ff_zero();
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            x = ff_add(x, s_part[threadIdx.x][w][0]);
+            y = ff_add(y, s_part[threadIdx.x][w][1]);
+            z = ff_add(z, s_part[threadIdx.x][w][2]);
+        }
+        float2* o = S.rowpart + 3 * ((size_t)parity * S.R + S.roff[b] + i + threadIdx.x);
+        o[0] = make_float2(x.hi, x.lo);
+        o[1] = make_float2(y.hi, y.lo);
+        o[2] = make_float2(z.hi, z.lo);
+        if (count) __threadfence();  // the partial before the count
+    }
+    __syncthreads();
+    if (!count) return false;
+    if (threadIdx.x == 0) {
+        const int old = atomicAdd(&S.cnt[b], n);
+        *s_last = (old + n == nT);
+    }
+    __syncthreads();
+    return *s_last != 0;
+}
+
+// Work weight of one theta row of a system with nT rows (nP = 2 nT columns
+// plus a fixed per-row cost of about 256 columns).
+__device__ __forceinline__ unsigned row_weight(int nT) { return 2u * (unsigned)nT + 256u; }
+
+// s_pre[b] = total weight of the systems before b that are active in phase
+// p (every system in phase 0 and in the final pass, p < 0); s_pre[nb] is the
+// total.  Every block computes the same table: a system's done_at only
+// moves during phase p from INT_MAX to p + 1, which reads as active in p.
+__device__ __forceinline__ unsigned active_prefix(const SbSolveSet& S, int p, unsigned* s_pre) {
+    __shared__ unsigned wsum[kSolveBlock / 32];
+    __shared__ unsigned carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < S.nb; base += kSolveBlock) {
+        const int b = base + threadIdx.x;
+        unsigned v = 0;
+        if (b < S.nb) {
+            const bool act = p <= 0 || __ldcg(&S.done_at[b]) > p;
+            if (act) v = (unsigned)(S.roff[b + 1] - S.roff[b]) * row_weight(S.roff[b + 1] - S.roff[b]);
+        }
+        unsigned incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        unsigned before = carry;
+        for (int k = 0; k < w; ++k) before += wsum[k];
+        if (b < S.nb) s_pre[b] = before + incl - v;
+        __syncthreads();
+        if (threadIdx.x == kSolveBlock - 1) carry = before + incl;
+        __syncthreads();
+    }
+    const unsigned total = carry;
+    if (threadIdx.x == 0) s_pre[S.nb] = total;
+    __syncthreads();
+    return total;
+}
+
+// First system whose weight range ends after `x` (s_pre is non-decreasing).
+__device__ __forceinline__ int first_system_after(const unsigned* s_pre, int nb, unsigned x) {
+    int lo = 0, hi = nb;  // answer in [0, nb)
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s_pre[mid + 1] > x) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Stages system b's descriptor in shared memory.
+__device__ __forceinline__ void stage_desc(const SbSolveSet& S, int b, SbBubbleDesc* s_d) {
+    constexpr int kWords = (int)(sizeof(SbBubbleDesc) / 4);
+    const int* src = reinterpret_cast<const int*>(S.descs[b]);
+    int* dst = reinterpret_cast<int*>(s_d);
+    for (int k = threadIdx.x; k < kWords; k += blockDim.x) dst[k] = src[k];
     __syncthreads();
 }
 
-// One cooperative launch per solve.  The search direction is double
-// buffered: the SpMV phase forms p_new = z + beta p_old for its own rows and,
-// on the fly, for the neighbouring rows it reads, so one grid barrier per
-// iteration is saved.
+// The work of phase p on theta row i of one system: set-up and build
+// (p = 0), q = A p or the true residual (odd p), update and preconditioner
+// or restart (even p).  The warp's share of the row's dot products goes to
+// out[0..2] (lane 0); warps move on to their next row without a block
+// barrier (the preconditioner synchronises the block internally).
+template <bool MIXED, int PER>
+__device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
+                                          const SolverConfig& cfg, int i, int p, int state,
+                                          float beta, double alpha, float* pA, const float* pB,
+                                          float* sm, Ring& R, ff* out) {
+    ff a = ff_zero(), b2 = ff_zero(), c2 = ff_zero();
+    float rv[PER];
+    if (p == 0) {
+        row_init<MIXED, PER>(g, f, i, rv, c2);
+        precondition_row<MIXED, PER, true>(g, f, cfg, i, sm, R, rv, a, b2);
+    } else if (p & 1) {
+        if (state == ST_ITER) a = row_spmv<MIXED, PER>(g, f, i, beta, pB, pA);
+        else if (MIXED) a = row_true_residual<PER>(g, f, i);
+    } else {
+        if (state == ST_ITER) row_update<MIXED, PER>(g, f, i, alpha, pA, rv);
+        else row_load_r<PER>(g, f, i, rv);
+        precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, R, rv, a, b2);
+    }
+    a = ff_warp_sum(a);
+    b2 = ff_warp_sum(b2);
+    c2 = ff_warp_sum(c2);
+    if ((threadIdx.x & 31) == 0) {
+        out[0] = a;
+        out[1] = b2;
+        out[2] = c2;
+    }
+}
+
+// The solve of a set of systems: phase 0 sets up and builds the
+// preconditioner; odd phases form q = A p (or the true residual); even
+// phases update the iterate and apply the preconditioner (or restart).  In
+// every phase the rows of the systems still iterating are split into G
+// contiguous ranges of equal work weight, one per block, so a block meets
+// one or two systems per phase and a system that iterates longer than the
+// others still spreads over the whole GPU.  Each block counts the rows it
+// finished per system; the block that completes a system sums its row
+// partials and advances it.  The loop ends when no system is left.
 template <bool MIXED, int PER>
 __global__ void __launch_bounds__(kSolveBlock, 4)
-k_pcg(SbGrid g, SbFields f, SolverConfig cfg) {
-    extern __shared__ float sm[];
+k_solve(SbSolveSet S, SolverConfig cfg) {
+    extern __shared__ __align__(16) float sm[];
+    __shared__ __align__(8) uint64_t bars[kMaxRing];
+    __shared__ __align__(16) SbBubbleDesc s_d;
+    __shared__ unsigned s_pre[kMaxSystems + 1];
+    __shared__ ff s_part[kRowChunk][kWarps][3];
+    __shared__ int s_last;
+    int staged = -1;  // system whose descriptor is in s_d
     cg::grid_group grid = cg::this_grid();
-    const int G = gridDim.x;
-    const int nP = g.nP, nT = g.nT;
-    double* partA = f.partials;
-    double* partB = f.partials + 3 * G;
+    Ring R;
+    ring_init(R, bars, sm, cfg.ring);
+    const unsigned G = gridDim.x;
+    const int warp = threadIdx.x >> 5;
 
-    // dx = 0, r = r0, z = M^-1 r (p_old = 0, beta = 0)
-    double rz = 0, rr = 0, bb = 0;
-    {
-        double a = 0, b2 = 0, c2 = 0;
-        for (int i = blockIdx.x; i < nT; i += G) {
-            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                const int c = i * nP + j;
-                if (MIXED) f.x64[c] = 0.0;
-                else f.dx[c] = 0.0f;
-                f.r[c] = f.r0[c];
-                f.q[c] = 0.0f;  // p_old
-                const double b = (double)f.rhs[c];
-                c2 += b * b;
+    for (int p = 0;; ++p) {
+        const unsigned W = active_prefix(S, p, s_pre);
+        if (W == 0) break;  // same in every block
+        const unsigned lo = (unsigned)(((unsigned long long)W * blockIdx.x) / G);
+        const unsigned hi = (unsigned)(((unsigned long long)W * (blockIdx.x + 1)) / G);
+        for (int b = first_system_after(s_pre, S.nb, lo); b < S.nb && s_pre[b] < hi; ++b) {
+            const unsigned w0 = s_pre[b];
+            if (s_pre[b + 1] == w0) continue;  // not active
+            const int nT = S.roff[b + 1] - S.roff[b];
+            const unsigned wr = row_weight(nT);
+            // rows whose start weight w0 + i wr lies in [lo, hi)
+            const int i0 = lo > w0 ? (int)((lo - w0 + wr - 1) / wr) : 0;
+            const int i1 = min(nT, (int)((hi - w0 + wr - 1) / wr));
+            if (i0 >= i1) continue;
+            // the system's scalars, loaded while the descriptor is staged
+            int state = ST_ITER, it = 0;
+            float beta = 0.0f;
+            double alpha = 0.0;
+            if (p > 0) {
+                const SbSolveRec* rp = S.rec + (p & 1) * S.nb + b;
+                state = __ldcg(&rp->state);
+                it = __ldcg(&rp->it);
+                beta = __ldcg(&rp->beta);
+                alpha = __ldcg(&rp->alpha);
             }
-            __syncthreads();
-            precondition_row<MIXED, PER, true>(g, f, cfg, i, sm, a, b2);
-        }
-        block_partial3(a, b2, c2, partA);
-    }
-    grid.sync();
-    all_sum3(partA, G, rz, rr, bb);
-    const double bnorm = bb > 0.0 ? sqrt(bb) : 1.0;
-    // the FP64 iterate is driven to 0.8 tol so that the returned FP32 gamma
-    // (whose rounding adds up to a few percent) still meets tol
-    const double tol2 = (MIXED ? 0.64 : 1.0) * cfg.tol * cfg.tol * bnorm * bnorm;
-    float* pold = f.q;
-    float* pnew = f.p;
-    float beta = 0.0f;
-    int it = 0;
-    bool conv = false;
-    while (it < cfg.max_iter) {
-        if (!(rr == rr)) break;  // NaN: give up (same decision in every block)
-        if (rr <= tol2) {
-            if (!MIXED) { conv = true; break; }
-            // true FP64 residual of the refined iterate
-            double a = 0;
-            for (int i = blockIdx.x; i < nT; i += G)
-                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                    const int c = i * nP + j;
-                    const double r = (double)f.r0[c] - apply_A<double, double>(g, f, f.x64, c, i, j);
-                    f.r[c] = (float)r;
-                    a += r * r;
-                }
-            block_partial3(a, 0.0, 0.0, partB);
-            grid.sync();
-            double d1, d2;
-            all_sum3(partB, G, rr, d1, d2);
-            if (rr <= tol2) { conv = true; break; }
-            // restart CG from the refined iterate
-            double a2 = 0, b2 = 0;
-            for (int i = blockIdx.x; i < nT; i += G) {
-                precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, a2, b2);
+            if (b != staged) {
+                stage_desc(S, b, &s_d);  // constant during the solve
+                staged = b;
             }
-            block_partial3(a2, b2, 0.0, partA);
-            grid.sync();
-            all_sum3(partA, G, rz, rr, d1);
-            beta = 0.0f;
-        }
-        // p_new = z + beta p_old; q = A p_new; <p_new, q>
-        {
-            double pq = 0;
-            for (int i = blockIdx.x; i < nT; i += G)
-                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                    const int c = i * nP + j;
-                    const int e = i * nP + ((j + 1) & g.maskP);
-                    const int w = i * nP + ((j - 1) & g.maskP);
-                    const float pc = f.z[c] + beta * pold[c];
-                    pnew[c] = pc;
-                    float qf = f.dmass[c] * pc + f.cE[c] * (pc - (f.z[e] + beta * pold[e])) +
-                               f.cE[w] * (pc - (f.z[w] + beta * pold[w]));
-                    if (i < nT - 1) {
-                        const int sc = c + nP;
-                        qf += f.cS[c] * (pc - (f.z[sc] + beta * pold[sc]));
-                    }
-                    if (i > 0) {
-                        const int nc = c - nP;
-                        qf += f.cS[nc] * (pc - (f.z[nc] + beta * pold[nc]));
-                    }
-                    f.x[c] = qf;  // q lives in x until the final phase
-                    pq += MIXED ? (double)pc * (double)qf : (double)(pc * qf);
-                }
-            block_partial3(pq, 0.0, 0.0, partA);
+            const SbGrid& g = s_d.g;
+            const SbFields& f = s_d.f;
+            float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
+            float* pB = (it & 1) ? f.p : f.q;  // p_old
+            bool last = false;
+            for (int i = i0; i < i1; ++i) {
+                const int k = (i - i0) % kRowChunk;
+                row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, sm, R,
+                                      s_part[k][warp]);
+                // publish and count every kRowChunk rows and at the end; the
+                // block that completes the system advances it
+                if (k == kRowChunk - 1 || i == i1 - 1)
+                    last = publish_rows(S, b, nT, i - k, k + 1, p & 1, true, s_part, &s_last);
+            }
+            if (last) {
+                double A, B, C;
+                system_sum3(S, b, nT, p & 1, A, B, C);
+                if (threadIdx.x == 0) advance<MIXED>(S, b, p, A, B, C, cfg);
+            }
+            __syncthreads();  // s_d and s_last are reused
         }
         grid.sync();
-        double pq, d1, d2;
-        all_sum3(partA, G, pq, d1, d2);
-        if (!(pq > 0.0)) break;
-        const double alpha = rz / pq;
-        const float af = (float)alpha;
-        double rz2 = 0, rr2 = 0;
-        for (int i = blockIdx.x; i < nT; i += G) {
-            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                const int c = i * nP + j;
-                const float pc = pnew[c];
-                if (MIXED) f.x64[c] += alpha * (double)pc;
-                else f.dx[c] += af * pc;
-                f.r[c] = f.r[c] - af * f.x[c];
-            }
-            __syncthreads();
-            precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, rz2, rr2);
-        }
-        block_partial3(rz2, rr2, 0.0, partB);
-        grid.sync();
-        all_sum3(partB, G, rz2, rr2, d1);
-        beta = (float)(rz2 / rz);
-        rz = rz2;
-        rr = rr2;
-        float* t = pold;
-        pold = pnew;
-        pnew = t;
-        ++it;
     }
-    // final increment and new gamma.  The reported residual is the FP64
-    // residual of the refined iterate checked above (mixed mode; it is held
-    // to 0.8 tol so that the FP32-rounded gamma also meets tol) or the
-    // recursive residual (plain mode).
-    for (int i = blockIdx.x; i < nT; i += G)
-        for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-            const int c = i * nP + j;
-            const float dx = MIXED ? (float)f.x64[c] : f.dx[c];
-            const float g0 = f.gam_adv[c];
-            f.dx[c] = dx;
-            f.x[c] = g0 + dx;
-        }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        f.stats->solver_iters = it;
-        f.stats->solver_rel_resid = sqrt(rr) / bnorm;
-        f.stats->solver_b_norm = bnorm;
-        f.stats->solver_converged = conv ? 1 : 0;
+    // the increment and the new gamma of every system, same split with all
+    // systems counted
+    const unsigned W = active_prefix(S, -1, s_pre);
+    const unsigned lo = (unsigned)(((unsigned long long)W * blockIdx.x) / G);
+    const unsigned hi = (unsigned)(((unsigned long long)W * (blockIdx.x + 1)) / G);
+    for (int b = first_system_after(s_pre, S.nb, lo); b < S.nb && s_pre[b] < hi; ++b) {
+        const unsigned w0 = s_pre[b];
+        const int nT = S.roff[b + 1] - S.roff[b];
+        const unsigned wr = row_weight(nT);
+        const int i0 = lo > w0 ? (int)((lo - w0 + wr - 1) / wr) : 0;
+        const int i1 = min(nT, (int)((hi - w0 + wr - 1) / wr));
+        if (i0 >= i1) continue;
+        stage_desc(S, b, &s_d);
+        for (int i = i0; i < i1; ++i) row_final<MIXED, PER>(s_d.g, s_d.f, i);
+        __syncthreads();
     }
 }
 
-// Sum of the partials of blocks [first, first + nblk), same order in every
-// block of that range.
-__device__ __forceinline__ void range_sum3(const double* part, int first, int nblk, double& A,
-                                           double& B, double& C) {
-    __shared__ double res[3];
-    if (threadIdx.x < 32) {
-        double x = 0.0, y = 0.0, z = 0.0;
-        for (int k = threadIdx.x; k < nblk; k += 32) {
-            x += part[3 * (first + k) + 0];
-            y += part[3 * (first + k) + 1];
-            z += part[3 * (first + k) + 2];
-        }
-        x = warp_sum(x); y = warp_sum(y); z = warp_sum(z);
-        if (threadIdx.x == 0) { res[0] = x; res[1] = y; res[2] = z; }
-    }
-    __syncthreads();
-    A = res[0]; B = res[1]; C = res[2];
-    __syncthreads();
-}
-
-// Batched PCG: k_pcg for every bubble of a batch in one cooperative launch.
-// Block k works on bubble blk_bubble[k]; a bubble's blocks are a contiguous
-// range and reduce only their own partials, in the same order as k_pcg, so
-// a bubble that gets as many blocks as its own k_pcg launch would have
-// produces bit-identical results.  The loop runs in slots of two grid
-// barriers; in each slot a bubble either does one CG iteration (ITER), or
-// the mixed-precision true-residual check followed by the restart (CHECK),
-// or nothing (DONE).  These are the branches of k_pcg's loop in the same
-// order.  The number of bubbles not yet done is counted on rotating
-// counters one barrier ahead of its use, so every block agrees on when to
-// stop without an extra barrier.
+// The solve of one system (a bubble stepped alone): the same phases, row
+// work and scalar transitions as k_solve, with the bubble's descriptor in
+// kernel parameters.  Rows are dealt round robin.  After every barrier each
+// block advances the scalars itself from the previous phase's row partials,
+// summed in row order like the publishing block of k_solve does, so no
+// block waits for another; row partials alternate between two buffers by
+// phase parity.  The results are bit-identical to solving the same system
+// inside a set (this file is compiled without multiply-add contraction, so
+// both kernels round the same operations the same way).
 template <bool MIXED, int PER>
 __global__ void __launch_bounds__(kSolveBlock, 4)
-k_pcg_batch(SbBatchSolve bs, SolverConfig cfg) {
-    enum { ITER = 0, CHECK = 1, DONE = 2 };
-    extern __shared__ float sm[];
+k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
+    extern __shared__ __align__(16) float sm[];
+    __shared__ __align__(8) uint64_t bars[kMaxRing];
+    __shared__ ff s_part[kRowChunk][kWarps][3];
     cg::grid_group grid = cg::this_grid();
-    const int G = gridDim.x;
-    const int bub = bs.blk_bubble[blockIdx.x];
-    const int first = bs.bub_first_blk[bub], nblk = bs.bub_nblk[bub];
-    const int lb = blockIdx.x - first;
-    const SbBubbleDesc& d = bs.descs[bub];
-    const SbGrid& g = d.g;
-    const SbFields& f = d.f;
-    const int nP = g.nP, nT = g.nT;
-    double* partA = bs.partials;
-    double* partB = bs.partials + 3 * G;
-    const bool lead = (lb == 0 && threadIdx.x == 0);
-    if (blockIdx.x == 0 && threadIdx.x < 3) bs.nactive[threadIdx.x] = 0;
-
-    // dx = 0, r = r0, z = M^-1 r (p_old = 0, beta = 0)
-    double rz = 0, rr = 0, bb = 0;
-    {
-        double a = 0, b2 = 0, c2 = 0;
-        for (int i = lb; i < nT; i += nblk) {
-            for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                const int c = i * nP + j;
-                if (MIXED) f.x64[c] = 0.0;
-                else f.dx[c] = 0.0f;
-                f.r[c] = f.r0[c];
-                f.q[c] = 0.0f;  // p_old
-                const double bv = (double)f.rhs[c];
-                c2 += bv * bv;
+    Ring R;
+    ring_init(R, bars, sm, cfg.ring);
+    __shared__ SbSolveRec s_rc;  // the system's scalars (the same in every block)
+    __shared__ int s_done;
+    const int G = gridDim.x, nT = g.nT;
+    const int warp = threadIdx.x >> 5;
+    for (int p = 0;; ++p) {
+        if (p > 0) {
+            double A, B, C;
+            system_sum3(S, 0, nT, (p - 1) & 1, A, B, C);
+            if (threadIdx.x == 0) {
+                s_done = transition<MIXED>(s_rc, p - 1, A, B, C, cfg) ? 1 : 0;
+                if (s_done && blockIdx.x == 0) write_stats(f.stats, s_rc);
             }
             __syncthreads();
-            precondition_row<MIXED, PER, true>(g, f, cfg, i, sm, a, b2);
+            if (s_done) break;  // same decision in every block
         }
-        block_partial3(a, b2, c2, partA);
-    }
-    grid.sync();
-    range_sum3(partA, first, nblk, rz, rr, bb);
-    const double bnorm = bb > 0.0 ? sqrt(bb) : 1.0;
-    const double tol2 = (MIXED ? 0.64 : 1.0) * cfg.tol * cfg.tol * bnorm * bnorm;
-    float* pold = f.q;
-    float* pnew = f.p;
-    float beta = 0.0f;
-    int it = 0;
-    bool conv = false;
-    // the loop head of k_pcg: iteration limit, NaN, target reached
-    auto next_state = [&]() -> int {
-        if (it >= cfg.max_iter || !(rr == rr)) return DONE;
-        if (rr <= tol2) {
-            if (!MIXED) { conv = true; return DONE; }
-            return CHECK;
-        }
-        return ITER;
-    };
-    int state = next_state();
-    if (state != DONE && lead) atomicAdd(&bs.nactive[0], 1);
-    for (int k = 0;; ++k) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) bs.nactive[(k + 2) % 3] = 0;
-        // first half: q = A p_new (ITER) or the true residual (CHECK)
-        double s1 = 0;
-        if (state == ITER) {
-            for (int i = lb; i < nT; i += nblk)
-                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                    const int c = i * nP + j;
-                    const int e = i * nP + ((j + 1) & g.maskP);
-                    const int w = i * nP + ((j - 1) & g.maskP);
-                    const float pc = f.z[c] + beta * pold[c];
-                    pnew[c] = pc;
-                    float qf = f.dmass[c] * pc + f.cE[c] * (pc - (f.z[e] + beta * pold[e])) +
-                               f.cE[w] * (pc - (f.z[w] + beta * pold[w]));
-                    if (i < nT - 1) {
-                        const int sc = c + nP;
-                        qf += f.cS[c] * (pc - (f.z[sc] + beta * pold[sc]));
+        const int state = s_rc.state, it = s_rc.it;
+        const float beta = s_rc.beta;
+        const double alpha = s_rc.alpha;
+        float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
+        float* pB = (it & 1) ? f.p : f.q;  // p_old
+        int k = 0, first = blockIdx.x;
+        for (int i = blockIdx.x; i < nT; i += G) {
+            row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, sm, R,
+                                  s_part[k][warp]);
+            ++k;
+            if (k == kRowChunk || i + G >= nT) {
+                // fold and publish the chunk's rows first, first + G, ...
+                __syncthreads();
+                if (threadIdx.x < k) {
+                    ff x = ff_zero(), y = ff_zero(), z = ff_zero();
+#pragma unroll
+                    for (int w = 0; w < kWarps; ++w) {
+                        x = ff_add(x, s_part[threadIdx.x][w][0]);
+                        y = ff_add(y, s_part[threadIdx.x][w][1]);
+                        z = ff_add(z, s_part[threadIdx.x][w][2]);
                     }
-                    if (i > 0) {
-                        const int nc = c - nP;
-                        qf += f.cS[nc] * (pc - (f.z[nc] + beta * pold[nc]));
-                    }
-                    f.x[c] = qf;  // q lives in x until the final phase
-                    s1 += MIXED ? (double)pc * (double)qf : (double)(pc * qf);
+                    float2* o = S.rowpart + 3 * ((size_t)(p & 1) * S.R + first + threadIdx.x * G);
+                    o[0] = make_float2(x.hi, x.lo);
+                    o[1] = make_float2(y.hi, y.lo);
+                    o[2] = make_float2(z.hi, z.lo);
                 }
-        } else if (MIXED && state == CHECK) {
-            for (int i = lb; i < nT; i += nblk)
-                for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                    const int c = i * nP + j;
-                    const double r = (double)f.r0[c] - apply_A<double, double>(g, f, f.x64, c, i, j);
-                    f.r[c] = (float)r;
-                    s1 += r * r;
-                }
-        }
-        block_partial3(s1, 0.0, 0.0, partA);
-        grid.sync();
-        if (bs.nactive[k % 3] == 0) break;  // same value in every block
-        double r1, d1, d2;
-        range_sum3(partA, first, nblk, r1, d1, d2);
-        // second half: update and precondition (ITER) or restart (CHECK)
-        double rz2 = 0, rr2 = 0;
-        if (state == ITER) {
-            if (!(r1 > 0.0)) {
-                state = DONE;  // breakdown: keep the current iterate
-            } else {
-                const double alpha = rz / r1;
-                const float af = (float)alpha;
-                for (int i = lb; i < nT; i += nblk) {
-                    for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-                        const int c = i * nP + j;
-                        const float pc = pnew[c];
-                        if (MIXED) f.x64[c] += alpha * (double)pc;
-                        else f.dx[c] += af * pc;
-                        f.r[c] = f.r[c] - af * f.x[c];
-                    }
-                    __syncthreads();
-                    precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, rz2, rr2);
-                }
-            }
-        } else if (state == CHECK) {
-            rr = r1;
-            if (rr <= tol2) {
-                conv = true;
-                state = DONE;
-            } else {
-                for (int i = lb; i < nT; i += nblk)
-                    precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, rz2, rr2);
+                __syncthreads();
+                k = 0;
+                first = i + G;
             }
         }
-        block_partial3(rz2, rr2, 0.0, partB);
         grid.sync();
-        double d3;
-        range_sum3(partB, first, nblk, rz2, rr2, d3);
-        if (state == ITER) {
-            beta = (float)(rz2 / rz);
-            rz = rz2;
-            rr = rr2;
-            float* t = pold;
-            pold = pnew;
-            pnew = t;
-            ++it;
-            state = next_state();
-        } else if (state == CHECK) {
-            // restarted from the refined iterate: the next slot iterates
-            rz = rz2;
-            rr = rr2;
-            beta = 0.0f;
-            state = ITER;
-        }
-        if (state != DONE && lead) atomicAdd(&bs.nactive[(k + 1) % 3], 1);
     }
-    // final increment and new gamma, as k_pcg
-    for (int i = lb; i < nT; i += nblk)
-        for (int j = threadIdx.x; j < nP; j += blockDim.x) {
-            const int c = i * nP + j;
-            const float dx = MIXED ? (float)f.x64[c] : f.dx[c];
-            const float g0 = f.gam_adv[c];
-            f.dx[c] = dx;
-            f.x[c] = g0 + dx;
-        }
-    if (lead) {
-        f.stats->solver_iters = it;
-        f.stats->solver_rel_resid = sqrt(rr) / bnorm;
-        f.stats->solver_b_norm = bnorm;
-        f.stats->solver_converged = conv ? 1 : 0;
+    for (int i = blockIdx.x; i < nT; i += G) row_final<MIXED, PER>(g, f, i);
+}
+
+template <bool MIXED>
+const void* solve_one_kernel(int per) {
+    switch (per) {
+        case 1: return (const void*)k_solve_one<MIXED, 1>;
+        case 2: return (const void*)k_solve_one<MIXED, 2>;
+        case 4: return (const void*)k_solve_one<MIXED, 4>;
+        default: return (const void*)k_solve_one<MIXED, 8>;
     }
 }
 
 template <bool MIXED>
-const void* pcg_batch_kernel(int per) {
+const void* solve_kernel(int per) {
     switch (per) {
-        case 1: return (const void*)k_pcg_batch<MIXED, 1>;
-        case 2: return (const void*)k_pcg_batch<MIXED, 2>;
-        case 4: return (const void*)k_pcg_batch<MIXED, 4>;
-        default: return (const void*)k_pcg_batch<MIXED, 8>;
-    }
-}
-
-template <bool MIXED>
-const void* pcg_kernel(int per) {
-    switch (per) {
-        case 1: return (const void*)k_pcg<MIXED, 1>;
-        case 2: return (const void*)k_pcg<MIXED, 2>;
-        case 4: return (const void*)k_pcg<MIXED, 4>;
-        default: return (const void*)k_pcg<MIXED, 8>;
+        case 1: return (const void*)k_solve<MIXED, 1>;
+        case 2: return (const void*)k_solve<MIXED, 2>;
+        case 4: return (const void*)k_solve<MIXED, 4>;
+        default: return (const void*)k_solve<MIXED, 8>;
     }
 }
 
@@ -644,87 +943,97 @@ int per_of(int nP) {
     return per <= 1 ? 1 : per <= 2 ? 2 : per <= 4 ? 4 : 8;
 }
 
-struct Occ {
-    int sms = 0;
-    int blocks = 0;
-    int nP = -1;
-};
+// Shared memory of one solve block: the factor ring (K slices of nP
+// float2) plus two nP-float buffers, or the four nP-float arrays of the
+// preconditioner build, whichever is larger.  K is as deep as fits while
+// four 256-thread blocks share an SM (228 KB: up to about 46 KB dynamic each
+// next to ~8 KB of static shared memory), at least 2 and at most the
+// log2(nP) slices a row can have.
+constexpr int kSolveSmemBudget = 46 * 1024;
 
-int solve_blocks(const SbGrid& g) {
-    static Occ cache[16];
+int ring_depth(int nP) {
+    int lg = 0;
+    while ((1 << lg) < nP) ++lg;
+    const int K = (kSolveSmemBudget - 8 * nP) / (8 * nP);
+    return std::max(2, std::min(K, std::min(lg, kMaxRing)));
+}
+
+size_t solve_smem(int nP) {
+    const int K = ring_depth(nP);
+    return std::max<size_t>(16 * (size_t)nP, 8 * (size_t)K * nP + 8 * (size_t)nP);
+}
+
+const void* kernel_for(int per, int mode, bool one) {
+    if (one) return mode == 1 ? solve_one_kernel<true>(per) : solve_one_kernel<false>(per);
+    return mode == 1 ? solve_kernel<true>(per) : solve_kernel<false>(per);
+}
+
+// Largest dynamic shared memory of a kernel variant (PER columns per thread
+// serve rows of up to PER * 256 columns; smaller rows need less).
+size_t variant_smem(int per) {
+    size_t m = 0;
+    for (int nP = 16; nP <= per * kSolveBlock; nP *= 2)
+        if (per_of(nP) == per) m = std::max(m, solve_smem(nP));
+    return m;
+}
+
+// Co-resident blocks of a kernel variant (cached per device).  The first
+// query also declares the variant's largest dynamic shared memory (the 48 KB
+// default limit counts static shared memory too, and a launch above the
+// declared size is refused).
+int max_blocks(int per, int mode, bool one) {
+    static int cache[16][4][2][2];
     int dev = 0;
     cudaGetDevice(&dev);
-    Occ& o = cache[dev & 15];
-    if (o.nP != g.nP) {
-        cudaDeviceGetAttribute(&o.sms, cudaDevAttrMultiProcessorCount, dev);
-        const size_t smem = 4 * sizeof(float) * (size_t)g.nP;
-        const int per = per_of(g.nP);
-        int a = 0, b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, pcg_kernel<false>(per), kSolveBlock, smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pcg_kernel<true>(per), kSolveBlock, smem);
-        o.blocks = o.sms * (a < b ? a : b);
-        o.nP = g.nP;
-    }
-    const int b = o.blocks > 0 ? o.blocks : 1;
-    return g.nT < b ? g.nT : b;
+    const int pi = per == 1 ? 0 : per == 2 ? 1 : per == 4 ? 2 : 3;
+    int& c = cache[dev & 15][pi][mode & 1][one ? 1 : 0];
+    if (c > 0) return c;
+    const void* fn = kernel_for(per, mode, one);
+    const size_t smem = variant_smem(per);
+    int sms = 0, occ = 0;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolveBlock, smem);
+    c = sms * (occ > 0 ? occ : 1);
+    return c;
 }
 
 }  // namespace
 
-int solver_partials_needed(const SbGrid& g) { return 6 * solve_blocks(g); }
-
-cudaError_t prepare_solve_batch(int maxNP, const SolverConfig& cfg, int* blocks) {
+cudaError_t prepare_solve(int maxNP, const SolverConfig& cfg, int* blocks) {
     if (maxNP > 8 * kSolveBlock) return cudaErrorInvalidValue;
-    const size_t smem = 4 * sizeof(float) * (size_t)maxNP;
-    const int per = per_of(maxNP);
-    const void* fn = cfg.mode == 1 ? pcg_batch_kernel<true>(per) : pcg_batch_kernel<false>(per);
-    cudaError_t e = cudaSuccess;
-    if (smem > 48 * 1024)
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0, occ = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolveBlock, smem);
-    *blocks = sms * (occ > 0 ? occ : 1);
-    return e;
+    const int b = max_blocks(per_of(maxNP), cfg.mode, false);
+    max_blocks(per_of(maxNP), cfg.mode, true);
+    if (blocks) *blocks = b;
+    return cudaGetLastError();
 }
 
-cudaError_t launch_solve_batch(const SbBatchSolve& bs, int G, int maxNP, const SolverConfig& cfg,
-                               cudaStream_t s) {
-    const size_t smem = 4 * sizeof(float) * (size_t)maxNP;
-    SbBatchSolve bb = bs;
-    SolverConfig cc = cfg;
-    void* args[] = {&bb, &cc};
-    const int per = per_of(maxNP);
-    const void* fn = cfg.mode == 1 ? pcg_batch_kernel<true>(per) : pcg_batch_kernel<false>(per);
-    return cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kSolveBlock), args, smem, s);
-}
-
-cudaError_t prepare_solve(const SbGrid& g, const SolverConfig& cfg) {
-    if (g.nP > 8 * kSolveBlock) return cudaErrorInvalidValue;
-    solve_blocks(g);
-    const size_t smem = 4 * sizeof(float) * (size_t)g.nP;
+cudaError_t launch_solve_one(const SbGrid& g, const SbFields& f, const SbSolveSet& set,
+                             const SolverConfig& cfg, cudaStream_t s) {
+    if (g.nP > 8 * kSolveBlock || set.nb != 1) return cudaErrorInvalidValue;
     const int per = per_of(g.nP);
-    const void* fn = cfg.mode == 1 ? pcg_kernel<true>(per) : pcg_kernel<false>(per);
-    if (smem > 48 * 1024)
-        return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return cudaSuccess;
-}
-
-cudaError_t launch_solve(const SbGrid& g, const SbPhys& ph, const SbFields& f,
-                         const SolverConfig& cfg, cudaStream_t s) {
-    (void)ph;
-    if (g.nP > 8 * kSolveBlock) return cudaErrorInvalidValue;
-    const int G = solve_blocks(g);
-    const size_t smem = 4 * sizeof(float) * (size_t)g.nP;
+    const int G = std::min(g.nT, max_blocks(per, cfg.mode, true));
     SbGrid gg = g;
     SbFields ff = f;
+    SbSolveSet ss = set;
     SolverConfig cc = cfg;
-    void* args[] = {&gg, &ff, &cc};
-    const int per = per_of(g.nP);
-    const void* fn = cfg.mode == 1 ? pcg_kernel<true>(per) : pcg_kernel<false>(per);
-    return cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kSolveBlock), args, smem, s);
+    cc.ring = ring_depth(g.nP);
+    void* args[] = {&gg, &ff, &ss, &cc};
+    return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, true), dim3(G), dim3(kSolveBlock),
+                                       args, solve_smem(g.nP), s);
+}
+
+cudaError_t launch_solve(const SbSolveSet& set, int maxNP, const SolverConfig& cfg,
+                         cudaStream_t s) {
+    if (maxNP > 8 * kSolveBlock || set.R <= 0) return cudaErrorInvalidValue;
+    const int per = per_of(maxNP);
+    const int G = std::min(set.R, max_blocks(per, cfg.mode, false));
+    SbSolveSet ss = set;
+    SolverConfig cc = cfg;
+    cc.ring = ring_depth(maxNP);
+    void* args[] = {&ss, &cc};
+    return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, false), dim3(G), dim3(kSolveBlock),
+                                       args, solve_smem(maxNP), s);
 }
 
 }  // namespace sb

@@ -425,38 +425,44 @@ __device__ __forceinline__ void block_max_distortion(float dist, SbDevStats* st)
 }
 
 // ---------------------------------------------------------------------------
-// Kernels: one bubble (parameters by value), or a batch of bubbles (one
-// descriptor per bubble, one 128..256-cell tile per block; a tile never
-// straddles two bubbles).
-#define SB_CELL_KERNELS(name)                                                          \
-    __global__ void __launch_bounds__(256) k_##name(SbGrid g, SbPhys ph, SbFields f, int cur) { \
-        const int idx = blockIdx.x * blockDim.x + threadIdx.x;                        \
-        if (idx < g.N) name##_cell(g, ph, f, cur, idx);                               \
-    }                                                                                  \
-    __global__ void __launch_bounds__(256) kb_##name(const SbBubbleDesc* __restrict__ descs, \
-                                                     const int2* __restrict__ tiles) {\
+// Kernels.  A launch covers a set of bubbles (one bubble, or every bubble of
+// a batch): descs[k] points to bubble k's descriptor, and block b works on
+// the cells tiles[b] = (bubble, first cell) .. + blockDim.x - 1 (a tile never
+// straddles two bubbles).  One bubble stepped alone and inside a batch runs
+// the same kernels on the same descriptor.
+// The block's bubble descriptor is copied to shared memory first, so the
+// cell code reads grid constants and array pointers from there.
+__device__ __forceinline__ const SbBubbleDesc& stage_tile_desc(SbBubbleDesc* const* descs, int b,
+                                                               SbBubbleDesc* s_d) {
+    constexpr int kWords = (int)(sizeof(SbBubbleDesc) / 4);
+    const int* src = reinterpret_cast<const int*>(descs[b]);
+    int* dst = reinterpret_cast<int*>(s_d);
+    for (int k = threadIdx.x; k < kWords; k += blockDim.x) dst[k] = src[k];
+    __syncthreads();
+    return *s_d;
+}
+
+#define SB_CELL_KERNEL(name)                                                           \
+    __global__ void __launch_bounds__(256) k_##name(SbBubbleDesc* const* __restrict__ descs, \
+                                                    const int2* __restrict__ tiles) {  \
+        __shared__ __align__(16) SbBubbleDesc s_d;                                     \
         const int2 t = tiles[blockIdx.x];                                              \
-        const SbBubbleDesc& d = descs[t.x];                                            \
+        const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);                     \
         const int idx = t.y + threadIdx.x;                                             \
         if (idx < d.g.N) name##_cell(d.g, d.ph, d.f, d.cur, idx);                     \
     }
 
-SB_CELL_KERNELS(advect_maps)
-SB_CELL_KERNELS(velocity)
-SB_CELL_KERNELS(bimocq)
-SB_CELL_KERNELS(assemble)
-SB_CELL_KERNELS(post)
+SB_CELL_KERNEL(advect_maps)
+SB_CELL_KERNEL(velocity)
+SB_CELL_KERNEL(bimocq)
+SB_CELL_KERNEL(assemble)
+SB_CELL_KERNEL(post)
 
-__global__ void __launch_bounds__(256) k_accum(SbGrid g, SbPhys ph, SbFields f, int cur) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    const float dist = idx < g.N ? accum_cell(g, ph, f, cur, idx) : 0.0f;
-    block_max_distortion(dist, f.stats);
-}
-
-__global__ void __launch_bounds__(256) kb_accum(const SbBubbleDesc* __restrict__ descs,
-                                                const int2* __restrict__ tiles) {
+__global__ void __launch_bounds__(256) k_accum(SbBubbleDesc* const* __restrict__ descs,
+                                               const int2* __restrict__ tiles) {
+    __shared__ __align__(16) SbBubbleDesc s_d;
     const int2 t = tiles[blockIdx.x];
-    const SbBubbleDesc& d = descs[t.x];
+    const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);
     const int idx = t.y + threadIdx.x;
     const float dist = idx < d.g.N ? accum_cell(d.g, d.ph, d.f, d.cur, idx) : 0.0f;
     block_max_distortion(dist, d.f.stats);
@@ -540,39 +546,20 @@ __device__ __forceinline__ void reinit_commit(const SbFields& f, int cur, int id
     f.bwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
 }
 
-// reInitializeMapping (kernel/bubble.cu:2509-2564) when the distortion
-// exceeds 4 cells (or when forced): one cooperative launch, three phases
-// separated by grid barriers.  Without a re-initialisation every block
-// returns at once (the decision is read from device memory, so no host
-// synchronisation is needed).
+// reInitializeMapping (kernel/bubble.cu:2509-2564) for every bubble of the
+// set whose distortion exceeds 4 cells (or that forces it): one cooperative
+// launch, three phases over the bubbles' tiles separated by grid barriers.
+// The decisions are read from device memory, so no host synchronisation is
+// needed; every block reads every bubble's decision, so all blocks agree on
+// whether any phase runs, and without a re-initialisation they return at
+// once.
 __global__ void __launch_bounds__(kBlock)
-k_reinit(SbGrid g, SbFields f, int cur) {
-    if (!reinit_now(f.stats)) return;  // same value in every block
-    cg::grid_group grid = cg::this_grid();
-    const int stride = gridDim.x * blockDim.x;
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t0 == 0) {
-        f.stats->reinit = 1;
-        f.stats->reinit_total += 1;
-    }
-    for (int idx = t0; idx < g.N; idx += stride) reinit_error(g, f, cur, idx);
-    grid.sync();
-    for (int idx = t0; idx < g.N; idx += stride) reinit_correct(g, f, cur, idx);
-    grid.sync();
-    for (int idx = t0; idx < g.N; idx += stride) reinit_commit(f, cur, idx);
-}
-
-// Batched re-initialisation: the bubbles whose distortion exceeds the
-// threshold are corrected in three grid-synchronised phases over their
-// tiles.  Every block reads every bubble's decision, so all blocks agree on
-// whether any phase runs.
-__global__ void __launch_bounds__(kBlock)
-kb_reinit(const SbBubbleDesc* __restrict__ descs, int nb, const int2* __restrict__ tiles,
-          int ntiles) {
+k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict__ tiles,
+         int ntiles) {
     __shared__ int any;
     if (threadIdx.x == 0) {
         int a = 0;
-        for (int b = 0; b < nb; ++b) a |= reinit_now(descs[b].f.stats) ? 1 : 0;
+        for (int b = 0; b < nb; ++b) a |= reinit_now(descs[b]->f.stats) ? 1 : 0;
         any = a;
     }
     __syncthreads();
@@ -580,7 +567,7 @@ kb_reinit(const SbBubbleDesc* __restrict__ descs, int nb, const int2* __restrict
     cg::grid_group grid = cg::this_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
-        const SbBubbleDesc& d = descs[tl.x];
+        const SbBubbleDesc& d = *descs[tl.x];
         if (!reinit_now(d.f.stats)) continue;
         for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x) {
             if (idx == 0) {
@@ -593,7 +580,7 @@ kb_reinit(const SbBubbleDesc* __restrict__ descs, int nb, const int2* __restrict
     grid.sync();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
-        const SbBubbleDesc& d = descs[tl.x];
+        const SbBubbleDesc& d = *descs[tl.x];
         if (!reinit_now(d.f.stats)) continue;
         for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
             reinit_correct(d.g, d.f, d.cur, idx);
@@ -601,16 +588,17 @@ kb_reinit(const SbBubbleDesc* __restrict__ descs, int nb, const int2* __restrict
     grid.sync();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
-        const SbBubbleDesc& d = descs[tl.x];
+        const SbBubbleDesc& d = *descs[tl.x];
         if (!reinit_now(d.f.stats)) continue;
         for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
             reinit_commit(d.f, d.cur, idx);
     }
 }
 
-__global__ void kb_flip(SbBubbleDesc* descs, int nb) {
+// End of a step: every bubble's map parity flips.
+__global__ void k_flip(SbBubbleDesc* const* descs, int nb) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nb) descs[b].cur ^= 1;
+    if (b < nb) descs[b]->cur ^= 1;
 }
 
 __global__ void k_reset_maps(SbGrid g, SbFields f) {
@@ -644,8 +632,6 @@ __global__ void k_mass(SbGrid g, SbFields f) {
     }
 }
 
-inline dim3 grid_for(const SbGrid& g) { return dim3((g.N + kBlock - 1) / kBlock); }
-
 // Co-resident grid of the cooperative re-initialisation kernel.
 int reinit_blocks() {
     static int cache[16] = {0};
@@ -663,22 +649,35 @@ int reinit_blocks() {
 
 }  // namespace
 
-cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbFields& f,
-                         const SolverConfig& cfg, int cur, cudaStream_t s) {
-    const dim3 grid = grid_for(g);
+const int kTileSizes[3] = {64, 128, 256};
+
+cudaError_t prepare_plan(const SbStepPlan& P) {
+    reinit_blocks();
+    return prepare_solve(P.maxNP, P.solver, nullptr);
+}
+
+cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s) {
+    const int k = P.sel[stage];
+    const int n = P.ntiles[k], block = kTileSizes[k];
+    SbBubbleDesc* const* d = P.descs;
+    const int2* t = P.tiles[k];
     switch (stage) {
-        case STAGE_MAPS: k_advect_maps<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
-        case STAGE_VELOCITY: k_velocity<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
-        case STAGE_BIMOCQ: k_bimocq<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
-        case STAGE_ASSEMBLE: k_assemble<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
-        case STAGE_SOLVE: return launch_solve(g, ph, f, cfg, s);
-        case STAGE_POST: k_post<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
-        case STAGE_ACCUM: k_accum<<<grid, kBlock, 0, s>>>(g, ph, f, cur); break;
+        case STAGE_MAPS: k_advect_maps<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_VELOCITY: k_velocity<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_BIMOCQ: k_bimocq<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_ASSEMBLE: k_assemble<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_SOLVE:
+            return P.one ? launch_solve_one(P.one->g, P.one->f, P.set, P.solver, s)
+                         : launch_solve(P.set, P.maxNP, P.solver, s);
+        case STAGE_POST: k_post<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_ACCUM: k_accum<<<n, block, 0, s>>>(d, t); break;
         case STAGE_REINIT: {
-            SbGrid gg = g;
-            SbFields ff = f;
-            int cc = cur;
-            void* args[] = {&gg, &ff, &cc};
+            // the re-initialisation works on kBlock-cell tiles
+            SbBubbleDesc* const* dd = P.descs;
+            int nb = P.nb;
+            const int2* tt = P.tiles[1];
+            int nt = P.ntiles[1];
+            void* args[] = {&dd, &nb, &tt, &nt};
             return cudaLaunchCooperativeKernel((const void*)k_reinit, dim3(reinit_blocks()),
                                                dim3(kBlock), args, 0, s);
         }
@@ -687,64 +686,28 @@ cudaError_t launch_stage(int stage, const SbGrid& g, const SbPhys& ph, const SbF
     return cudaGetLastError();
 }
 
-cudaError_t prepare_launches(const SbGrid& g, const SolverConfig& cfg) {
-    reinit_blocks();
-    return prepare_solve(g, cfg);
-}
-
-cudaError_t launch_stage_batch(int stage, const SbBubbleDesc* descs, const int2* tiles, int ntiles,
-                               int block, cudaStream_t s) {
-    switch (stage) {
-        case STAGE_MAPS: kb_advect_maps<<<ntiles, block, 0, s>>>(descs, tiles); break;
-        case STAGE_VELOCITY: kb_velocity<<<ntiles, block, 0, s>>>(descs, tiles); break;
-        case STAGE_BIMOCQ: kb_bimocq<<<ntiles, block, 0, s>>>(descs, tiles); break;
-        case STAGE_ASSEMBLE: kb_assemble<<<ntiles, block, 0, s>>>(descs, tiles); break;
-        case STAGE_POST: kb_post<<<ntiles, block, 0, s>>>(descs, tiles); break;
-        case STAGE_ACCUM: kb_accum<<<ntiles, block, 0, s>>>(descs, tiles); break;
-        default: return cudaErrorInvalidValue;
-    }
+cudaError_t launch_plan_flip(const SbStepPlan& P, cudaStream_t s) {
+    k_flip<<<(P.nb + 127) / 128, 128, 0, s>>>(P.descs, P.nb);
     return cudaGetLastError();
 }
 
-int reinit_batch_blocks() {
-    static int cache[16] = {0};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int& b = cache[dev & 15];
-    if (b == 0) {
-        int sms = 0, per = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_reinit, kBlock, 0);
-        b = sms * (per > 0 ? per : 1);
+cudaError_t launch_plan_step(const SbStepPlan& P, cudaStream_t s) {
+    for (int st = 0; st < STAGE_COUNT; ++st) {
+        cudaError_t e = launch_plan_stage(P, st, s);
+        if (e != cudaSuccess) return e;
     }
-    return b;
-}
-
-cudaError_t launch_reinit_batch(const SbBubbleDesc* descs, int nb, const int2* tiles, int ntiles,
-                                cudaStream_t s) {
-    const SbBubbleDesc* dd = descs;
-    int nn = nb;
-    const int2* tt = tiles;
-    int nt = ntiles;
-    void* args[] = {&dd, &nn, &tt, &nt};
-    return cudaLaunchCooperativeKernel((const void*)kb_reinit, dim3(reinit_batch_blocks()),
-                                       dim3(kBlock), args, 0, s);
-}
-
-cudaError_t launch_flip_batch(SbBubbleDesc* descs, int nb, cudaStream_t s) {
-    kb_flip<<<(nb + 127) / 128, 128, 0, s>>>(descs, nb);
-    return cudaGetLastError();
+    return launch_plan_flip(P, s);
 }
 
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s) {
-    k_reset_maps<<<grid_for(g), kBlock, 0, s>>>(g, f);
+    k_reset_maps<<<(g.N + kBlock - 1) / kBlock, kBlock, 0, s>>>(g, f);
     return cudaGetLastError();
 }
 
 cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(&f.stats->mass_eta, 0, 2 * sizeof(double), s);
     if (e != cudaSuccess) return e;
-    k_mass<<<grid_for(g), kBlock, 0, s>>>(g, f);
+    k_mass<<<(g.N + kBlock - 1) / kBlock, kBlock, 0, s>>>(g, f);
     return cudaGetLastError();
 }
 

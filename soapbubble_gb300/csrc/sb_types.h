@@ -47,6 +47,8 @@ struct SbDevStats {
     double mass_eta;               // sum eta * sin(theta)
     double mass_gamma;
     long long reinit_total;        // re-initialisations since creation
+    int wait_faults;               // bounded waits that gave up (copy never landed)
+    int pad;
 };
 
 }  // namespace sb

@@ -89,3 +89,21 @@ def test_full_size_steps_are_sane(gpulib, nT, recipe, dt):
         for name in ("gamma", "u_theta", "u_phi"):
             assert np.isfinite(gb.download(name)).all(), name
         assert abs(s.mass_eta - m0) / m0 < 0.05
+
+
+def test_autotuned_tiles_give_identical_results(gpulib):
+    """sb_autotune only changes how many cells a block covers: a tuned
+    bubble and an untuned twin stay bit-identical."""
+    a = _bubble(64, force_reinit=0)
+    b = _bubble(64, force_reinit=0)
+    with a, b:
+        tiles = a.autotune(0.0, 0.005)
+        ms = np.zeros(16)
+        b.step_timed(3, 0.0, 0.005, ms)
+        assert all(t in (64, 128, 256) for t in tiles[:8])
+        for k in range(10):
+            a.step(1, 0.0, 0.005)
+            b.step(1, 0.0, 0.005)
+        for name in ("eta", "gamma", "u_theta", "u_phi", "eta_delta", "fwd_t", "bwd_p"):
+            np.testing.assert_array_equal(a.download(name), b.download(name), err_msg=name)
+        assert a.stats().steps == b.stats().steps == 13
