@@ -325,6 +325,19 @@ def run_ours(args):
                "sample": f"{n} steps of the same 512x1024 workload (FP64 oracle, OpenMP "
                          f"{threads} threads, PCG to 1e-6), {el:.1f} s"}
 
+    ensemble = serving = None
+    if rank == 0 and world == 1:
+        h_u.free(); h_v.free(); h_eta.free(); flush.free()
+        gb.close()
+        gb = None
+        from soapbubble_gb300 import ensemble as ens, serve
+        if args.ensemble_steps > 0:
+            ensemble = ens.compare(steps=args.ensemble_steps, device=local)
+        if args.serve_requests > 0:
+            serving = serve.serve(args.serve_requests, 20.0, device=local)
+            serving["sample"] = (f"first {args.serve_requests} requests of the seeded stream "
+                                 "(python -m soapbubble_gb300.serve runs all 2000)")
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -347,10 +360,13 @@ def run_ours(args):
             "stage_steps": kr, "step_path": "CUDA graph per step (value); kernel-by-kernel with events (stages)",
             "solver_iters_mean": mean_iters, "solver_rel_resid_last": st.solver_rel_resid,
             "reinits": int(final.reinits), "result_finite": finite,
+            "ensemble": ensemble,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
-    h_u.free(); h_v.free(); h_eta.free(); flush.free()
-    gb.close()
+    if gb is not None:
+        h_u.free(); h_v.free(); h_eta.free(); flush.free()
+        gb.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -365,6 +381,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # the 64-bubble ensemble, plain vs batched (steps per member; 0 skips)
+    ap.add_argument("--ensemble-steps", type=int, default=200)
+    # a sample of the serving stream (requests; 0 skips)
+    ap.add_argument("--serve-requests", type=int, default=100)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -241,6 +241,10 @@ int sb_batch_destroy(sb_batch* batch);
  * Replays one captured CUDA graph per step on the batch's stream. */
 int sb_batch_step(sb_batch* batch, int n_steps, double t_frame, double dt);
 
+/* As sb_batch_step with member k at frame time t_frames[k] (members at
+ * different points of their runs, as in a serving loop). */
+int sb_batch_step_each(sb_batch* batch, int n_steps, const double* t_frames, double dt);
+
 /* As sb_batch_step but launching stage by stage and adding each stage's
  * device time (ms) to stage_ms[0 .. sb_stage_count()-1]; synchronises. */
 int sb_batch_step_timed(sb_batch* batch, int n_steps, double t_frame, double dt,

@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
     L.sb_batch_destroy.argtypes = [H]
     L.sb_batch_step.argtypes = [H, C.c_int, C.c_double, C.c_double]
     L.sb_batch_step_timed.argtypes = [H, C.c_int, C.c_double, C.c_double, dp]
+    L.sb_batch_step_each.argtypes = [H, C.c_int, dp, C.c_double]
     L.sb_batch_autotune.argtypes = [H, C.c_double, C.c_double, ip]
     L.sb_batch_synchronize.argtypes = [H]
     L.sb_batch_stream.argtypes = [H]
@@ -113,7 +114,7 @@ def lib() -> C.CDLL:
                  "sb_download_field_f32", "sb_synchronize", "sb_get_stats",
                  "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
-                 "sb_batch_autotune", "sb_batch_synchronize"):
+                 "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -131,4 +132,5 @@ EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_download_field_f32", "sb_synchronize", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
            "sb_run", "sb_write_exr_gray", "sb_mass_integrals_noalloc", "sb_bytes_required",
            "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",
-           "sb_batch_step_timed", "sb_batch_autotune", "sb_batch_synchronize", "sb_batch_stream"]
+           "sb_batch_step_timed", "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
+           "sb_batch_stream"]

@@ -189,8 +189,15 @@ class GpuBatch:
     def __exit__(self, *exc):
         self.close()
 
-    def step(self, n: int, t: float, dt: float) -> None:
-        check(lib().sb_batch_step(self.h, n, t, dt), "sb_batch_step")
+    def step(self, n: int, t, dt: float) -> None:
+        """n steps at frame time t (one float for every member, or one per
+        member)."""
+        if np.ndim(t) == 0:
+            check(lib().sb_batch_step(self.h, n, float(t), dt), "sb_batch_step")
+        else:
+            ts = np.ascontiguousarray(t, dtype=np.float64)
+            assert ts.size == len(self.members)
+            check(lib().sb_batch_step_each(self.h, n, _dp(ts), dt), "sb_batch_step_each")
 
     def step_timed(self, n: int, t: float, dt: float, stage_ms: np.ndarray) -> None:
         assert stage_ms.dtype == np.float64 and stage_ms.size >= lib().sb_stage_count()

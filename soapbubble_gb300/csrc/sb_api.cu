@@ -887,29 +887,34 @@ struct sb_batch {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[STAGE_COUNT + 1] = {};
     long long steps = 0;
-    double last_t = -1e300, last_dt = -1;
 };
 
 namespace {
 
-int batch_set_params(sb_batch* B, double t, double dt) {
-    if (t == B->last_t && dt == B->last_dt) return SB_OK;
+// Step scalars of every member for frame time t[k] (members may be at
+// different points of their runs); rewritten only when a member's (t, dt)
+// changes.  Each member's last (t, dt) mirrors its device copy.
+int batch_set_params_each(sb_batch* B, const double* t, double dt) {
+    bool same = true;
+    for (size_t k = 0; k < B->m.size() && same; ++k)
+        same = B->m[k]->last_t == t[k] && B->m[k]->last_dt == dt;
+    if (same) return SB_OK;
     SB_CHECK(cudaStreamSynchronize(B->stream));  // pinned slots may be in flight
-    for (sb_bubble* b : B->m) {
-        int rc = write_step_params(b, t, dt, B->stream);
+    for (size_t k = 0; k < B->m.size(); ++k) {
+        int rc = write_step_params(B->m[k], t[k], dt, B->stream);
         if (rc != SB_OK) return rc;
     }
-    B->last_t = t;
-    B->last_dt = dt;
     return SB_OK;
+}
+
+int batch_set_params(sb_batch* B, double t, double dt) {
+    std::vector<double> ts(B->m.size(), t);
+    return batch_set_params_each(B, ts.data(), dt);
 }
 
 void batch_advance(sb_batch* B, int n) {
     B->steps += n;
-    for (sb_bubble* b : B->m) {
-        bubble_advance(b, n);
-        b->last_t = -1e300;  // the bubble's own stream did not see the batch's copies
-    }
+    for (sb_bubble* b : B->m) bubble_advance(b, n);
 }
 
 }  // namespace
@@ -1036,6 +1041,19 @@ int sb_batch_step(sb_batch* B, int n_steps, double t_frame, double dt) {
     if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
     SB_CHECK(cudaSetDevice(B->device));
     int rc = batch_set_params(B, t_frame, dt);
+    if (rc != SB_OK) return rc;
+    if (n_steps > 0 && !B->graph && (rc = capture_plan(B->plan, B->stream, &B->graph)) != SB_OK)
+        return rc;
+    for (int s = 0; s < n_steps; ++s) SB_CHECK(cudaGraphLaunch(B->graph, B->stream));
+    batch_advance(B, n_steps);
+    return SB_OK;
+}
+
+int sb_batch_step_each(sb_batch* B, int n_steps, const double* t_frames, double dt) {
+    if (!B || !t_frames) return fail(SB_ERR_INVALID, "null argument");
+    if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
+    SB_CHECK(cudaSetDevice(B->device));
+    int rc = batch_set_params_each(B, t_frames, dt);
     if (rc != SB_OK) return rc;
     if (n_steps > 0 && !B->graph && (rc = capture_plan(B->plan, B->stream, &B->graph)) != SB_OK)
         return rc;

@@ -87,18 +87,23 @@ class SHSeries:
         return A, B
 
     def evaluate(self, theta: np.ndarray, phi: np.ndarray, dphi: bool = False) -> np.ndarray:
-        """Values (or d/dphi) on the tensor grid theta[:, None] x phi[None, :]."""
+        """Values (or d/dphi) on the tensor grid theta[:, None] x phi[None, :]:
+        sum over m of a_m(theta) cos(m phi) + b_m(theta) sin(m phi), as one
+        matrix product of the theta factors and the phi factors."""
         A, B = self._theta_parts(theta)
-        out = np.zeros((theta.size, phi.size))
-        for m in set(A) | set(B):
-            a = A.get(m, np.zeros_like(theta))
-            b = B.get(m, np.zeros_like(theta))
+        ms = sorted(set(A) | set(B))
+        zero = np.zeros_like(theta)
+        T = np.empty((theta.size, 2 * len(ms)))
+        F = np.empty((2 * len(ms), phi.size))
+        for k, m in enumerate(ms):
+            T[:, 2 * k] = A.get(m, zero)
+            T[:, 2 * k + 1] = B.get(m, zero)
             c, s = np.cos(m * phi), np.sin(m * phi)
             if dphi:
-                out += m * (-np.outer(a, s) + np.outer(b, c))
+                F[2 * k], F[2 * k + 1] = -m * s, m * c
             else:
-                out += np.outer(a, c) + np.outer(b, s)
-        return out
+                F[2 * k], F[2 * k + 1] = c, s
+        return T @ F
 
     def dtheta(self, theta: np.ndarray, phi: np.ndarray, step: float = 1e-6) -> np.ndarray:
         return (self.evaluate(theta + step, phi) - self.evaluate(theta - step, phi)) / (2 * step)
