@@ -24,10 +24,14 @@
 #include "sb_fastmath.cuh"
 #include "sb_types.h"
 
-// Inlining of the heavy geometry helpers (conversions, slerp, map lookup):
-// out-of-line calls keep the map kernels small in the instruction cache.
+// Inlining of the geometry helpers: the slerp and the map lookup are inlined
+// (measured faster); the two position / displacement conversions stay out of
+// line, which keeps the map kernels small in the instruction cache.
 #ifndef SB_GEOM_INLINE
-#define SB_GEOM_INLINE __noinline__
+#define SB_GEOM_INLINE __forceinline__
+#endif
+#ifndef SB_CONV_INLINE
+#define SB_CONV_INLINE __noinline__
 #endif
 
 namespace sb {
@@ -67,7 +71,7 @@ __device__ __forceinline__ float blerp(float from, float to, float a) {
 
 // Displacement P - C, in the frame, of the point at grid offsets (dth, dph)
 // from the frame's base.
-__device__ SB_GEOM_INLINE f3 disp_from_offsets(Frame F, float dth, float dph, float h) {
+__device__ SB_CONV_INLINE f3 disp_from_offsets(Frame F, float dth, float dph, float h) {
     float sh, chh;
     fsincos(0.5f * dth * h, &sh, &chh);
     const float sm = F.s0 * chh + F.c0 * sh;  // sin(t0 + dt/2)
@@ -84,7 +88,7 @@ __device__ SB_GEOM_INLINE f3 disp_from_offsets(Frame F, float dth, float dph, fl
 
 // Grid position of the point C + d.  Points past a pole come back with the
 // base column shifted by nTheta (azimuth + pi) so the float offset stays small.
-__device__ SB_GEOM_INLINE Pos pos_from_disp(Frame F, f3 d, float invh, int nT) {
+__device__ SB_CONV_INLINE Pos pos_from_disp(Frame F, f3 d, float invh, int nT) {
     const float Px = F.s0 + d.x, Py = d.y, Pz = F.c0 + d.z;
     const float rho = sqrtf(Px * Px + Py * Py);
     const float den = rho + F.s0;
