@@ -138,14 +138,25 @@ __device__ __noinline__ f3 slerp_disp_far(float s0, float c0, f3 dA, f3 dB, floa
 //   cA as cB with a -> 1-a,
 //   k / (p u / 2) = 1 + (1+p) u/12 + (p^2+3p+3) u^2/360
 //                   + (p^3+6p^2+17p+17) u^3/20160,   p = a (1-a);
-// the truncation is below 1e-9 relative.  Farther points take the exact
-// formula out of line.
+// the truncation is below 1e-9 relative.  For chords up to 1/16 (u < 0.004)
+// the u^2 and u^3 terms change the coefficients by less than 1e-9 and are
+// dropped.  Farther points take the exact formula out of line.
 __device__ __forceinline__ f3 slerp_disp_inl(float s0, float c0, f3 dA, f3 dB, float a) {
     const f3 e = dB - dA;
     const float c2 = dot3(e, e);
     if (c2 > 0.0625f) return slerp_disp_far(s0, c0, dA, dB, a);
-    const float u = c2 * fmaf(c2, fmaf(c2, fmaf(c2, 1.0f / 560.0f, 1.0f / 90.0f), 1.0f / 12.0f), 1.0f);
     const float b = 1.0f - a;
+    if (c2 <= 0.00390625f) {
+        const float u = c2 * fmaf(c2, 1.0f / 12.0f, 1.0f);
+        const float a2 = a * a, b2 = b * b;
+        const float cB = a * fmaf(u * (1.0f - a2), fmaf(u, fmaf(a2, -3.0f, 7.0f) * (1.0f / 360.0f), 1.0f / 6.0f), 1.0f);
+        const float cA = b * fmaf(u * (1.0f - b2), fmaf(u, fmaf(b2, -3.0f, 7.0f) * (1.0f / 360.0f), 1.0f / 6.0f), 1.0f);
+        const float p = a * b;
+        const float k = 0.5f * p * u * fmaf(u, (1.0f + p) * (1.0f / 12.0f), 1.0f);
+        const f3 C = {s0, 0.0f, c0};
+        return cA * dA + cB * dB + k * C;
+    }
+    const float u = c2 * fmaf(c2, fmaf(c2, fmaf(c2, 1.0f / 560.0f, 1.0f / 90.0f), 1.0f / 12.0f), 1.0f);
     const float a2 = a * a, b2 = b * b;
     const float pa = fmaf(u, fmaf(u, fmaf(a2, fmaf(a2, 3.0f, -18.0f), 31.0f) * (1.0f / 15120.0f),
                                   fmaf(a2, -3.0f, 7.0f) * (1.0f / 360.0f)),
@@ -315,6 +326,27 @@ __device__ __forceinline__ float sample_utheta(const SbGrid& g, const float* __r
 // four map points around q, slerped along phi on each row and then along
 // theta.  Map entries are float2 offsets from their own cell centre.  The
 // result is a displacement in frame F.
+// The lookup for a stencil already computed at the query point (the same
+// cell-centred stencil also serves scalar samples there).
+__device__ SB_GEOM_INLINE f3 map_at_stencil(const float2* __restrict__ map, Frame F,
+                                             const CStencil& s, int nT, float h) {
+    const int nP = 2 * nT, maskP = nP - 1;
+    const float baseI = (float)0.5f - F.fi;
+    auto point = [&](int r, int c) -> f3 {
+        const float2 m = map[r * nP + c];
+        const float dth = (float)(r - F.bi) + baseI + m.x;
+        int dj = c - F.bj;
+        dj = ((dj + nT) & maskP) - nT;  // wrap to [-nT, nT)
+        const float dph = (float)dj + (m.y - F.fj);
+        return disp_from_offsets(F, dth, dph, h);
+    };
+    const f3 ll = point(s.r0, s.c00), lr = point(s.r0, s.c01);
+    const f3 hl = point(s.r1, s.c10), hr = point(s.r1, s.c11);
+    const f3 lo = slerp_disp(F.s0, F.c0, ll, lr, s.b);
+    const f3 hi = slerp_disp(F.s0, F.c0, hl, hr, s.b);
+    return slerp_disp(F.s0, F.c0, lo, hi, s.a);
+}
+
 __device__ SB_GEOM_INLINE f3 sample_map_impl(const float2* __restrict__ map, Frame F, Pos q,
                                               int nT, float h, float invh) {
     SbGrid g;
@@ -323,22 +355,7 @@ __device__ SB_GEOM_INLINE f3 sample_map_impl(const float2* __restrict__ map, Fra
     g.maskP = g.nP - 1;
     g.h = h;
     g.invh = invh;
-    const CStencil s = centred_stencil(g, q, 0.0f);
-    const int nP = g.nP;
-    const float baseI = (float)0.5f - F.fi;
-    auto point = [&](int r, int c) -> f3 {
-        const float2 m = map[r * nP + c];
-        const float dth = (float)(r - F.bi) + baseI + m.x;
-        int dj = c - F.bj;
-        dj = ((dj + nT) & g.maskP) - nT;  // wrap to [-nT, nT)
-        const float dph = (float)dj + (m.y - F.fj);
-        return disp_from_offsets(F, dth, dph, g.h);
-    };
-    const f3 ll = point(s.r0, s.c00), lr = point(s.r0, s.c01);
-    const f3 hl = point(s.r1, s.c10), hr = point(s.r1, s.c11);
-    const f3 lo = slerp_disp(F.s0, F.c0, ll, lr, s.b);
-    const f3 hi = slerp_disp(F.s0, F.c0, hl, hr, s.b);
-    return slerp_disp(F.s0, F.c0, lo, hi, s.a);
+    return map_at_stencil(map, F, centred_stencil(g, q, 0.0f), nT, h);
 }
 
 __device__ __forceinline__ f3 sample_map(const SbGrid& g, const float2* __restrict__ map,
@@ -448,8 +465,7 @@ struct SStencil {
     float a, b;
 };
 
-__device__ __forceinline__ SStencil scalar_stencil(const SbGrid& g, Pos q) {
-    const CStencil c = centred_stencil(g, q, 0.0f);
+__device__ __forceinline__ SStencil sstencil_of(const SbGrid& g, const CStencil& c) {
     SStencil s;
     s.i00 = c.r0 * g.nP + c.c00;
     s.i01 = c.r0 * g.nP + c.c01;
@@ -458,6 +474,10 @@ __device__ __forceinline__ SStencil scalar_stencil(const SbGrid& g, Pos q) {
     s.a = c.a;
     s.b = c.b;
     return s;
+}
+
+__device__ __forceinline__ SStencil scalar_stencil(const SbGrid& g, Pos q) {
+    return sstencil_of(g, centred_stencil(g, q, 0.0f));
 }
 
 __device__ __forceinline__ float gather(const float* __restrict__ f, const SStencil& s) {

@@ -20,9 +20,16 @@ __device__ __noinline__ float slow_cos(float x) { return cosf(x); }
 __device__ __noinline__ float slow_arc(float x) { return 2.0f * asinf(fminf(x, 1.0f)); }
 __device__ __noinline__ float slow_atan2(float y, float x) { return atan2f(y, x); }
 
-// sin and cos; Taylor to x^7 / x^8 on |x| <= 0.2 (truncation < 2e-12),
-// to x^11 / x^12 on |x| <= 0.8 (truncation < 1e-11).
+// sin and cos; Taylor to x^3 / x^4 on |x| <= 1/32 (the usual half-angle of
+// a few cells; relative truncation < 1e-8), to x^7 / x^8 on |x| <= 0.2
+// (< 2e-12), to x^11 / x^12 on |x| <= 0.8 (< 1e-11).
 __device__ __forceinline__ void fsincos(float x, float* s, float* c) {
+    if (fabsf(x) <= 0.03125f) {
+        const float x2 = x * x;
+        *s = fmaf(-1.6666666667e-1f * x2, x, x);                 // x - x^3/3!
+        *c = fmaf(fmaf(x2, 4.1666666667e-2f, -0.5f), x2, 1.0f);  // 1 - x^2/2! + x^4/4!
+        return;
+    }
     if (fabsf(x) <= 0.2f) {
         const float x2 = x * x;
         float ps = -1.9841269841e-4f;          // -1/7!
@@ -84,10 +91,15 @@ __device__ __forceinline__ float fcos_small(float x) {
 }
 
 // 2 asin(c / 2) for a chord c in [0, 2]: the arc of a chord on the unit
-// sphere.  Binomial series of arcsin to x^11 on x = c/2 <= 0.25
-// (truncation < 3e-10 relative).
+// sphere.  Binomial series of arcsin to x^5 on x = c/2 <= 1/16 (truncation
+// < 3e-9 relative), to x^11 on x <= 0.25 (< 3e-10).
 __device__ __forceinline__ float farc_of_chord(float c) {
     const float x = 0.5f * c;
+    if (x <= 0.0625f) {
+        const float x2 = x * x;
+        const float p = fmaf(x2, 7.5e-2f, 1.6666666667e-1f);  // 1/6 + 3/40 x^2
+        return 2.0f * fmaf(p * x2, x, x);
+    }
     if (x <= 0.25f) {
         const float x2 = x * x;
         float p = 2.2372159091e-2f;            // 63/2816
@@ -100,12 +112,17 @@ __device__ __forceinline__ float farc_of_chord(float c) {
     return slow_arc(x);
 }
 
-// atan2(y, x); Gregory series of atan(y/x) to t^15 when x > 0 and
-// |y| <= x/4 (truncation < 1e-10 relative), library atan2f otherwise.
+// atan2(y, x); Gregory series of atan(y/x) to t^5 when x > 0 and
+// |y| <= x/16 (truncation < 1e-8 relative), to t^15 when |y| <= x/4
+// (< 1e-10), library atan2f otherwise.
 __device__ __forceinline__ float fatan2(float y, float x) {
     if (x > 0.0f && fabsf(y) <= 0.25f * x) {
         const float t = y / x;
         const float t2 = t * t;
+        if (t2 <= 0.00390625f) {
+            const float p = fmaf(t2, 2.0e-1f, -3.3333333333e-1f);  // -1/3 + t^2/5
+            return fmaf(p * t2, t, t);
+        }
         float p = -6.6666666667e-2f;           // -1/15
         p = fmaf(p, t2, 7.6923076923e-2f);     //  1/13
         p = fmaf(p, t2, -9.0909090909e-2f);    // -1/11

@@ -75,10 +75,10 @@ __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& 
 
     // backward map and gamma share the backward trace
     const Trace Tb = trace_gc(g, f.uth, f.uph, F, gt, gp, dt);
-    const Pos qb = pos_of(F, Tb, g);
-    const f3 db = sample_map(g, f.bwd[cur], F, qb);
+    const CStencil cb = centred_stencil(g, pos_of(F, Tb, g), 0.0f);
+    const f3 db = map_at_stencil(f.bwd[cur], F, cb, g.nT, g.h);
     f.bwd[cur ^ 1][idx] = map_entry_from_disp(g, F, db);
-    f.gam_adv[idx] = sample_scalar(g, f.gam, qb);
+    f.gam_adv[idx] = gather(f.gam, sstencil_of(g, cb));
 
     // air flow = initial wind + corridor(t); NaN -> 0
     const float wg = f.step->windg;
@@ -153,10 +153,10 @@ __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, c
     float attrib = 0.0f;
 #pragma unroll 1
     for (int k = 0; k < 5; ++k) {
-        const Pos q1 = pos_from_disp(F, d1s[k], g.invh, g.nT);
-        const f3 d2 = sample_map(g, f.bwdprev, F, q1);
+        const CStencil c1 = centred_stencil(g, pos_from_disp(F, d1s[k], g.invh, g.nT), 0.0f);
+        const f3 d2 = map_at_stencil(f.bwdprev, F, c1, g.nT, g.h);
         const Pos q2 = pos_from_disp(F, d2, g.invh, g.nT);
-        const SStencil s1 = scalar_stencil(g, q1);
+        const SStencil s1 = sstencil_of(g, c1);
         const SStencil s2 = scalar_stencil(g, q2);
         const float sDelta = gather(f.eta_delta, s1);
         attrib += (1.0f - blend) * kW5[k] *
