@@ -12,9 +12,10 @@
 //   k_post         divergenceKernel_fromGamma, applyforcevel{theta,phi},
 //                  applyforceThickness, substractPitched (1276-1295, 1819-1935,
 //                  2041-2078)
-//   k_accum        accumulateChangesCentered x2 (2081-2114) and
-//                  estimateDistortionKernel + maxAbs (1131-1168, 1019-1043)
-//   k_reinit{1,2,3} reInitializeMapping, correctCentered1/2 (2180-2280, 2509-2564)
+//   k_accum        accumulateChangesCentered x2 (2081-2114),
+//                  estimateDistortionKernel + maxAbs (1131-1168, 1019-1043) and
+//                  the error of correctCentered1 (2180-2216)
+//   k_reinit       reInitializeMapping, correctCentered2 (2218-2280, 2509-2564)
 // van der Waals is identically zero in the reference (W1 = W2 = 0,
 // bubble.cu:2633-2638) and is folded out.
 #include <cooperative_groups.h>
@@ -381,7 +382,10 @@ __device__ __forceinline__ float warp_max(float v) {
 }
 
 // BIMOCQ change accumulation through the forward map, fused with the
-// forward/backward distortion estimate of the same maps.
+// forward/backward distortion estimate of the same maps and with the error
+// estimate of a re-initialisation (correctCentered1, which samples the new
+// fields at the same five points): the error is formed every step, and the
+// re-initialisation, when the distortion calls for it, only corrects.
 // returns the cell's distortion (0 outside the grid)
 __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                            int idx) {
@@ -391,6 +395,7 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
     const float2* fwd = f.fwd[cur ^ 1];
     const float2* bwd = f.bwd[cur ^ 1];
     float ed = f.eta_delta[idx], gd = f.gam_delta[idx];
+    float th = 0.0f, gm = 0.0f;
     f3 ds[5];
     sample_map_multi5(g, fwd, F, ds);
 #pragma unroll
@@ -398,9 +403,13 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
         const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
         ed += kW5[k] * gather(f.d_eta, s);
         gd += kW5[k] * gather(f.d_gam, s);
+        th += kW5[k] * gather(f.eta, s);
+        gm += kW5[k] * gather(f.gam, s);
     }
     f.eta_delta[idx] = ed;
     f.gam_delta[idx] = gd;
+    f.err_eta[idx] = (th - ed - f.eta_init[idx]) * 0.5f;
+    f.err_gam[idx] = (gm - gd - f.gam_init[idx]) * 0.5f;
     // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
     float2 m = fwd[idx];
     const float d1 = dist_from_disp(sample_map(g, bwd, F, frame_pos(F, m.x, m.y)), g.invh);
@@ -473,24 +482,6 @@ __device__ __forceinline__ bool reinit_now(const SbDevStats* st) {
     return __uint_as_float(st->distortion_bits) > 4.0f;
 }
 
-// correctCentered1: BIMOCQ error estimate through the forward map.
-__device__ __forceinline__ void reinit_error(const SbGrid& g, const SbFields& f, int cur, int idx) {
-    const int i = idx >> g.logP, j = idx & g.maskP;
-    const Frame F = cell_frame(g, i, j);
-    const float2* fwd = f.fwd[cur ^ 1];
-    float th = 0.0f, gm = 0.0f;
-    f3 ds[5];
-    sample_map_multi5(g, fwd, F, ds);
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-        const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
-        th += kW5[k] * gather(f.eta, s);
-        gm += kW5[k] * gather(f.gam, s);
-    }
-    f.err_eta[idx] = (th - f.eta_delta[idx] - f.eta_init[idx]) * 0.5f;
-    f.err_gam[idx] = (gm - f.gam_delta[idx] - f.gam_init[idx]) * 0.5f;
-}
-
 // 3x3 neighbour of (i, j) with the reference's across-pole rule (validateId).
 __device__ __forceinline__ int nb_index(const SbGrid& g, int i, int j) {
     if (i < 0) { i = 0; j += g.nT; }
@@ -548,7 +539,8 @@ __device__ __forceinline__ void reinit_commit(const SbFields& f, int cur, int id
 
 // reInitializeMapping (kernel/bubble.cu:2509-2564) for every bubble of the
 // set whose distortion exceeds 4 cells (or that forces it): one cooperative
-// launch, three phases over the bubbles' tiles separated by grid barriers.
+// launch, two phases over the bubbles' tiles separated by a grid barrier
+// (correct, then commit; the error estimate was formed by k_accum).
 // The decisions are read from device memory, so no host synchronisation is
 // needed; every block reads every bubble's decision, so all blocks agree on
 // whether any phase runs, and without a re-initialisation they return at
@@ -574,16 +566,8 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
                 d.f.stats->reinit = 1;
                 d.f.stats->reinit_total += 1;
             }
-            reinit_error(d.g, d.f, d.cur, idx);
-        }
-    }
-    grid.sync();
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int2 tl = tiles[t];
-        const SbBubbleDesc& d = *descs[tl.x];
-        if (!reinit_now(d.f.stats)) continue;
-        for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
             reinit_correct(d.g, d.f, d.cur, idx);
+        }
     }
     grid.sync();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
