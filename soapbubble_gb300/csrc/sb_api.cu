@@ -143,7 +143,7 @@ struct ArenaPlan {
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
     size_t div, d_eta, d_gam, err_eta, err_gam;
     size_t dmass, cE, cS, rhs, r0, x, dx, r, z, p, q, xff, pcr, pcr_levels, step, stats;
-    size_t self, self_list, roff, done_at, cnt, rec, rowpart;  // the bubble's solve set
+    size_t self, self_list, roff, done_at, cnt, rec, acc;  // the bubble's solve set
     size_t tiles[3];                                           // its cell tiles
 };
 
@@ -180,7 +180,7 @@ ArenaPlan plan_arena(const SbGrid& g) {
     a.done_at = a.L.take(4);
     a.cnt = a.L.take(4);
     a.rec = a.L.take(2 * sizeof(SbSolveRec));
-    a.rowpart = a.L.take((size_t)g.nT * 2 * 3 * sizeof(float2));
+    a.acc = a.L.take(sizeof(unsigned long long) * kSolveAccWords);
     a.step = a.L.take(sizeof(SbStepParams));
     a.stats = a.L.take(sizeof(SbDevStats) + 64);
     return a;
@@ -390,7 +390,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.done_at = (int*)(A + a.done_at);
     f.cnt = (int*)(A + a.cnt);
     f.rec = (SbSolveRec*)(A + a.rec);
-    f.rowpart = (float2*)(A + a.rowpart);
+    f.acc = (unsigned long long*)(A + a.acc);
 
     // trigonometric tables in FP64, stored FP32
     std::vector<float> tab(4 * g.nT + 2);
@@ -476,7 +476,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
         S.rec = f.rec;
         S.done_at = f.done_at;
         S.cnt = f.cnt;
-        S.rowpart = f.rowpart;
+        S.acc = f.acc;
         P.maxNP = g.nP;
         P.solver = b->solver;
         b->desc = d;
@@ -975,7 +975,8 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     for (int s = 0; s < 3; ++s) o_tiles[s] = L.take(sizeof(int2) * tiles[s].size());
     const size_t o_roff = L.take(sizeof(int) * (n + 1)),
                  o_rec = L.take(sizeof(SbSolveRec) * 2 * n), o_done = L.take(sizeof(int) * n),
-                 o_cnt = L.take(sizeof(int) * n), o_part = L.take(sizeof(float2) * 2 * 3 * R);
+                 o_cnt = L.take(sizeof(int) * n),
+                 o_acc = L.take(sizeof(unsigned long long) * kSolveAccWords * n);
     e = cudaMalloc((void**)&B->arena, L.bytes);
     if (e == cudaSuccess) e = cudaMemset(B->arena, 0, L.bytes);
     if (e != cudaSuccess) {
@@ -1004,7 +1005,7 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     S.rec = (SbSolveRec*)(A + o_rec);
     S.done_at = (int*)(A + o_done);
     S.cnt = (int*)(A + o_cnt);
-    S.rowpart = (float2*)(A + o_part);
+    S.acc = (unsigned long long*)(A + o_acc);
     // members may have work queued on their own streams
     for (sb_bubble* b : B->m) e = e == cudaSuccess ? cudaStreamSynchronize(b->stream) : e;
     if (e == cudaSuccess)

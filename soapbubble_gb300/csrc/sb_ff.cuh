@@ -83,6 +83,22 @@ __device__ __forceinline__ ff ff_mul_f(ff x, float a) {
 
 __device__ __forceinline__ ff ff_neg(ff x) { return {-x.hi, -x.lo}; }
 
+// x / y: a float quotient corrected by one step on the float-float
+// remainder x - q y (about 44 correct bits).
+__device__ __forceinline__ ff ff_div(ff x, ff y) {
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    const ff r = ff_add(x, ff_neg(ff_mul_f(y, q1)));
+    const float q2 = __fdiv_rn(r.hi, y.hi);
+    ff q;
+    fast_two_sum(q1, q2, q.hi, q.lo);
+    return q;
+}
+
+// x <= y for normalised values.
+__device__ __forceinline__ bool ff_le(ff x, ff y) {
+    return x.hi < y.hi || (x.hi == y.hi && x.lo <= y.lo);
+}
+
 // Rounded to the nearest float (up to one rounding of hi + lo).
 __device__ __forceinline__ float ff_to_f(ff x) { return __fadd_rn(x.hi, x.lo); }
 

@@ -35,7 +35,7 @@ struct SbFields {
     SbBubbleDesc* self;
     int *roff, *done_at, *cnt;
     SbSolveRec* rec;
-    float2* rowpart;
+    unsigned long long* acc;
     SbStepParams* step;                            // device copy of step scalars
     SbDevStats* stats;
 };
@@ -56,6 +56,7 @@ struct SolverConfig {
     double tol;     // relative residual ||b - A x|| / ||b||
     int precond;    // 0: Jacobi, 1: exact phi-line (periodic tridiagonal per row)
     int ring;       // factor levels staged in shared memory at once (set at launch)
+    float tol2f;    // target r.r / |b|^2 of the iterate (set at launch)
 };
 
 // Step stages in launch order (sb_step.cu, sb_solver.cu).  `cur` selects the
@@ -78,13 +79,19 @@ cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s);
 
 // Scalars of one system of a solve, written by the block that completes the
 // system's last row in a phase and read in the next phase (double buffered).
+// Scalars of one system's conjugate-gradient iteration; float-float values
+// are stored as (hi, lo) pairs.
 struct SbSolveRec {
-    double rz, rr, bnorm, tol2, alpha;
+    float2 rz, rr, bb, tol2, alpha;  // r.z, r.r, |b|^2, target for r.r, step length
     float beta;
     int state;  // iterate, or check the true residual / restart (mixed mode)
     int it;
     int conv;
 };
+
+// Words of a system's exact dot-product accumulators: three buffers (used
+// in rotation by phase) of three values of 10 fixed-point chunks and a flag.
+constexpr int kSolveAccWords = 3 * 3 * 11;
 
 // A set of implicit systems solved by one cooperative launch: the system of
 // one bubble, or the systems of every bubble of a batch (at most 1024, with
@@ -97,7 +104,7 @@ struct SbSolveSet {
     SbSolveRec* rec;            // [2 * nb]
     int* done_at;               // [nb] first phase in which the system is finished
     int* cnt;                   // [nb] rows completed in the current phase (0 between launches)
-    float2* rowpart;            // [2][3 * R] float-float partial sums of every row, by phase parity
+    unsigned long long* acc;    // [nb][kSolveAccWords] exact dot-product accumulators (0 between launches)
 };
 
 // Implicit surfactant solve (sb_solver.cu).  prepare_solve sets the kernel

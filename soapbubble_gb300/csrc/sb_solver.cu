@@ -10,11 +10,11 @@
 // systems form one list that is dealt to the blocks round robin; a phase
 // (separated from the next by a grid barrier) visits the rows of the
 // systems still iterating, so a system that needs more iterations than the
-// others is spread over the whole GPU.  Every row publishes its partial dot
-// products; the block that completes the last row of a system in a phase
-// sums that system's row partials in row order and advances the system's
-// scalars.  Scalars therefore do not depend on how rows are distributed:
-// a bubble solved alone and inside a batch gives bit-identical results.
+// others is spread over the whole GPU.  Every row adds its partial dot
+// products into the system's exact fixed-point accumulator, so the sums,
+// and the scalars advanced from them, do not depend on how rows are
+// distributed or in which order blocks add: a bubble solved alone and
+// inside a batch gives bit-identical results.
 //
 // Preconditioner: exact solve of each theta row's periodic tridiagonal block
 // (phi couplings; the theta couplings stay on its diagonal).  Near the poles
@@ -51,28 +51,6 @@ constexpr int kWaitPolls = 1 << 22;   // mbarrier polls before a copy counts as 
 constexpr int kMaxSystems = 1024;     // systems of one solve set
 constexpr int kRowChunk = 16;         // rows a block publishes at a time
 enum { ST_ITER = 0, ST_CHECK = 1 };
-
-// Block sums of three float-float values, returned to every thread.  Fixed
-// order (lanes by shuffle tree, then the warps in order), so equal inputs
-// give equal sums in every block.
-__device__ __forceinline__ void block_sum3(ff& a, ff& b, ff& c) {
-    __shared__ ff part[3][kSolveBlock / 32];
-    a = ff_warp_sum(a);
-    b = ff_warp_sum(b);
-    c = ff_warp_sum(c);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) { part[0][w] = a; part[1][w] = b; part[2][w] = c; }
-    __syncthreads();
-    ff x = ff_zero(), y = ff_zero(), z = ff_zero();
-#pragma unroll
-    for (int k = 0; k < kSolveBlock / 32; ++k) {
-        x = ff_add(x, part[0][k]);
-        y = ff_add(y, part[1][k]);
-        z = ff_add(z, part[2][k]);
-    }
-    __syncthreads();
-    a = x; b = y; c = z;
-}
 
 // ---------------------------------------------------------------------------
 // Shared-memory staging of the stored cyclic-reduction factors.  Each
@@ -445,11 +423,11 @@ __device__ __forceinline__ ff row_true_residual(const SbGrid& g, const SbFields&
 
 // x += alpha p_new, r -= alpha q; rv = the new r.
 template <bool MIXED, int PER>
-__device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, int i, double alpha,
+__device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, int i, ff alpha,
                                            const float* __restrict__ pnew, float (&rv)[PER]) {
     const int nP = g.nP, row = i * nP;
-    const float af = (float)alpha;
-    const ff a2 = ff_from_d(alpha);
+    const float af = ff_to_f(alpha);
+    const ff a2 = alpha;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int j = col_of(k);
@@ -498,13 +476,161 @@ __device__ __forceinline__ void row_final(const SbGrid& g, const SbFields& f, in
 }
 
 // ---------------------------------------------------------------------------
-// Per-system scalars.  Records are read with L2 loads (__ldcg): they are
-// written by other blocks between phases.
+// Exact sums.  A row's dot-product partials (float-float) are added into a
+// long fixed-point accumulator: every float is an integer multiple of
+// 2^-149 below 2^128, so 9 chunks of 32 bits held in 64-bit integers (and a
+// tenth for carries) cover it exactly, and integer additions do not depend
+// on their order.  The
+// total is therefore the same whichever block adds which row, and the same
+// for a system solved alone or inside a set; a system's blocks add with
+// fire-and-forget atomics and nobody sums row partials.  A word per value
+// flags NaN or infinity.  Each system has three buffers of three values,
+// used in rotation by phase (p % 3): added in phase p, read at the end of
+// phase p (sets) or at the start of phase p + 1 (one system), and zeroed
+// again before phase p + 3.
+constexpr int kAccChunks = 10;             // chunks 0..8 take additions, chunk 9 carries
+constexpr int kAccWords = kAccChunks + 1;  // per value
+constexpr int kAccBuf = 3 * kAccWords;     // per buffer (three values)
+static_assert(3 * kAccBuf == kSolveAccWords, "accumulator words per system");
+
+__device__ __forceinline__ unsigned long long* acc_buf(const SbSolveSet& S, int b, int p) {
+    return S.acc + (size_t)b * kSolveAccWords + (size_t)(p % 3) * kAccBuf;
+}
+
+// a += v exactly.
+__device__ __forceinline__ void acc_add(unsigned long long* a, float v) {
+    const unsigned u = __float_as_uint(v);
+    const int ex = (int)((u >> 23) & 0xffu);
+    if (ex == 0xff) {
+        atomicOr(a + kAccChunks, 1ull);
+        return;
+    }
+    long long m = (long long)(u & 0x7fffffu);
+    if (ex == 0 && m == 0) return;  // +-0
+    int P = 0;                      // exponent of the mantissa's last bit, plus 149
+    if (ex != 0) {
+        m |= 0x800000;
+        P = ex - 1;
+    }
+    if (u >> 31) m = -m;
+    const long long w = m << (P & 31);  // |w| < 2^55: two chunks
+    const int k = P >> 5;
+    atomicAdd(a + k, (unsigned long long)(w & 0xffffffffll));
+    atomicAdd(a + k + 1, (unsigned long long)(w >> 32));
+}
+
+// x.hi + x.lo into value v of buffer a.
+__device__ __forceinline__ void acc_add_ff(unsigned long long* a, int v, ff x) {
+    acc_add(a + v * kAccWords, x.hi);
+    acc_add(a + v * kAccWords, x.lo);
+}
+
+// Carries: chunks 0..8 into [0, 2^32), the sign in chunk 9.
+__device__ __forceinline__ void acc_normalize(long long (&c)[kAccChunks]) {
+    long long carry = 0;
+#pragma unroll
+    for (int k = 0; k < kAccChunks - 1; ++k) {
+        const long long v = c[k] + carry;
+        c[k] = v & 0xffffffffll;
+        carry = v >> 32;
+    }
+    c[kAccChunks - 1] += carry;
+}
+
+// The accumulated value (words a[0 .. kAccWords)) as a normalised
+// float-float, formed with integer and FP32 operations only: GB300 issues
+// FP64 at a small fraction of its FP32 rate, and this sits on every phase's
+// critical path.  The leading 48 bits are kept (truncated below).
+__device__ __forceinline__ ff acc_ff(const unsigned long long* a) {
+    if (a[kAccChunks]) return {__int_as_float(0x7fffffff), 0.0f};
+    long long c[kAccChunks];
+#pragma unroll
+    for (int k = 0; k < kAccChunks; ++k) c[k] = (long long)a[k];
+    acc_normalize(c);
+    const bool neg = c[kAccChunks - 1] < 0;
+    if (neg) {
+#pragma unroll
+        for (int k = 0; k < kAccChunks; ++k) c[k] = -c[k];
+        acc_normalize(c);
+    }
+    // the top non-zero chunk t and the two below it (unrolled: the chunks
+    // stay in registers)
+    int t = -1;
+    unsigned long long c0 = 0, c1 = 0, c2 = 0;
+#pragma unroll
+    for (int k = 0; k < kAccChunks; ++k) {
+        if (c[k] != 0) {
+            t = k;
+            c0 = (unsigned long long)c[k];
+            c1 = k >= 1 ? (unsigned long long)c[k - 1] : 0ull;
+            c2 = k >= 2 ? (unsigned long long)c[k - 2] : 0ull;
+        }
+    }
+    if (t < 0) return ff_zero();
+    // 64-bit window from the top chunk, leading bit at bit 63: the value is
+    // M 2^e0 up to the bits below the window
+    const unsigned long long H = (c0 << 32) | c1;
+    const unsigned long long L = c2;
+    const int lz = __clzll(H);  // 0..31: c[t] is in [1, 2^32)
+    const unsigned long long M = lz ? (H << lz) | (L >> (32 - lz)) : H;
+    const int e0 = 32 * (t - 1) - lz - 149;
+    const float hi = scalbnf((float)(unsigned)(M >> 40), e0 + 40);  // 24 bits: exact
+    const unsigned long long rem = M & ((1ull << 40) - 1);
+    const float lo = scalbnf(__fmaf_rn((float)(unsigned)(rem >> 20), 1048576.0f,
+                                       (float)(unsigned)(rem & 0xfffffull)),
+                             e0);
+    ff r;
+    fast_two_sum(hi, lo, r.hi, r.lo);
+    return neg ? ff_neg(r) : r;
+}
+
+__device__ __forceinline__ void acc_zero(unsigned long long* a, int n, int tid, int nthreads) {
+    for (int k = tid; k < n; k += nthreads) a[k] = 0ull;
+}
+
+// Rows r0, r0 + stride, ... (n of them) of system b were computed by this
+// block; warp w left its share of the k-th in s_part[k][w].  Folds each
+// row's warp shares in warp order and adds the row's partials into the
+// phase's accumulator buffer.
+__device__ __forceinline__ void publish_rows(const SbSolveSet& S, int b, int p, int n,
+                                             ff (*s_part)[kWarps][3]) {
+    __syncthreads();
+    if (threadIdx.x < 3 * n) {
+        const int k = threadIdx.x / 3, v = threadIdx.x - 3 * k;
+        ff x = ff_zero();
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) x = ff_add(x, s_part[k][w][v]);
+        acc_add_ff(acc_buf(S, b, p), v, x);
+    }
+    __syncthreads();
+}
+
+// Counts n finished rows of system b; returns (in every thread) whether
+// they were the system's last.  The accumulator updates of the block come
+// first.
+__device__ __forceinline__ bool count_rows(const SbSolveSet& S, int b, int nT, int n, int* s_last) {
+    if (threadIdx.x < 3 * n) __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int old = atomicAdd(&S.cnt[b], n);
+        *s_last = (old + n == nT);
+    }
+    __syncthreads();
+    return *s_last != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-system scalars, in float-float on the FP32 pipes (no FP64 on the
+// phase's critical path).  Records are read with L2 loads (__ldcg): they
+// are written by other blocks between phases.
+__device__ __forceinline__ ff to_ff(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ float2 to_f2(ff v) { return make_float2(v.hi, v.lo); }
+
 __device__ __forceinline__ SbSolveRec load_rec(const SbSolveRec* p) {
     SbSolveRec r;
     r.rz = __ldcg(&p->rz);
     r.rr = __ldcg(&p->rr);
-    r.bnorm = __ldcg(&p->bnorm);
+    r.bb = __ldcg(&p->bb);
     r.tol2 = __ldcg(&p->tol2);
     r.alpha = __ldcg(&p->alpha);
     r.beta = __ldcg(&p->beta);
@@ -514,11 +640,12 @@ __device__ __forceinline__ SbSolveRec load_rec(const SbSolveRec* p) {
     return r;
 }
 
-// Final statistics of a system that leaves the solve.
+// Final statistics of a system that leaves the solve (FP64, once).
 __device__ __forceinline__ void write_stats(SbDevStats* st, const SbSolveRec& rc) {
+    const double bb = ff_to_d(to_ff(rc.bb));
     st->solver_iters = rc.it;
-    st->solver_rel_resid = sqrt(rc.rr) / rc.bnorm;
-    st->solver_b_norm = rc.bnorm;
+    st->solver_rel_resid = sqrt(ff_to_d(to_ff(rc.rr)) / bb);
+    st->solver_b_norm = sqrt(bb);
     st->solver_converged = rc.conv;
 }
 
@@ -527,8 +654,8 @@ __device__ __forceinline__ void write_stats(SbDevStats* st, const SbSolveRec& rc
 // finished.
 template <bool MIXED>
 __device__ __forceinline__ bool loop_head(SbSolveRec& rc, const SolverConfig& cfg) {
-    if (rc.it >= cfg.max_iter || !(rc.rr == rc.rr)) return true;
-    if (rc.rr <= rc.tol2) {
+    if (rc.it >= cfg.max_iter || !(rc.rr.x == rc.rr.x)) return true;
+    if (ff_le(to_ff(rc.rr), to_ff(rc.tol2))) {
         if (!MIXED) {
             rc.conv = 1;
             return true;
@@ -540,24 +667,26 @@ __device__ __forceinline__ bool loop_head(SbSolveRec& rc, const SolverConfig& cf
     return false;
 }
 
-// Advances a system's scalars past phase p with its summed row partials
-// (A, B, C); returns true when the system is finished.
+// Advances a system's scalars past phase p with its exact sums (A, B, C);
+// returns true when the system is finished.
 //   p = 0 (set-up): A = r.z, B = r.r, C = |b|^2
 //   odd p:  iterate -> A = p.q;   check -> A = |r_true|^2
 //   even p: iterate -> A = r.z, B = r.r (after the update); restart -> same
 // Every path that advances a system (one block for a batch, every block
 // for a single system) runs this same function on the same sums.
 template <bool MIXED>
-__device__ __forceinline__ bool transition(SbSolveRec& rc, int p, double A, double B, double C,
+__device__ __forceinline__ bool transition(SbSolveRec& rc, int p, ff A, ff B, ff C,
                                            const SolverConfig& cfg) {
     if (p == 0) {
-        rc.bnorm = C > 0.0 ? sqrt(C) : 1.0;
-        // the FP64 iterate is driven to 0.8 tol so that the returned FP32
-        // gamma (whose rounding adds up to a few percent) still meets tol
-        rc.tol2 = (MIXED ? 0.64 : 1.0) * cfg.tol * cfg.tol * rc.bnorm * rc.bnorm;
-        rc.rz = A;
-        rc.rr = B;
-        rc.alpha = 0.0;
+        const ff bb = C.hi > 0.0f ? C : ff{1.0f, 0.0f};
+        rc.bb = to_f2(bb);
+        // tol2f = tol^2 (plain) or (0.8 tol)^2 (mixed: the float-float
+        // iterate is driven below tol so that the returned FP32 gamma, whose
+        // rounding adds up to a few percent, still meets tol)
+        rc.tol2 = to_f2(ff_mul_f(bb, cfg.tol2f));
+        rc.rz = to_f2(A);
+        rc.rr = to_f2(B);
+        rc.alpha = make_float2(0.0f, 0.0f);
         rc.beta = 0.0f;
         rc.it = 0;
         rc.conv = 0;
@@ -566,97 +695,65 @@ __device__ __forceinline__ bool transition(SbSolveRec& rc, int p, double A, doub
     }
     if (p & 1) {
         if (rc.state == ST_ITER) {
-            if (!(A > 0.0)) return true;  // breakdown: keep the current iterate
-            rc.alpha = rc.rz / A;
+            if (!(A.hi > 0.0f)) return true;  // breakdown: keep the current iterate
+            rc.alpha = to_f2(ff_div(to_ff(rc.rz), A));
             return false;
         }
-        rc.rr = A;
-        if (rc.rr <= rc.tol2) {
+        rc.rr = to_f2(A);
+        if (ff_le(A, to_ff(rc.tol2))) {
             rc.conv = 1;
             return true;
         }
         return false;  // restart from the refined iterate
     }
     if (rc.state == ST_ITER) {
-        rc.beta = (float)(A / rc.rz);
-        rc.rz = A;
-        rc.rr = B;
+        rc.beta = ff_to_f(ff_div(A, to_ff(rc.rz)));
+        rc.rz = to_f2(A);
+        rc.rr = to_f2(B);
         ++rc.it;
         return loop_head<MIXED>(rc, cfg);
     }
-    rc.rz = A;
-    rc.rr = B;
+    rc.rz = to_f2(A);
+    rc.rr = to_f2(B);
     rc.beta = 0.0f;
     rc.state = ST_ITER;
     return false;
 }
 
+// The three sums of buffer ab, for a whole block: warp 0 copies the buffer
+// with coalesced L2 loads (one request per line, where a load per word from
+// every block of the grid would queue on the same few lines), threads 0..2
+// convert one value each; the sums land in out[0..2] (shared memory) for
+// every thread after the call.
+__device__ __forceinline__ void acc_sums(const unsigned long long* ab, unsigned long long* s_w,
+                                         ff* out) {
+    if (threadIdx.x < 32) {
+        for (int k = threadIdx.x; k < kAccBuf; k += 32) s_w[k] = __ldcg(ab + k);
+        __syncwarp();
+        if (threadIdx.x < 3) out[threadIdx.x] = acc_ff(s_w + threadIdx.x * kAccWords);
+    }
+    __syncthreads();
+}
+
 // Thread 0 of the block that completed system b's last row in phase p
-// (sets of several systems): advance the system and publish its scalars
-// for phase p + 1, or retire it (from phase p + 1 on no block visits its
-// rows).
+// (sets of several systems): advance the system with the phase's sums and
+// publish its scalars for phase p + 1, or retire it (from phase p + 1 on no
+// block visits its rows).
 template <bool MIXED>
-__device__ __forceinline__ void advance(const SbSolveSet& S, int b, int p, double A, double B,
-                                        double C, const SolverConfig& cfg) {
+__device__ __forceinline__ void advance(const SbSolveSet& S, int b, int p, const ff* sums,
+                                        const SolverConfig& cfg) {
     SbSolveRec rc = load_rec(S.rec + (p & 1) * S.nb + b);
-    if (transition<MIXED>(rc, p, A, B, C, cfg)) {
+    if (transition<MIXED>(rc, p, sums[0], sums[1], sums[2], cfg)) {
         write_stats(S.descs[b]->f.stats, rc);
         S.done_at[b] = p + 1;
+        // retired: this block was the only reader of the system's buffers
+        acc_zero(S.acc + (size_t)b * kSolveAccWords, kSolveAccWords, 0, 1);
     } else {
         S.rec[((p + 1) & 1) * S.nb + b] = rc;
         if (p == 0) S.done_at[b] = INT_MAX;
+        acc_zero(acc_buf(S, b, p + 1), kAccBuf, 0, 1);  // read in phase p - 2
     }
     S.cnt[b] = 0;
-}
-
-// Sum of system b's row partials in row order (the same in every block).
-__device__ __forceinline__ void system_sum3(const SbSolveSet& S, int b, int nT, int parity,
-                                            double& A, double& B, double& C) {
-    const float2* p = S.rowpart + 3 * ((size_t)parity * S.R + S.roff[b]);
-    ff x = ff_zero(), y = ff_zero(), z = ff_zero();
-#pragma unroll 4
-    for (int i = threadIdx.x; i < nT; i += kSolveBlock) {
-        const float2 u = __ldcg(p + 3 * i), v = __ldcg(p + 3 * i + 1), w = __ldcg(p + 3 * i + 2);
-        x = ff_add(x, {u.x, u.y});
-        y = ff_add(y, {v.x, v.y});
-        z = ff_add(z, {w.x, w.y});
-    }
-    block_sum3(x, y, z);
-    A = ff_to_d(x);
-    B = ff_to_d(y);
-    C = ff_to_d(z);
-}
-
-// Rows [i, i + n) of system b were computed by this block; warp w left its
-// share of row i + k in s_part[k][w].  Folds every row's warp shares in warp
-// order into the row's partial, publishes the partials and counts the rows.
-// Returns (in every thread) whether these were the system's last rows.
-__device__ __forceinline__ bool publish_rows(const SbSolveSet& S, int b, int nT, int i, int n,
-                                             int parity, bool count, ff (*s_part)[kWarps][3],
-                                             int* s_last) {
-    __syncthreads();
-    if (threadIdx.x < n) {
-        ff x = ff_zero(), y = ff_zero(), z = ff_zero();
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            x = ff_add(x, s_part[threadIdx.x][w][0]);
-            y = ff_add(y, s_part[threadIdx.x][w][1]);
-            z = ff_add(z, s_part[threadIdx.x][w][2]);
-        }
-        float2* o = S.rowpart + 3 * ((size_t)parity * S.R + S.roff[b] + i + threadIdx.x);
-        o[0] = make_float2(x.hi, x.lo);
-        o[1] = make_float2(y.hi, y.lo);
-        o[2] = make_float2(z.hi, z.lo);
-        if (count) __threadfence();  // the partial before the count
-    }
-    __syncthreads();
-    if (!count) return false;
-    if (threadIdx.x == 0) {
-        const int old = atomicAdd(&S.cnt[b], n);
-        *s_last = (old + n == nT);
-    }
-    __syncthreads();
-    return *s_last != 0;
 }
 
 // Work weight of one theta row of a system with nT rows (nP = 2 nT columns
@@ -729,7 +826,7 @@ __device__ __forceinline__ void stage_desc(const SbSolveSet& S, int b, SbBubbleD
 template <bool MIXED, int PER>
 __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
                                           const SolverConfig& cfg, int i, int p, int state,
-                                          float beta, double alpha, float* pA, const float* pB,
+                                          float beta, ff alpha, float* pA, const float* pB,
                                           float* sm, Ring& R, ff* out) {
     ff a = ff_zero(), b2 = ff_zero(), c2 = ff_zero();
     float rv[PER];
@@ -760,9 +857,10 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
 // every phase the rows of the systems still iterating are split into G
 // contiguous ranges of equal work weight, one per block, so a block meets
 // one or two systems per phase and a system that iterates longer than the
-// others still spreads over the whole GPU.  Each block counts the rows it
-// finished per system; the block that completes a system sums its row
-// partials and advances it.  The loop ends when no system is left.
+// others still spreads over the whole GPU.  Each block adds its rows'
+// partials into the system's exact accumulator and counts the rows; the
+// block that completes a system reads the sums and advances it.  The loop
+// ends when no system is left.
 template <bool MIXED, int PER>
 __global__ void __launch_bounds__(kSolveBlock, 4)
 k_solve(SbSolveSet S, SolverConfig cfg) {
@@ -772,6 +870,9 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     __shared__ unsigned s_pre[kMaxSystems + 1];
     __shared__ ff s_part[kRowChunk][kWarps][3];
     __shared__ int s_last;
+    __shared__ unsigned long long s_w[kAccBuf];
+    __shared__ ff s_sums[3];
+    __shared__ SbSolveRec s_rc;
     int staged = -1;  // system whose descriptor is in s_d
     cg::grid_group grid = cg::this_grid();
     Ring R;
@@ -793,21 +894,32 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             const int i0 = lo > w0 ? (int)((lo - w0 + wr - 1) / wr) : 0;
             const int i1 = min(nT, (int)((hi - w0 + wr - 1) / wr));
             if (i0 >= i1) continue;
-            // the system's scalars, loaded while the descriptor is staged
-            int state = ST_ITER, it = 0;
-            float beta = 0.0f;
-            double alpha = 0.0;
-            if (p > 0) {
-                const SbSolveRec* rp = S.rec + (p & 1) * S.nb + b;
-                state = __ldcg(&rp->state);
-                it = __ldcg(&rp->it);
-                beta = __ldcg(&rp->beta);
-                alpha = __ldcg(&rp->alpha);
+            // the system's scalars (one thread loads them: every block of the
+            // grid reads the same record), staged with the descriptor
+            if (threadIdx.x == 0) {
+                SbSolveRec rc;
+                rc.state = ST_ITER;
+                rc.it = 0;
+                rc.beta = 0.0f;
+                rc.alpha = make_float2(0.0f, 0.0f);
+                if (p > 0) {
+                    const SbSolveRec* rp = S.rec + (p & 1) * S.nb + b;
+                    rc.state = __ldcg(&rp->state);
+                    rc.it = __ldcg(&rp->it);
+                    rc.beta = __ldcg(&rp->beta);
+                    rc.alpha = __ldcg(&rp->alpha);
+                }
+                s_rc = rc;
             }
             if (b != staged) {
                 stage_desc(S, b, &s_d);  // constant during the solve
                 staged = b;
+            } else {
+                __syncthreads();
             }
+            const int state = s_rc.state, it = s_rc.it;
+            const float beta = s_rc.beta;
+            const ff alpha = to_ff(s_rc.alpha);
             const SbGrid& g = s_d.g;
             const SbFields& f = s_d.f;
             float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
@@ -819,13 +931,15 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
                                       s_part[k][warp]);
                 // publish and count every kRowChunk rows and at the end; the
                 // block that completes the system advances it
-                if (k == kRowChunk - 1 || i == i1 - 1)
-                    last = publish_rows(S, b, nT, i - k, k + 1, p & 1, true, s_part, &s_last);
+                if (k == kRowChunk - 1 || i == i1 - 1) {
+                    publish_rows(S, b, p, k + 1, s_part);
+                    last = count_rows(S, b, nT, k + 1, &s_last);
+                }
             }
             if (last) {
-                double A, B, C;
-                system_sum3(S, b, nT, p & 1, A, B, C);
-                if (threadIdx.x == 0) advance<MIXED>(S, b, p, A, B, C, cfg);
+                __threadfence();
+                acc_sums(acc_buf(S, b, p), s_w, s_sums);
+                if (threadIdx.x == 0) advance<MIXED>(S, b, p, s_sums, cfg);
             }
             __syncthreads();  // s_d and s_last are reused
         }
@@ -852,12 +966,11 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
 // The solve of one system (a bubble stepped alone): the same phases, row
 // work and scalar transitions as k_solve, with the bubble's descriptor in
 // kernel parameters.  Rows are dealt round robin.  After every barrier each
-// block advances the scalars itself from the previous phase's row partials,
-// summed in row order like the publishing block of k_solve does, so no
-// block waits for another; row partials alternate between two buffers by
-// phase parity.  The results are bit-identical to solving the same system
-// inside a set (this file is compiled without multiply-add contraction, so
-// both kernels round the same operations the same way).
+// block reads the previous phase's exact sums and advances the scalars
+// itself, so no block waits for another.  The sums, and so every scalar and
+// result, are bit-identical to solving the same system inside a set (this
+// file is compiled without multiply-add contraction, so both kernels round
+// the same operations the same way).
 template <bool MIXED, int PER>
 __global__ void __launch_bounds__(kSolveBlock, 4)
 k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
@@ -869,52 +982,42 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     ring_init(R, bars, sm, cfg.ring);
     __shared__ SbSolveRec s_rc;  // the system's scalars (the same in every block)
     __shared__ int s_done;
+    __shared__ unsigned long long s_w[kAccBuf];
+    __shared__ ff s_sums[3];
     const int G = gridDim.x, nT = g.nT;
     const int warp = threadIdx.x >> 5;
     for (int p = 0;; ++p) {
         if (p > 0) {
-            double A, B, C;
-            system_sum3(S, 0, nT, (p - 1) & 1, A, B, C);
+            acc_sums(acc_buf(S, 0, p - 1), s_w, s_sums);
             if (threadIdx.x == 0) {
-                s_done = transition<MIXED>(s_rc, p - 1, A, B, C, cfg) ? 1 : 0;
+                s_done = transition<MIXED>(s_rc, p - 1, s_sums[0], s_sums[1], s_sums[2], cfg) ? 1 : 0;
                 if (s_done && blockIdx.x == 0) write_stats(f.stats, s_rc);
             }
             __syncthreads();
             if (s_done) break;  // same decision in every block
         }
+        // the buffer of phase p + 1 was last read at the start of phase p - 1
+        if (blockIdx.x == 0) acc_zero(acc_buf(S, 0, p + 1), kAccBuf, threadIdx.x, blockDim.x);
         const int state = s_rc.state, it = s_rc.it;
         const float beta = s_rc.beta;
-        const double alpha = s_rc.alpha;
+        const ff alpha = to_ff(s_rc.alpha);
         float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
         float* pB = (it & 1) ? f.p : f.q;  // p_old
-        int k = 0, first = blockIdx.x;
+        int k = 0;
         for (int i = blockIdx.x; i < nT; i += G) {
             row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, sm, R,
                                   s_part[k][warp]);
             ++k;
             if (k == kRowChunk || i + G >= nT) {
-                // fold and publish the chunk's rows first, first + G, ...
-                __syncthreads();
-                if (threadIdx.x < k) {
-                    ff x = ff_zero(), y = ff_zero(), z = ff_zero();
-#pragma unroll
-                    for (int w = 0; w < kWarps; ++w) {
-                        x = ff_add(x, s_part[threadIdx.x][w][0]);
-                        y = ff_add(y, s_part[threadIdx.x][w][1]);
-                        z = ff_add(z, s_part[threadIdx.x][w][2]);
-                    }
-                    float2* o = S.rowpart + 3 * ((size_t)(p & 1) * S.R + first + threadIdx.x * G);
-                    o[0] = make_float2(x.hi, x.lo);
-                    o[1] = make_float2(y.hi, y.lo);
-                    o[2] = make_float2(z.hi, z.lo);
-                }
-                __syncthreads();
+                publish_rows(S, 0, p, k, s_part);
                 k = 0;
-                first = i + G;
             }
         }
         grid.sync();
     }
+    // every block has read its last sums: clear the buffers for the next solve
+    grid.sync();
+    if (blockIdx.x == 0) acc_zero(S.acc, kSolveAccWords, threadIdx.x, blockDim.x);
     for (int i = blockIdx.x; i < nT; i += G) row_final<MIXED, PER>(g, f, i);
 }
 
@@ -936,6 +1039,11 @@ const void* solve_kernel(int per) {
         case 4: return (const void*)k_solve<MIXED, 4>;
         default: return (const void*)k_solve<MIXED, 8>;
     }
+}
+
+// Target r.r / |b|^2 of the iterate.
+float tol2_factor(const SolverConfig& cfg) {
+    return (float)((cfg.mode == 1 ? 0.64 : 1.0) * cfg.tol * cfg.tol);
 }
 
 int per_of(int nP) {
@@ -1018,6 +1126,7 @@ cudaError_t launch_solve_one(const SbGrid& g, const SbFields& f, const SbSolveSe
     SbSolveSet ss = set;
     SolverConfig cc = cfg;
     cc.ring = ring_depth(g.nP);
+    cc.tol2f = tol2_factor(cfg);
     void* args[] = {&gg, &ff, &ss, &cc};
     return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, true), dim3(G), dim3(kSolveBlock),
                                        args, solve_smem(g.nP), s);
@@ -1031,6 +1140,7 @@ cudaError_t launch_solve(const SbSolveSet& set, int maxNP, const SolverConfig& c
     SbSolveSet ss = set;
     SolverConfig cc = cfg;
     cc.ring = ring_depth(maxNP);
+    cc.tol2f = tol2_factor(cfg);
     void* args[] = {&ss, &cc};
     return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, false), dim3(G), dim3(kSolveBlock),
                                        args, solve_smem(maxNP), s);
