@@ -168,9 +168,7 @@ ArenaPlan plan_arena(const SbGrid& g) {
     a.r = a.L.take(N * F);
     a.z = a.L.take(N * F); a.p = a.L.take(N * F); a.q = a.L.take(N * F);
     a.xff = a.L.take(N * 8);
-    int lg = 0;
-    while ((1 << lg) < g.nP) ++lg;
-    a.pcr = a.L.take((size_t)lg * N * 8);  // <= log2(nP) - 1 levels + final factors
+    a.pcr = a.L.take((size_t)g.nT * factor_blob(g.nP).bytes);
     a.pcr_levels = a.L.take((size_t)g.nT * 4);
     a.self = a.L.take(sizeof(SbBubbleDesc));
     a.self_list = a.L.take(sizeof(SbBubbleDesc*));
@@ -379,7 +377,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.dmass = F32(a.dmass); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs); f.r0 = F32(a.r0);
     f.x = F32(a.x); f.dx = F32(a.dx); f.r = F32(a.r); f.z = F32(a.z); f.p = F32(a.p); f.q = F32(a.q);
     f.xff = (float2*)(A + a.xff);
-    f.pcr = (float2*)(A + a.pcr);
+    f.pcr = (float*)(A + a.pcr);
     f.pcr_levels = (int*)(A + a.pcr_levels);
     f.step = (SbStepParams*)(A + a.step);
     f.stats = (SbDevStats*)(A + a.stats);

@@ -9,6 +9,32 @@ namespace sb {
 struct SbBubbleDesc;
 struct SbSolveRec;
 
+// Byte layout of one row's phi-line preconditioner factors (sb_solver.cu)
+// for rows of n = nPhi columns (a power of two, >= 16): q = n / 4 reduced
+// equations and up to lp parallel-reduction levels.  Every offset is a
+// multiple of 16 bytes.
+struct SbFactorBlob {
+    int n, q, lp;
+    int cr1, cr2, pcr, fin, bs2, bs1, bytes;
+};
+
+__host__ __device__ inline SbFactorBlob factor_blob(int n) {
+    SbFactorBlob b;
+    b.n = n;
+    b.q = n / 4;
+    int lq = 0;
+    while ((1 << lq) < b.q) ++lq;
+    b.lp = lq > 1 ? lq - 1 : 0;
+    b.cr1 = 0;                      // float2 [n/2]
+    b.cr2 = 4 * n;                  // float2 [q]
+    b.pcr = 6 * n;                  // float2 [lp][q]
+    b.fin = b.pcr + 2 * n * b.lp;   // float2 [q]
+    b.bs2 = b.fin + 2 * n;          // float [3][q]
+    b.bs1 = b.bs2 + 3 * n;          // float [3][n/2]
+    b.bytes = b.bs1 + 6 * n;
+    return b;
+}
+
 // Every device array of one bubble.  Fields are FP32, row-major [theta][phi]
 // with row stride nPhi; u_theta has nTheta-1 rows.  "A" buffers hold the
 // state between steps, "adv" buffers the advected intermediate state.
@@ -28,7 +54,7 @@ struct SbFields {
     float *dmass, *cE, *cS, *rhs, *r0;
     float *x, *dx, *r, *z, *p, *q;                 // solver vectors
     float2 *xff;                                   // mixed-precision iterate (float-float)
-    float2 *pcr;                                   // phi-line factors, (log2 nPhi) x N
+    float *pcr;                                    // phi-line factors, one blob per row
     int *pcr_levels;                               // reduction levels per row
     // the bubble's own solve set (one system): its device descriptor and
     // the solver's per-row and per-system scratch (see SbSolveSet)
@@ -55,7 +81,7 @@ struct SolverConfig {
     int max_iter;
     double tol;     // relative residual ||b - A x|| / ||b||
     int precond;    // 0: Jacobi, 1: exact phi-line (periodic tridiagonal per row)
-    int ring;       // factor levels staged in shared memory at once (set at launch)
+    int blob;       // bytes of a block's shared-memory factor blob (set at launch)
     float tol2f;    // target r.r / |b|^2 of the iterate (set at launch)
 };
 

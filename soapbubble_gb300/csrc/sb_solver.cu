@@ -46,78 +46,85 @@ namespace {
 
 constexpr int kSolveBlock = 256;
 constexpr int kWarps = kSolveBlock / 32;  // row partials per row: one per warp
-constexpr int kMaxRing = 12;          // >= log2(nP) for every supported nP
 constexpr int kWaitPolls = 1 << 22;   // mbarrier polls before a copy counts as lost
 constexpr int kMaxSystems = 1024;     // systems of one solve set
 constexpr int kRowChunk = 16;         // rows a block publishes at a time
 enum { ST_ITER = 0, ST_CHECK = 1 };
 
 // ---------------------------------------------------------------------------
-// Shared-memory staging of the stored cyclic-reduction factors.  Each
-// (level, row) factor slice is nP contiguous float2 in global memory; one
-// thread copies it into one of K ring slots with a bulk asynchronous copy
-// (cp.async.bulk, completion counted on the slot's mbarrier), so the levels
-// of a row arrive together instead of one dependent load per level.
-struct Ring {
-    float2* buf;    // K slots of nP float2 at the start of dynamic shared memory
-    uint32_t bar;   // shared address of K mbarriers, 8 bytes apart
-    int K;
-    unsigned seq;   // slices issued (and waited for) by this block so far
+// Shared-memory copy of one row's preconditioner factors.  A block keeps
+// the factors of the row it last built or fetched; fetching another row's
+// factors is one bulk asynchronous copy (cp.async.bulk, completion counted
+// on an mbarrier), started before the row's update so that it lands while
+// the update runs.  When a block owns a single row for the whole solve the
+// factors never leave shared memory.
+struct Stage {
+    float* blob;           // factors of row `resident` (shared memory)
+    float* work;           // reduction work arrays (shared memory)
+    uint32_t bar;          // shared address of the mbarrier
+    unsigned copies;       // bulk copies issued (and waited for) so far
+    const float* resident; // global address of the factors in `blob`
+    bool pending;          // a copy into `blob` is in flight
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ void ring_init(Ring& R, uint64_t* bars, float* sm, int K) {
-    R.buf = reinterpret_cast<float2*>(sm);
-    R.bar = smem_u32(bars);
-    R.K = K;
-    R.seq = 0;
+__device__ __forceinline__ void stage_init(Stage& S, uint64_t* bar, float* sm, int blob_bytes) {
+    S.blob = sm;
+    S.work = sm + blob_bytes / 4;
+    S.bar = smem_u32(bar);
+    S.copies = 0;
+    S.resident = nullptr;
+    S.pending = false;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < K; ++s)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(R.bar + 8 * s) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(S.bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 }
 
-// Thread 0: start copying the slice `src` (n float2) into the slot of seq.
-__device__ __forceinline__ void ring_issue(const Ring& R, unsigned seq, const float2* src, int n) {
-    if (threadIdx.x != 0) return;
-    const unsigned s = seq % (unsigned)R.K;
-    const uint32_t bar = R.bar + 8 * s;
-    const uint32_t dst = smem_u32(R.buf + (size_t)s * n);
-    const uint32_t bytes = (uint32_t)n * 8u;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            dst),
-        "l"(src), "r"(bytes), "r"(bar)
-        : "memory");
+// Start copying the factors at `src` (bytes, a multiple of 16) unless they
+// are the block's resident ones.  Called by every thread with the same
+// arguments; every earlier read of the blob must be complete.
+__device__ __forceinline__ void stage_fetch(Stage& S, const float* src, int bytes) {
+    if (src == S.resident) return;
+    if (threadIdx.x == 0) {
+        // the block's generic reads of the blob come before the copy's writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(S.bar),
+                     "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(S.blob)),
+            "l"(src), "r"(bytes), "r"(S.bar)
+            : "memory");
+    }
+    S.resident = src;
+    S.pending = true;
 }
 
-// Every thread: wait (bounded) until the slice of seq has landed; returns
-// its slot.  A wait that gives up is counted in the stats, and the solve is
-// then reported as failed instead of hanging.
-__device__ __forceinline__ const float2* ring_wait(const Ring& R, unsigned seq, int n,
-                                                   SbDevStats* st) {
-    const unsigned s = seq % (unsigned)R.K;
-    const uint32_t bar = R.bar + 8 * s;
-    const uint32_t parity = (seq / (unsigned)R.K) & 1u;
+// Every thread: wait (bounded) for the copy in flight.  A wait that gives
+// up is counted in the stats, and the solve is then reported as failed
+// instead of hanging.
+__device__ __forceinline__ void stage_wait(Stage& S, SbDevStats* st) {
+    if (!S.pending) return;
+    const uint32_t parity = S.copies & 1u;
     for (int k = 0;; ++k) {
         uint32_t ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+            " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(S.bar), "r"(parity) : "memory");
         if (ok) break;
         if (k >= kWaitPolls) {
             if (threadIdx.x == 0) atomicAdd(&st->wait_faults, 1);
             break;
         }
     }
-    return R.buf + (size_t)s * n;
+    ++S.copies;
+    S.pending = false;
 }
 
 // ---------------------------------------------------------------------------
@@ -151,21 +158,42 @@ __device__ __forceinline__ ff acc(ff s, float a, float b) {
 // Column of element k of this thread in a row.
 __device__ __forceinline__ int col_of(int k) { return threadIdx.x + k * kSolveBlock; }
 
-// z = M^-1 r on theta row i: Jacobi, or the exact periodic tridiagonal solve.
-// rv[k] holds r at column col_of(k) (this thread's elements).  Adds the
-// row's r.z and r.r to rz, rr.  PER = equations per thread
+// z = M^-1 r on theta row i: Jacobi, or the exact solve of the row's
+// periodic tridiagonal block (phi couplings; the theta couplings stay on its
+// diagonal).  rv[k] holds r at column col_of(k) (this thread's elements).
+// Adds the row's r.z and r.r to rz, rr.  PER = equations per thread
 // (nP <= PER * kSolveBlock).
 //
-// The row matrix does not change during a solve, so the first application
-// (BUILD) runs the full cyclic reduction and stores, per level, the two
-// elimination factors of every equation (f.pcr) and the number of levels the
-// row needed (f.pcr_levels); later applications only replay
-// D' = D + a D[j - s] + c D[j + s] with the stored factors.
+// Row solve of n = nP equations (indices mod n) in excess form: equation j
+//   (E_j + L_j + U_j) x_j - L_j x_{j-s} - U_j x_{j+s} = D_j,  E, L, U >= 0,
+// at stride s = 1 to begin with:
+//   1. cyclic reduction at stride 1: every even equation absorbs its odd
+//      neighbours (D_j += a D_{j-1} + c D_{j+1}) and couples at stride 2;
+//   2. the same at stride 2 for the equations j = 0 mod 4;
+//   3. parallel cyclic reduction of the q = n/4 equations j = 0 mod 4 at
+//      strides 4, 8, .., n/4 (stopping once every coupling is below 2^-26
+//      of its excess, the row having decoupled to float precision), ending
+//      with 2 x 2 solves of j and j + n/2;
+//   4. back substitution of j = 2 mod 4 from their stride-2 equations, then
+//      of the odd j from the original ones: x_j = g D_j + a' x_{j-s} +
+//      b' x_{j+s} with g = 1 / diagonal and a' + b' < 1.
+// Every update of an excess or a right-hand side adds non-negative terms
+// (the Grassmann-Taksar-Heyman idea applied to cyclic reduction), so FP32
+// keeps full relative accuracy even when the diagonal exceeds the
+// off-diagonal sum by a factor 1 + 1e-5.  Steps 1, 2 and 4 are O(n) work and
+// step 3 O(n/4 log n), against O(n log n) for parallel reduction of the
+// whole row.
+//
+// The row matrix does not change during a solve: the first application
+// (BUILD) computes the factors of every step into the block's shared-memory
+// blob, copies the blob to the row's slot of f.pcr (layout factor_blob) and
+// records the levels of step 3 in f.pcr_levels; later applications replay
+// the right-hand-side updates with the factors (fetched by stage_fetch
+// unless the block still holds them), with the same arithmetic.
 template <bool MIXED, int PER, bool BUILD>
 __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f,
-                                                 const SolverConfig& cfg, int i, float* sm,
-                                                 Ring& R, const float (&rv)[PER], ff& rz,
-                                                 ff& rr) {
+                                                 const SolverConfig& cfg, int i, Stage& S,
+                                                 const float (&rv)[PER], ff& rz, ff& rr) {
     const int nP = g.nP, nT = g.nT, mask = g.maskP;
     const int row = i * nP;
     if (cfg.precond == 0) {
@@ -186,18 +214,26 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         }
         return;
     }
-    // factor storage of this row: level l at f.pcr[(l * nT + i) * nP + j]
-    const size_t lvl_stride = (size_t)nT * nP;
-    float2* fac = f.pcr + (size_t)row;
+    constexpr int H = PER >= 2 ? PER / 2 : 1;  // items per thread of the n/2-item steps
+    constexpr int Q = PER >= 4 ? PER / 4 : 1;  // and of the n/4-item steps
+    const SbFactorBlob B = factor_blob(nP);
+    const int n = nP, h = n / 2, q = B.q, qmask = q - 1;
+    char* const bl = reinterpret_cast<char*>(S.blob);
+    float2* const cr1 = reinterpret_cast<float2*>(bl + B.cr1);
+    float2* const cr2 = reinterpret_cast<float2*>(bl + B.cr2);
+    float2* const pcr = reinterpret_cast<float2*>(bl + B.pcr);
+    float2* const fin = reinterpret_cast<float2*>(bl + B.fin);
+    float* const g2 = reinterpret_cast<float*>(bl + B.bs2);  // [3][q]: g, a', b' of 4m + 2
+    float* const g1 = reinterpret_cast<float*>(bl + B.bs1);  // [3][h]: g, a', b' of 2m + 1
+    float* const D = S.work;                                  // right-hand side, then x
     if (BUILD) {
-        float* E = sm;            // excess: diagonal minus the phi couplings
-        float* L = sm + nP;       // |coupling to j - s|
-        float* U = sm + 2 * nP;   // |coupling to j + s|
-        float* D = sm + 3 * nP;   // right-hand side
+        float* const E = S.work + n;      // excess: diagonal minus the phi couplings
+        float* const L = S.work + 2 * n;  // coupling to j - s
+        float* const U = S.work + 3 * n;  // coupling to j + s
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int j = col_of(k);
-            if (j < nP) {
+            if (j < n) {
                 const int c = row + j;
                 float ex = f.dmass[c];
                 if (i < nT - 1) ex += f.cS[c];
@@ -209,131 +245,230 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
             }
         }
         __syncthreads();
-        // Parallel cyclic reduction: after the step with stride s every
-        // equation couples j to j -/+ 2s (indices mod nP).  It stops early
-        // once every coupling is below 2^-26 of its excess (the row has
-        // decoupled to float precision); otherwise it ends with 2 x 2
-        // solves of j and j + nP/2.
-        bool decoupled = false;
-        int levels = 0;
-        for (int s = 1; s <= nP / 4; s <<= 1) {
-            float nE[PER], nL[PER], nU[PER], nD[PER];
+        // step 1; an even entry is read only by its own thread: in place
 #pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int j = col_of(k);
-                if (j < nP) {
-                    const int jm = (j - s) & mask, jp = (j + s) & mask;
-                    const float bm = E[jm] + L[jm] + U[jm];
-                    const float bp = E[jp] + L[jp] + U[jp];
-                    // fast division: the preconditioner stays a fixed operator
-                    const float am = __fdividef(L[j], bm);
-                    const float cp = __fdividef(U[j], bp);
-                    fac[levels * lvl_stride + j] = make_float2(am, cp);
-                    nE[k] = E[j] + am * E[jm] + cp * E[jp];
-                    nL[k] = am * L[jm];
-                    nU[k] = cp * U[jp];
-                    nD[k] = D[j] + am * D[jm] + cp * D[jp];
-                }
+        for (int t = 0; t < H; ++t) {
+            const int m = threadIdx.x + t * kSolveBlock;
+            if (m < h) {
+                const int j = 2 * m, jm = (j - 1) & mask, jp = j + 1;
+                const float bm = E[jm] + L[jm] + U[jm];
+                const float bp = E[jp] + L[jp] + U[jp];
+                // fast division: the preconditioner stays a fixed operator
+                const float am = __fdividef(L[j], bm), cp = __fdividef(U[j], bp);
+                cr1[m] = make_float2(am, cp);
+                const float gi = __fdividef(1.0f, bp);  // odd equation jp
+                g1[m] = gi;
+                g1[h + m] = L[jp] * gi;
+                g1[2 * h + m] = U[jp] * gi;
+                const float nE = E[j] + am * E[jm] + cp * E[jp];
+                const float nL = am * L[jm], nU = cp * U[jp];
+                D[j] = D[j] + am * D[jm] + cp * D[jp];
+                E[j] = nE;
+                L[j] = nL;
+                U[j] = nU;
             }
-            __syncthreads();
-            bool need = false;
+        }
+        __syncthreads();
+        // step 2, into compact arrays (index m = j / 4) that reuse the space
+        // of E, L, U once every thread has read them
+        float sE[Q], sL[Q], sU[Q], sD[Q];
 #pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int j = col_of(k);
-                if (j < nP) {
-                    E[j] = nE[k]; L[j] = nL[k]; U[j] = nU[k]; D[j] = nD[k];
-                    need |= (nL[k] + nU[k]) > 1.4901161e-8f * nE[k];
+        for (int t = 0; t < Q; ++t) {
+            const int m = threadIdx.x + t * kSolveBlock;
+            if (m < q) {
+                const int j = 4 * m, jm = (j - 2) & mask, jp = j + 2;
+                const float bm = E[jm] + L[jm] + U[jm];
+                const float bp = E[jp] + L[jp] + U[jp];
+                const float am = __fdividef(L[j], bm), cp = __fdividef(U[j], bp);
+                cr2[m] = make_float2(am, cp);
+                const float gi = __fdividef(1.0f, bp);  // equation jp = 4m + 2
+                g2[m] = gi;
+                g2[q + m] = L[jp] * gi;
+                g2[2 * q + m] = U[jp] * gi;
+                sE[t] = E[j] + am * E[jm] + cp * E[jp];
+                sL[t] = am * L[jm];
+                sU[t] = cp * U[jp];
+                sD[t] = D[j] + am * D[jm] + cp * D[jp];
+            }
+        }
+        __syncthreads();
+        float* const P = S.work + n;  // two sets (E, L, U, D) of q entries
+        bool need = false;
+#pragma unroll
+        for (int t = 0; t < Q; ++t) {
+            const int m = threadIdx.x + t * kSolveBlock;
+            if (m < q) {
+                P[m] = sE[t];
+                P[q + m] = sL[t];
+                P[2 * q + m] = sU[t];
+                P[3 * q + m] = sD[t];
+                need |= (sL[t] + sU[t]) > 1.4901161e-8f * sE[t];
+            }
+        }
+        // step 3, ping-pong between the two sets
+        bool decoupled = !__syncthreads_or(need);
+        int levels = 0, cur = 0;
+        for (int s = 1; !decoupled && s <= q / 4; s <<= 1) {
+            const float* Ei = P + cur * 4 * q;
+            const float *Li = Ei + q, *Ui = Ei + 2 * q, *Di = Ei + 3 * q;
+            float* Eo = P + (cur ^ 1) * 4 * q;
+            need = false;
+#pragma unroll
+            for (int t = 0; t < Q; ++t) {
+                const int m = threadIdx.x + t * kSolveBlock;
+                if (m < q) {
+                    const int mm = (m - s) & qmask, mp = (m + s) & qmask;
+                    const float bm = Ei[mm] + Li[mm] + Ui[mm];
+                    const float bp = Ei[mp] + Li[mp] + Ui[mp];
+                    const float am = __fdividef(Li[m], bm), cp = __fdividef(Ui[m], bp);
+                    pcr[levels * q + m] = make_float2(am, cp);
+                    const float nE = Ei[m] + am * Ei[mm] + cp * Ei[mp];
+                    const float nL = am * Li[mm], nU = cp * Ui[mp];
+                    Eo[m] = nE;
+                    Eo[q + m] = nL;
+                    Eo[2 * q + m] = nU;
+                    Eo[3 * q + m] = Di[m] + am * Di[mm] + cp * Di[mp];
+                    need |= (nL + nU) > 1.4901161e-8f * nE;
                 }
             }
             ++levels;
-            if (!__syncthreads_or(need)) {
-                decoupled = true;
-                break;
-            }
+            cur ^= 1;
+            decoupled = !__syncthreads_or(need);
         }
         if (threadIdx.x == 0) f.pcr_levels[i] = decoupled ? levels : -levels;
+        // 2 x 2 solves of m and m + q/2 (or the decoupled diagonal): x at
+        // j = 4m, whose D entry is free since step 2
+        {
+            const float* Ef = P + cur * 4 * q;
+            const float *Lf = Ef + q, *Uf = Ef + 2 * q, *Df = Ef + 3 * q;
+#pragma unroll
+            for (int t = 0; t < Q; ++t) {
+                const int m = threadIdx.x + t * kSolveBlock;
+                if (m < q) {
+                    const int kk = (m + q / 2) & qmask;
+                    float c1, c2;
+                    if (decoupled) {
+                        c1 = 1.0f / (Ef[m] + Lf[m] + Uf[m]);
+                        c2 = 0.0f;
+                    } else {
+                        const float mj = Lf[m] + Uf[m], mk = Lf[kk] + Uf[kk];
+                        const float ej = Ef[m], ek = Ef[kk];
+                        const float idet = 1.0f / (ej * ek + ej * mk + mj * ek);
+                        c1 = (ek + mk) * idet;
+                        c2 = mj * idet;
+                    }
+                    fin[m] = make_float2(c1, c2);
+                    D[4 * m] = c1 * Df[m] + c2 * Df[kk];
+                }
+            }
+        }
+        __syncthreads();
+    } else {
+        // replay: the factors are in the blob (or on their way)
+        const int lv = f.pcr_levels[i];
+        const int levels = lv < 0 ? -lv : lv;
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int j = col_of(k);
-            if (j < nP) {
-                float c1, c2;
-                if (decoupled) {
-                    c1 = 1.0f / (E[j] + L[j] + U[j]);
-                    c2 = 0.0f;
-                } else {
-                    const int kk = (j + nP / 2) & mask;
-                    const float mj = L[j] + U[j], mk = L[kk] + U[kk];
-                    const float ej = E[j], ek = E[kk];
-                    const float idet = 1.0f / (ej * ek + ej * mk + mj * ek);
-                    c1 = (ek + mk) * idet;
-                    c2 = mj * idet;
-                }
-                fac[levels * lvl_stride + j] = make_float2(c1, c2);
-                const int kk = (j + nP / 2) & mask;
-                const float zj = c1 * D[j] + c2 * D[kk];
-                const float rc = rv[k];
-                f.z[row + j] = zj;
-                rz = acc<MIXED>(rz, rc, zj);
-                rr = acc<MIXED>(rr, rc, rc);
+            if (j < n) D[j] = rv[k];
+        }
+        stage_wait(S, f.stats);
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < H; ++t) {
+            const int m = threadIdx.x + t * kSolveBlock;
+            if (m < h) {
+                const int j = 2 * m;
+                const float2 c = cr1[m];
+                D[j] = D[j] + c.x * D[(j - 1) & mask] + c.y * D[j + 1];
             }
         }
-        // the factors written here (global) and the E, L, U, D arrays
-        // (shared, where the ring slots will land) are next touched by bulk
-        // asynchronous copies: order these generic writes before them
-        asm volatile("fence.proxy.async.global;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        return;
-    }
-    // replay with the stored factors: the row's slices stream into the
-    // shared-memory ring (all of them at once when the ring is deep enough);
-    // D ping-pongs between two buffers behind the ring
-    float* D0 = sm + 2 * R.K * nP;
-    float* D1 = D0 + nP;
-    const int lv = f.pcr_levels[i];
-    const int levels = lv < 0 ? -lv : lv;
-    const int nbuf = levels + 1;  // reduction levels + final factors
-    const unsigned base = R.seq;
-    for (int l = 0; l < nbuf && l < R.K; ++l) ring_issue(R, base + l, fac + l * lvl_stride, nP);
+        float* Pi = S.work + n;
+        float* Po = Pi + q;
 #pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
-        if (j < nP) D0[j] = rv[k];
+        for (int t = 0; t < Q; ++t) {
+            const int m = threadIdx.x + t * kSolveBlock;
+            if (m < q) {
+                const int j = 4 * m;
+                const float2 c = cr2[m];
+                Pi[m] = D[j] + c.x * D[(j - 2) & mask] + c.y * D[j + 2];
+            }
+        }
+        __syncthreads();
+        for (int l = 0, s = 1; l < levels; ++l, s <<= 1) {
+#pragma unroll
+            for (int t = 0; t < Q; ++t) {
+                const int m = threadIdx.x + t * kSolveBlock;
+                if (m < q) {
+                    const float2 c = pcr[l * q + m];
+                    Po[m] = Pi[m] + c.x * Pi[(m - s) & qmask] + c.y * Pi[(m + s) & qmask];
+                }
+            }
+            __syncthreads();
+            float* tmp = Pi;
+            Pi = Po;
+            Po = tmp;
+        }
+#pragma unroll
+        for (int t = 0; t < Q; ++t) {
+            const int m = threadIdx.x + t * kSolveBlock;
+            if (m < q) {
+                const float2 c = fin[m];
+                D[4 * m] = c.x * Pi[m] + c.y * Pi[(m + q / 2) & qmask];
+            }
+        }
+        __syncthreads();
+    }
+    // step 4 (both paths)
+#pragma unroll
+    for (int t = 0; t < Q; ++t) {
+        const int m = threadIdx.x + t * kSolveBlock;
+        if (m < q) {
+            const int j = 4 * m + 2;
+            D[j] = g2[m] * D[j] + g2[q + m] * D[j - 2] + g2[2 * q + m] * D[(j + 2) & mask];
+        }
     }
     __syncthreads();
-    int s = 1;
-    for (int l = 0; l < levels; ++l, s <<= 1) {
-        const float2* ac = ring_wait(R, base + l, nP, f.stats);
-        const float* Din = (l & 1) ? D1 : D0;
-        float* Dout = (l & 1) ? D0 : D1;
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int j = col_of(k);
-            if (j < nP) {
-                const float2 c = ac[j];
-                Dout[j] = Din[j] + c.x * Din[(j - s) & mask] + c.y * Din[(j + s) & mask];
-            }
+    for (int t = 0; t < H; ++t) {
+        const int m = threadIdx.x + t * kSolveBlock;
+        if (m < h) {
+            const int j = 2 * m + 1;
+            D[j] = g1[m] * D[j] + g1[h + m] * D[j - 1] + g1[2 * h + m] * D[(j + 1) & mask];
         }
-        __syncthreads();
-        // slot of level l is free again
-        if (l + R.K < nbuf) ring_issue(R, base + l + R.K, fac + (l + R.K) * lvl_stride, nP);
     }
-    const float2* fin = ring_wait(R, base + levels, nP, f.stats);
-    const float* Dn = (levels & 1) ? D1 : D0;
+    __syncthreads();
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int j = col_of(k);
-        if (j < nP) {
-            const float2 cc = fin[j];
-            const float zj = cc.x * Dn[j] + cc.y * Dn[(j + nP / 2) & mask];
+        if (j < n) {
+            const float zj = D[j];
             const float rc = rv[k];
             f.z[row + j] = zj;
             rz = acc<MIXED>(rz, rc, zj);
             rr = acc<MIXED>(rr, rc, rc);
         }
     }
-    __syncthreads();
-    R.seq = base + nbuf;
+    if (BUILD) {
+        // the row's factors to its global slot, for fetches by any block in
+        // later phases; the blob is the block's resident copy
+        float* const dst = f.pcr + (size_t)i * (B.bytes / 4);
+        const float4* src = reinterpret_cast<const float4*>(S.blob);
+        for (int k = threadIdx.x; k < B.bytes / 16; k += kSolveBlock)
+            reinterpret_cast<float4*>(dst)[k] = src[k];
+        S.resident = dst;
+        // generic writes of both copies before later bulk copies from the
+        // global slot and into the blob
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();  // blob and work arrays are free again
+}
+
+// Global slot of row i's factors.
+__device__ __forceinline__ const float* row_blob(const SbGrid& g, const SbFields& f, int i) {
+    return f.pcr + (size_t)i * (factor_blob(g.nP).bytes / 4);
 }
 
 // ---------------------------------------------------------------------------
@@ -827,19 +962,21 @@ template <bool MIXED, int PER>
 __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
                                           const SolverConfig& cfg, int i, int p, int state,
                                           float beta, ff alpha, float* pA, const float* pB,
-                                          float* sm, Ring& R, ff* out) {
+                                          Stage& St, ff* out) {
     ff a = ff_zero(), b2 = ff_zero(), c2 = ff_zero();
     float rv[PER];
     if (p == 0) {
         row_init<MIXED, PER>(g, f, i, rv, c2);
-        precondition_row<MIXED, PER, true>(g, f, cfg, i, sm, R, rv, a, b2);
+        precondition_row<MIXED, PER, true>(g, f, cfg, i, St, rv, a, b2);
     } else if (p & 1) {
         if (state == ST_ITER) a = row_spmv<MIXED, PER>(g, f, i, beta, pB, pA);
         else if (MIXED) a = row_true_residual<PER>(g, f, i);
     } else {
+        // the row's factors travel while the update runs
+        if (cfg.precond != 0) stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
         if (state == ST_ITER) row_update<MIXED, PER>(g, f, i, alpha, pA, rv);
         else row_load_r<PER>(g, f, i, rv);
-        precondition_row<MIXED, PER, false>(g, f, cfg, i, sm, R, rv, a, b2);
+        precondition_row<MIXED, PER, false>(g, f, cfg, i, St, rv, a, b2);
     }
     a = ff_warp_sum(a);
     b2 = ff_warp_sum(b2);
@@ -865,7 +1002,7 @@ template <bool MIXED, int PER>
 __global__ void __launch_bounds__(kSolveBlock, 4)
 k_solve(SbSolveSet S, SolverConfig cfg) {
     extern __shared__ __align__(16) float sm[];
-    __shared__ __align__(8) uint64_t bars[kMaxRing];
+    __shared__ __align__(8) uint64_t bar;
     __shared__ __align__(16) SbBubbleDesc s_d;
     __shared__ unsigned s_pre[kMaxSystems + 1];
     __shared__ ff s_part[kRowChunk][kWarps][3];
@@ -875,8 +1012,8 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     __shared__ SbSolveRec s_rc;
     int staged = -1;  // system whose descriptor is in s_d
     cg::grid_group grid = cg::this_grid();
-    Ring R;
-    ring_init(R, bars, sm, cfg.ring);
+    Stage St;
+    stage_init(St, &bar, sm, cfg.blob);
     const unsigned G = gridDim.x;
     const int warp = threadIdx.x >> 5;
 
@@ -927,7 +1064,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             bool last = false;
             for (int i = i0; i < i1; ++i) {
                 const int k = (i - i0) % kRowChunk;
-                row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, sm, R,
+                row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St,
                                       s_part[k][warp]);
                 // publish and count every kRowChunk rows and at the end; the
                 // block that completes the system advances it
@@ -975,11 +1112,11 @@ template <bool MIXED, int PER>
 __global__ void __launch_bounds__(kSolveBlock, 4)
 k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     extern __shared__ __align__(16) float sm[];
-    __shared__ __align__(8) uint64_t bars[kMaxRing];
+    __shared__ __align__(8) uint64_t bar;
     __shared__ ff s_part[kRowChunk][kWarps][3];
     cg::grid_group grid = cg::this_grid();
-    Ring R;
-    ring_init(R, bars, sm, cfg.ring);
+    Stage St;
+    stage_init(St, &bar, sm, cfg.blob);
     __shared__ SbSolveRec s_rc;  // the system's scalars (the same in every block)
     __shared__ int s_done;
     __shared__ unsigned long long s_w[kAccBuf];
@@ -1005,7 +1142,7 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
         float* pB = (it & 1) ? f.p : f.q;  // p_old
         int k = 0;
         for (int i = blockIdx.x; i < nT; i += G) {
-            row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, sm, R,
+            row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St,
                                   s_part[k][warp]);
             ++k;
             if (k == kRowChunk || i + G >= nT) {
@@ -1051,25 +1188,12 @@ int per_of(int nP) {
     return per <= 1 ? 1 : per <= 2 ? 2 : per <= 4 ? 4 : 8;
 }
 
-// Shared memory of one solve block: the factor ring (K slices of nP
-// float2) plus two nP-float buffers, or the four nP-float arrays of the
-// preconditioner build, whichever is larger.  K is as deep as fits while
-// four 256-thread blocks share an SM (228 KB: up to about 46 KB dynamic each
-// next to ~8 KB of static shared memory), at least 2 and at most the
-// log2(nP) slices a row can have.
-constexpr int kSolveSmemBudget = 46 * 1024;
-
-int ring_depth(int nP) {
-    int lg = 0;
-    while ((1 << lg) < nP) ++lg;
-    const int K = (kSolveSmemBudget - 8 * nP) / (8 * nP);
-    return std::max(2, std::min(K, std::min(lg, kMaxRing)));
-}
-
-size_t solve_smem(int nP) {
-    const int K = ring_depth(nP);
-    return std::max<size_t>(16 * (size_t)nP, 8 * (size_t)K * nP + 8 * (size_t)nP);
-}
+// Dynamic shared memory of one solve block for rows of up to nP columns:
+// the factor blob of one row and the four nP-float work arrays of the
+// preconditioner build (the replay needs 1.5 nP floats).  For nP = 1024
+// that is 47 KB, so four 256-thread blocks share an SM next to their
+// static shared memory.
+size_t solve_smem(int nP) { return (size_t)factor_blob(nP).bytes + 16 * (size_t)nP; }
 
 const void* kernel_for(int per, int mode, bool one) {
     if (one) return mode == 1 ? solve_one_kernel<true>(per) : solve_one_kernel<false>(per);
@@ -1125,7 +1249,7 @@ cudaError_t launch_solve_one(const SbGrid& g, const SbFields& f, const SbSolveSe
     SbFields ff = f;
     SbSolveSet ss = set;
     SolverConfig cc = cfg;
-    cc.ring = ring_depth(g.nP);
+    cc.blob = factor_blob(g.nP).bytes;
     cc.tol2f = tol2_factor(cfg);
     void* args[] = {&gg, &ff, &ss, &cc};
     return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, true), dim3(G), dim3(kSolveBlock),
@@ -1139,7 +1263,7 @@ cudaError_t launch_solve(const SbSolveSet& set, int maxNP, const SolverConfig& c
     const int G = std::min(set.R, max_blocks(per, cfg.mode, false));
     SbSolveSet ss = set;
     SolverConfig cc = cfg;
-    cc.ring = ring_depth(maxNP);
+    cc.blob = factor_blob(maxNP).bytes;
     cc.tol2f = tol2_factor(cfg);
     void* args[] = {&ss, &cc};
     return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, false), dim3(G), dim3(kSolveBlock),
