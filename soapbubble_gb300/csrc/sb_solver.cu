@@ -26,10 +26,13 @@
 // even when the diagonal exceeds the off-diagonal sum by a factor 1 + 1e-5
 // (the Grassmann-Taksar-Heyman idea applied to cyclic reduction).
 //
-// Modes: plain FP32 (FP32 vectors and sums), or mixed precision (FP32 SpMV
-// and preconditioner, FP64 iterate and dot products, and a true FP64
-// residual check that restarts CG from the refined iterate until the
-// relative residual target holds).
+// Modes: plain FP32 (FP32 iterate, float products), or mixed precision
+// (FP32 SpMV and preconditioner, float-float iterate, exact products in the
+// dot products, and a float-float true-residual check that restarts CG from
+// the refined iterate until the relative residual target holds).  Dot
+// products are summed in float-float within a row and exactly across rows.
+// (Rounding the products, as plain mode does, costs the mixed mode about a
+// fifth more iterations on ruptured films.)
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -501,34 +504,41 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
 
 // p_new = z + beta p_old on the row and, on the fly, on the neighbours it
 // reads (so no barrier is needed between forming p and using it); q = A p_new
-// is kept in f.x.  Returns the row's p.q.
+// is kept in f.x.  Returns the row's p.q.  Every load of a column is issued
+// before its arithmetic, through restrict-qualified pointers so that the
+// compiler may also start the next column's loads early.
 template <bool MIXED, int PER>
 __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i, float beta,
-                                           const float* __restrict__ pold,
-                                           float* __restrict__ pnew) {
+                                       const float* __restrict__ pold, float* __restrict__ pnew) {
     const int nP = g.nP, nT = g.nT, row = i * nP;
     const float* __restrict__ z = f.z;
+    const float* __restrict__ dmass = f.dmass;
+    const float* __restrict__ cE = f.cE;
+    const float* __restrict__ cS = f.cS;
+    float* __restrict__ qout = f.x;
+    const bool hasS = i < nT - 1, hasN = i > 0;
     ff pq = ff_zero();
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int j = col_of(k);
+        const int jj = j < nP ? j : 0;  // rows shorter than the block: a valid dummy
+        const int c = row + jj;
+        const int e = row + ((jj + 1) & g.maskP);
+        const int w = row + ((jj - 1) & g.maskP);
+        const int sc = hasS ? c + nP : c, nc = hasN ? c - nP : c;
+        const float zc = z[c], pc0 = pold[c];
+        const float ze = z[e], pe = pold[e], zw = z[w], pw = pold[w];
+        const float zs = z[sc], ps = pold[sc], zn = z[nc], pn = pold[nc];
+        const float dm = dmass[c], ce = cE[c], cw = cE[w];
+        const float cs = hasS ? cS[c] : 0.0f;
+        const float cn = hasN ? cS[nc] : 0.0f;
         if (j < nP) {
-            const int c = row + j;
-            const int e = row + ((j + 1) & g.maskP);
-            const int w = row + ((j - 1) & g.maskP);
-            const float pc = z[c] + beta * pold[c];
-            float qf = f.dmass[c] * pc + f.cE[c] * (pc - (z[e] + beta * pold[e])) +
-                       f.cE[w] * (pc - (z[w] + beta * pold[w]));
-            if (i < nT - 1) {
-                const int sc = c + nP;
-                qf += f.cS[c] * (pc - (z[sc] + beta * pold[sc]));
-            }
-            if (i > 0) {
-                const int nc = c - nP;
-                qf += f.cS[nc] * (pc - (z[nc] + beta * pold[nc]));
-            }
+            const float pc = zc + beta * pc0;
+            float qf = dm * pc + ce * (pc - (ze + beta * pe)) + cw * (pc - (zw + beta * pw));
+            if (hasS) qf += cs * (pc - (zs + beta * ps));
+            if (hasN) qf += cn * (pc - (zn + beta * pn));
             pnew[c] = pc;
-            f.x[c] = qf;
+            qout[c] = qf;
             pq = acc<MIXED>(pq, pc, qf);
         }
     }
@@ -556,27 +566,39 @@ __device__ __forceinline__ ff row_true_residual(const SbGrid& g, const SbFields&
     return a;
 }
 
-// x += alpha p_new, r -= alpha q; rv = the new r.
+// x += alpha p_new, r -= alpha q; rv = the new r.  Every load of the
+// thread's columns is issued before any arithmetic.
 template <bool MIXED, int PER>
 __device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, int i, ff alpha,
                                            const float* __restrict__ pnew, float (&rv)[PER]) {
     const int nP = g.nP, row = i * nP;
     const float af = ff_to_f(alpha);
     const ff a2 = alpha;
+    float pc[PER], rc[PER], qc[PER];
+    float2 xc[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        const int c = row + (j < nP ? j : 0);
+        pc[k] = pnew[c];
+        rc[k] = f.r[c];
+        qc[k] = f.x[c];
+        if (MIXED) xc[k] = f.xff[c];
+        else xc[k].x = f.dx[c];
+    }
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int j = col_of(k);
         rv[k] = 0.0f;
         if (j < nP) {
             const int c = row + j;
-            const float pc = pnew[c];
             if (MIXED) {
-                const ff x = ff_add(ld_ff(f.xff, c), ff_mul_f(a2, pc));
+                const ff x = ff_add({xc[k].x, xc[k].y}, ff_mul_f(a2, pc[k]));
                 f.xff[c] = make_float2(x.hi, x.lo);
             } else {
-                f.dx[c] += af * pc;
+                f.dx[c] = xc[k].x + af * pc[k];
             }
-            rv[k] = f.r[c] - af * f.x[c];
+            rv[k] = rc[k] - af * qc[k];
             f.r[c] = rv[k];
         }
     }
@@ -978,9 +1000,10 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
         else row_load_r<PER>(g, f, i, rv);
         precondition_row<MIXED, PER, false>(g, f, cfg, i, St, rv, a, b2);
     }
+    // warp sums of the values the phase produces (the others are zero)
     a = ff_warp_sum(a);
-    b2 = ff_warp_sum(b2);
-    c2 = ff_warp_sum(c2);
+    if (!(p & 1)) b2 = ff_warp_sum(b2);
+    if (p == 0) c2 = ff_warp_sum(c2);
     if ((threadIdx.x & 31) == 0) {
         out[0] = a;
         out[1] = b2;
