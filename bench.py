@@ -55,6 +55,11 @@ ALG_BYTES_PER_CELL = {
     "k_reinit": 0,        # no traffic unless re-initialising (about 1 step in 10)
 }
 PCG_BYTES_FIXED, PCG_BYTES_PER_ITER = 84, 80
+ROOFLINE_NOTES = {
+    "k_solve": "latency-bound, not HBM-bound: the solve's vectors and factors stay in L2 and in "
+               "shared memory across its iterations (DRAM traffic per launch is their first touch "
+               "and does not grow with the iteration count); two grid barriers per CG iteration",
+}
 
 
 def load_peaks():
@@ -156,14 +161,22 @@ def max_over_ranks(x: float, dist) -> float:
     return float(t.item())
 
 
+def state_mb() -> float:
+    from soapbubble_gb300.bubble import bytes_required, make_params
+    return bytes_required(make_params(NTHETA, DT)) / 1e6
+
+
 def workload_config(extra=None):
     c = {"workload": "c1: single bubble, lat-long MAC grid 512 x 1024, radius 1, dt 0.002 s, "
                      "thickness 1+0.2*SH(8..32), surfactant 1+0.01*U(-1,1), wind max speed 1, "
                      "mixed-precision PCG to relative residual 1e-6",
          "nTheta": NTHETA, "nPhi": 2 * NTHETA, "cells": NTHETA * 2 * NTHETA, "dt": DT,
-         "steps_per_frame": STEPS_PER_FRAME, "solver": "mixed FP32/FP64 PCG, phi-line preconditioner",
+         "steps_per_frame": STEPS_PER_FRAME,
+         "solver": "mixed-precision PCG (float-float iterate and scalars, exact dot-product sums, "
+                   "float-float true-residual refinement), phi-line preconditioner",
          "solver_tol": 1e-6, "seed": SEED,
-         "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); state ~105 MB"}
+         "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); "
+               f"state {state_mb():.0f} MB per bubble"}
     if extra:
         c.update(extra)
     return c
@@ -286,6 +299,12 @@ def run_ours(args):
     achieved = per_launch_bytes / avg_launch_s / 1e9
     peak, peak_kind = load_peaks()
     traffic = load_traffic().get(dom)
+    # every stage against the same HBM peak (algorithmic bytes / live time)
+    stage_roofline = {}
+    for k_, n_ in enumerate(names):
+        if stage_ms[k_] > 0 and alg.get(n_, 0) > 0:
+            gbs = alg[n_] * N / (stage_ms[k_] / 1e3 / kr) / 1e9
+            stage_roofline[n_] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
     stage_total = float(stage_ms.sum())
     stage_share = {n: round(float(m / stage_total), 4) for n, m in zip(names, stage_ms)}
     stage_us = {n: round(float(1e3 * m / kr), 2) for n, m in zip(names, stage_ms)}
@@ -355,7 +374,9 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes_per_launch": per_launch_bytes,
-                         "avg_launch_us": avg_launch_s * 1e6},
+                         "avg_launch_us": avg_launch_s * 1e6,
+                         "note": ROOFLINE_NOTES.get(dom, "")},
+            "stage_roofline": stage_roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
                     "same_steps_as_value": same,
