@@ -51,7 +51,8 @@ ALG_BYTES_PER_CELL = {
     "k_bimocq": 40,       # eta,bwd',bwdprev,init,delta,initLast,deltaLast -> eta'
     "k_assemble": 44,     # eta',gamma',u_th',u_ph',uair,vair -> dmass,cE,cS,r0,b
     "k_post": 56,         # gamma',x,dx,eta',u_th',u_ph',uair,vair -> gamma,dgamma,eta,deta,u_th,u_ph
-    "k_accum": 40,        # eta_delta,gamma_delta,fwd',bwd',deta,dgamma -> eta_delta,gamma_delta
+    "k_accum": 64,        # eta_delta,gamma_delta,fwd',bwd',deta,dgamma,eta,gamma,eta_init,gamma_init
+                          # -> eta_delta,gamma_delta,err_eta,err_gamma
     "k_reinit": 0,        # no traffic unless re-initialising (about 1 step in 10)
 }
 PCG_BYTES_FIXED, PCG_BYTES_PER_ITER = 84, 80
@@ -351,7 +352,7 @@ def run_ours(args):
                "sample": f"{n} steps of the same 512x1024 workload (FP64 oracle, OpenMP "
                          f"{threads} threads, PCG to 1e-6), {el:.1f} s"}
 
-    ensemble = serving = None
+    ensemble = serving = storage = None
     if rank == 0 and world == 1:
         h_u.free(); h_v.free(); h_eta.free(); flush.free()
         gb.close()
@@ -363,6 +364,9 @@ def run_ours(args):
             serving = serve.serve(args.serve_requests, 20.0, device=local)
             serving["sample"] = (f"first {args.serve_requests} requests of the seeded stream "
                                  "(python -m soapbubble_gb300.serve runs all 2000)")
+        if args.storage_steps > 0:
+            from soapbubble_gb300 import storage as stor
+            storage = stor.compare(steps=args.storage_steps, device=local, peak_gbs=peak)
 
     if rank == 0:
         line = {
@@ -391,6 +395,7 @@ def run_ours(args):
             "reinits": int(final.reinits), "result_finite": finite,
             "ensemble": ensemble,
             "serving": serving,
+            "storage_c2": storage,
         }
         print(json.dumps(line), flush=True)
     if gb is not None:
@@ -415,6 +420,8 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=200)
     # a sample of the serving stream (requests; 0 skips)
     ap.add_argument("--serve-requests", type=int, default=100)
+    # c2 (1024 x 2048) with FP32 and with BF16 field storage (steps; 0 skips)
+    ap.add_argument("--storage-steps", type=int, default=100)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

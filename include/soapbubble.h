@@ -58,13 +58,20 @@ typedef struct {
     /* extensions (zero selects the default) */
     double gs_scale;      /* multiplies the nondimensional gravity (0 -> 1) */
     double M_scale;       /* multiplies the Marangoni coefficient M (0 -> 1) */
-    int solver_mode;      /* 0: mixed precision (FP64 dots + refinement), 1: plain FP32 */
+    int solver_mode;      /* 0: mixed precision (float-float iterate, exact dot-product sums,
+                             true-residual refinement), 1: plain FP32 */
     double solver_tol;    /* relative residual target (0 -> 1e-6) */
     int solver_max_iter;  /* (0 -> 1000) */
     int force_reinit;     /* 0: decide by distortion > 4; 1: never; 2: every step */
     double nu_scale;      /* multiplies the air's kinematic viscosity in the drag
                              coefficient Cr (0 -> 1) */
+    int storage;          /* SB_STORE_FP32 (0) or SB_STORE_BF16 (1): storage of the thickness
+                             and surfactant fields between steps (eta, gamma and the BIMOCQ
+                             reference fields *_init, *_init_last; the *_delta accumulators
+                             stay FP32); arithmetic is FP32 either way */
 } sb_params;
+
+enum { SB_STORE_FP32 = 0, SB_STORE_BF16 = 1 };
 
 /* Diagnostics of the most recent step (the reference prints these:
  * kernel/solver.cu:282, kernel/bubble.cu:1495-1497, solver.cu:592). */

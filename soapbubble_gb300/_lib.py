@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsoapbubble_gb300.so")
 
 SB_OK, SB_ERR_INVALID, SB_ERR_CUDA, SB_ERR_OOM, SB_ERR_NOT_CONVERGED, SB_ERR_BROKEN, SB_ERR_IO = range(7)
+SB_STORE_FP32, SB_STORE_BF16 = 0, 1
 
 FIELDS = ["eta", "gamma", "u_theta", "u_phi",
           "eta_init", "eta_delta", "eta_init_last", "eta_delta_last",
@@ -29,7 +30,7 @@ class SbParams(C.Structure):
         ("blendCoeff", C.c_double), ("device", C.c_int),
         ("gs_scale", C.c_double), ("M_scale", C.c_double), ("solver_mode", C.c_int),
         ("solver_tol", C.c_double), ("solver_max_iter", C.c_int), ("force_reinit", C.c_int),
-        ("nu_scale", C.c_double),
+        ("nu_scale", C.c_double), ("storage", C.c_int),
     ]
 
 

@@ -33,7 +33,7 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
                 DT: Optional[float] = None, frames: int = 1, solver_mode: int = 0,
                 solver_tol: float = 1e-6, solver_max_iter: int = 1000, force_reinit: int = 0,
                 gs_scale: float = 0.0, M_scale: float = 0.0, nu_scale: float = 0.0,
-                device: int = 0) -> SbParams:
+                device: int = 0, storage: int = 0) -> SbParams:
     p = default_params()
     p.nTheta, p.dt, p.radius, p.H, p.Gamma_m, p.T = nTheta, dt, radius, H, Gamma_m, T
     p.blendCoeff = blendCoeff
@@ -42,6 +42,7 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
     p.solver_mode, p.solver_tol, p.solver_max_iter = solver_mode, solver_tol, solver_max_iter
     p.force_reinit, p.gs_scale, p.M_scale, p.device = force_reinit, gs_scale, M_scale, device
     p.nu_scale = nu_scale
+    p.storage = storage  # 0: FP32, 1: BF16 thickness / surfactant fields
     return p
 
 

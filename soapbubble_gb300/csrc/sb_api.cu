@@ -69,6 +69,7 @@ struct sb_bubble {
     SbFields f;
     SolverConfig solver;
     int force_reinit;  // -1 decide, 0 never, 1 always
+    int storage;       // kStoreF32 / kStoreBF16 (thickness and surfactant fields)
     int device;
     cudaStream_t stream = nullptr;
     char* arena = nullptr;
@@ -84,6 +85,8 @@ struct sb_bubble {
     SbBubbleDesc desc{};               // host copy of the bubble's descriptor
     cudaGraphExec_t graph = nullptr;   // one captured step
 };
+
+static_assert(SB_STORE_FP32 == kStoreF32 && SB_STORE_BF16 == kStoreBF16, "storage codes");
 
 namespace {
 
@@ -147,15 +150,21 @@ struct ArenaPlan {
     size_t tiles[3];                                           // its cell tiles
 };
 
-ArenaPlan plan_arena(const SbGrid& g) {
+// Bytes of one stored thickness / surfactant element.
+size_t scalar_bytes(int storage) { return storage == kStoreBF16 ? 2 : 4; }
+
+ArenaPlan plan_arena(const SbGrid& g, int storage) {
     ArenaPlan a;
     const size_t N = (size_t)g.N, Nv = (size_t)g.Nv, F = sizeof(float);
     a.tables = a.L.take((size_t)(4 * g.nT + 2) * F);
-    a.eta = a.L.take(N * F); a.gam = a.L.take(N * F);
+    const size_t S = scalar_bytes(storage);
+    a.eta = a.L.take(N * S); a.gam = a.L.take(N * S);
     a.uth = a.L.take(Nv * F); a.uph = a.L.take(N * F);
     a.eta_adv = a.L.take(N * F); a.gam_adv = a.L.take(N * F);
     a.uth_adv = a.L.take(Nv * F); a.uph_adv = a.L.take(N * F);
-    for (size_t& b : a.bim) b = a.L.take(N * F);
+    // init, delta, initL, deltaL of eta, then of gamma: the reference fields
+    // in the stored type, the accumulators in FP32
+    for (int k = 0; k < 8; ++k) a.bim[k] = a.L.take(N * ((k & 1) ? F : S));
     for (int k = 0; k < 2; ++k) { a.fwd[k] = a.L.take(N * 8); a.bwd[k] = a.L.take(N * 8); }
     a.bwdprev = a.L.take(N * 8);
     a.uair_init = a.L.take(N * F); a.vair_init = a.L.take(Nv * F);
@@ -191,23 +200,34 @@ int validate(const sb_params* p) {
     if (!(p->radius > 0) || !(p->H > 0) || !(p->Gamma_m > 0) || !(p->T > 0))
         return fail(SB_ERR_INVALID, "radius, H, Gamma_m and T must be positive");
     if (!(p->dt > 0)) return fail(SB_ERR_INVALID, "timePerStep must be positive");
+    if (p->storage != SB_STORE_FP32 && p->storage != SB_STORE_BF16)
+        return fail(SB_ERR_INVALID, "storage must be SB_STORE_FP32 or SB_STORE_BF16");
     return SB_OK;
 }
 
-float* fptr(sb_bubble* b, sb_field w) {
+// The stored thickness / surfactant fields (FP32 or BF16 per bubble).
+SbScalar* sptr(sb_bubble* b, sb_field w) {
     SbFields& f = b->f;
     switch (w) {
         case SB_ETA: return f.eta;
         case SB_GAMMA: return f.gam;
+        case SB_ETA_INIT: return f.eta_init;
+        case SB_ETA_INIT_LAST: return f.eta_initL;
+        case SB_GAMMA_INIT: return f.gam_init;
+        case SB_GAMMA_INIT_LAST: return f.gam_initL;
+        default: return nullptr;
+    }
+}
+
+// The FP32 fields.
+float* fptr(sb_bubble* b, sb_field w) {
+    SbFields& f = b->f;
+    switch (w) {
         case SB_UTHETA: return f.uth;
         case SB_UPHI: return f.uph;
-        case SB_ETA_INIT: return f.eta_init;
         case SB_ETA_DELTA: return f.eta_delta;
-        case SB_ETA_INIT_LAST: return f.eta_initL;
         case SB_ETA_DELTA_LAST: return f.eta_deltaL;
-        case SB_GAMMA_INIT: return f.gam_init;
         case SB_GAMMA_DELTA: return f.gam_delta;
-        case SB_GAMMA_INIT_LAST: return f.gam_initL;
         case SB_GAMMA_DELTA_LAST: return f.gam_deltaL;
         case SB_UAIR_INIT: return f.uair_init;
         case SB_VAIR_INIT: return f.vair_init;
@@ -254,16 +274,16 @@ int set_step_params(sb_bubble* b, double t, double dt_s) {
 }
 
 int reset_bimocq(sb_bubble* b) {
-    const size_t N = (size_t)b->g.N * sizeof(float);
+    const size_t N = (size_t)b->g.N * scalar_bytes(b->storage), N4 = (size_t)b->g.N * 4;
     SbFields& f = b->f;
     SB_CHECK(cudaMemcpyAsync(f.eta_init, f.eta, N, cudaMemcpyDeviceToDevice, b->stream));
     SB_CHECK(cudaMemcpyAsync(f.eta_initL, f.eta, N, cudaMemcpyDeviceToDevice, b->stream));
     SB_CHECK(cudaMemcpyAsync(f.gam_init, f.gam, N, cudaMemcpyDeviceToDevice, b->stream));
     SB_CHECK(cudaMemcpyAsync(f.gam_initL, f.gam, N, cudaMemcpyDeviceToDevice, b->stream));
-    SB_CHECK(cudaMemsetAsync(f.eta_delta, 0, N, b->stream));
-    SB_CHECK(cudaMemsetAsync(f.eta_deltaL, 0, N, b->stream));
-    SB_CHECK(cudaMemsetAsync(f.gam_delta, 0, N, b->stream));
-    SB_CHECK(cudaMemsetAsync(f.gam_deltaL, 0, N, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.eta_delta, 0, N4, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.eta_deltaL, 0, N4, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.gam_delta, 0, N4, b->stream));
+    SB_CHECK(cudaMemsetAsync(f.gam_deltaL, 0, N4, b->stream));
     SB_CHECK(launch_reset_maps(b->g, b->f, b->stream));
     return SB_OK;
 }
@@ -276,11 +296,39 @@ int upload_f32(sb_bubble* b, float* dst, const double* src, size_t n) {
     return SB_OK;
 }
 
-int fill_const(sb_bubble* b, float* dst, size_t n, float v) {
-    std::vector<float> tmp(n, v);
-    SB_CHECK(cudaMemcpyAsync(dst, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+// Device FP32 staging for stored fields: the re-initialisation error
+// array, which only lives inside a step (k_accum -> k_reinit), while
+// uploads and downloads run between steps on the bubble's stream.
+float* staging(sb_bubble* b) { return b->f.err_eta; }
+
+// FP32 data already on the device (staging) into a stored field.
+int store_from_staging(sb_bubble* b, SbScalar* dst, size_t n) {
+    SB_CHECK(launch_store(dst, staging(b), (int)n, b->storage, b->stream));
+    b->launches += 1;
+    return SB_OK;
+}
+
+// A stored field as FP32 into the staging array.
+int load_to_staging(sb_bubble* b, const SbScalar* src, size_t n) {
+    SB_CHECK(launch_load(staging(b), src, (int)n, b->storage, b->stream));
+    b->launches += 1;
+    return SB_OK;
+}
+
+int upload_scalar(sb_bubble* b, SbScalar* dst, const double* src, size_t n) {
+    std::vector<float> tmp(n);
+    for (size_t i = 0; i < n; ++i) tmp[i] = (float)src[i];
+    SB_CHECK(cudaMemcpyAsync(staging(b), tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice,
+                             b->stream));
+    int rc = store_from_staging(b, dst, n);
+    if (rc != SB_OK) return rc;
     SB_CHECK(cudaStreamSynchronize(b->stream));
     return SB_OK;
+}
+
+int fill_const(sb_bubble* b, SbScalar* dst, size_t n, float v) {
+    std::vector<double> tmp(n, (double)v);
+    return upload_scalar(b, dst, tmp.data(), n);
 }
 
 }  // namespace
@@ -312,7 +360,7 @@ size_t sb_bytes_required(const sb_params* p) {
     g.nP = 2 * p->nTheta;
     g.N = g.nT * g.nP;
     g.Nv = (g.nT - 1) * g.nP;
-    return plan_arena(g).L.bytes;
+    return plan_arena(g, p->storage).L.bytes;
 }
 
 int sb_create(const sb_params* p, sb_bubble** out) {
@@ -340,8 +388,9 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     b->solver.max_iter = p->solver_max_iter > 0 ? p->solver_max_iter : 1000;
     b->solver.precond = 1;
     b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
+    b->storage = p->storage;
 
-    ArenaPlan a = plan_arena(g);
+    ArenaPlan a = plan_arena(g, p->storage);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->arena, a.L.bytes);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_step, sizeof(SbStepParams));
@@ -357,13 +406,14 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     auto F32 = [&](size_t off) { return (float*)(A + off); };
     SbFields& f = b->f;
     b->tables = F32(a.tables);
-    f.eta = F32(a.eta); f.gam = F32(a.gam); f.uth = F32(a.uth); f.uph = F32(a.uph);
+    auto SCL = [&](size_t off) { return (SbScalar*)(A + off); };
+    f.eta = SCL(a.eta); f.gam = SCL(a.gam); f.uth = F32(a.uth); f.uph = F32(a.uph);
     f.eta_adv = F32(a.eta_adv); f.gam_adv = F32(a.gam_adv);
     f.uth_adv = F32(a.uth_adv); f.uph_adv = F32(a.uph_adv);
-    f.eta_init = F32(a.bim[0]); f.eta_delta = F32(a.bim[1]);
-    f.eta_initL = F32(a.bim[2]); f.eta_deltaL = F32(a.bim[3]);
-    f.gam_init = F32(a.bim[4]); f.gam_delta = F32(a.bim[5]);
-    f.gam_initL = F32(a.bim[6]); f.gam_deltaL = F32(a.bim[7]);
+    f.eta_init = SCL(a.bim[0]); f.eta_delta = F32(a.bim[1]);
+    f.eta_initL = SCL(a.bim[2]); f.eta_deltaL = F32(a.bim[3]);
+    f.gam_init = SCL(a.bim[4]); f.gam_delta = F32(a.bim[5]);
+    f.gam_initL = SCL(a.bim[6]); f.gam_deltaL = F32(a.bim[7]);
     for (int k = 0; k < 2; ++k) {
         f.fwd[k] = (float2*)(A + a.fwd[k]);
         f.bwd[k] = (float2*)(A + a.bwd[k]);
@@ -477,6 +527,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
         S.acc = f.acc;
         P.maxNP = g.nP;
         P.solver = b->solver;
+        P.storage = b->storage;
         b->desc = d;
         P.one = &b->desc;
         if (e != cudaSuccess) rc = cuda_fail(e, "step plan");
@@ -551,6 +602,7 @@ int sb_upload_field(sb_bubble* b, sb_field which, const double* src, size_t n) {
         SB_CHECK(cudaStreamSynchronize(b->stream));
         return SB_OK;
     }
+    if (SbScalar* s = sptr(b, which)) return upload_scalar(b, s, src, n);
     float* d = fptr(b, which);
     if (!d) return fail(SB_ERR_INVALID, "unknown field");
     return upload_f32(b, d, src, n);
@@ -580,7 +632,12 @@ int sb_download_field(sb_bubble* b, sb_field which, double* dst, size_t n) {
             }
         return SB_OK;
     }
-    float* d = fptr(b, which);
+    const float* d = fptr(b, which);
+    if (SbScalar* s = sptr(b, which)) {
+        int rc = load_to_staging(b, s, n);
+        if (rc != SB_OK) return rc;
+        d = staging(b);
+    }
     if (!d) return fail(SB_ERR_INVALID, "unknown field");
     std::vector<float> tmp(n);
     SB_CHECK(cudaMemcpyAsync(tmp.data(), d, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
@@ -595,8 +652,8 @@ int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma, const
     SB_CHECK(cudaSetDevice(b->device));
     const size_t N = (size_t)b->g.N, Nv = (size_t)b->g.Nv;
     int rc = SB_OK;
-    if (eta && rc == SB_OK) rc = upload_f32(b, b->f.eta, eta, N);
-    if (gamma && rc == SB_OK) rc = upload_f32(b, b->f.gam, gamma, N);
+    if (eta && rc == SB_OK) rc = upload_scalar(b, b->f.eta, eta, N);
+    if (gamma && rc == SB_OK) rc = upload_scalar(b, b->f.gam, gamma, N);
     if (u_theta && rc == SB_OK) rc = upload_f32(b, b->f.uth, u_theta, Nv);
     if (u_phi && rc == SB_OK) rc = upload_f32(b, b->f.uph, u_phi, N);
     if (uair_init && rc == SB_OK) rc = upload_f32(b, b->f.uair_init, uair_init, N);
@@ -736,19 +793,28 @@ const char* sb_stage_name(int stage) {
 int sb_upload_field_f32(sb_bubble* b, sb_field which, const float* src, size_t n) {
     if (!b || !src) return fail(SB_ERR_INVALID, "null argument");
     if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
-    float* d = fptr(b, which);
+    SbScalar* s = sptr(b, which);
+    float* d = s ? (b->storage == kStoreF32 ? reinterpret_cast<float*>(s) : staging(b))
+                 : fptr(b, which);
     if (!d) return fail(SB_ERR_INVALID, "maps move through sb_upload_field");
     SB_CHECK(cudaSetDevice(b->device));
     SB_CHECK(cudaMemcpyAsync(d, src, n * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+    if (s && b->storage != kStoreF32) return store_from_staging(b, s, n);
     return SB_OK;
 }
 
 int sb_download_field_f32(sb_bubble* b, sb_field which, float* dst, size_t n) {
     if (!b || !dst) return fail(SB_ERR_INVALID, "null argument");
     if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
-    float* d = fptr(b, which);
+    SbScalar* s = sptr(b, which);
+    const float* d = s ? (b->storage == kStoreF32 ? reinterpret_cast<const float*>(s) : staging(b))
+                       : fptr(b, which);
     if (!d) return fail(SB_ERR_INVALID, "maps move through sb_download_field");
     SB_CHECK(cudaSetDevice(b->device));
+    if (s && b->storage != kStoreF32) {
+        int rc = load_to_staging(b, s, n);
+        if (rc != SB_OK) return rc;
+    }
     SB_CHECK(cudaMemcpyAsync(dst, d, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
     return SB_OK;
 }
@@ -788,7 +854,7 @@ int sb_get_stats(sb_bubble* b, sb_stats* out) {
 int sb_update_mass(sb_bubble* b) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     SB_CHECK(cudaSetDevice(b->device));
-    SB_CHECK(launch_mass(b->g, b->f, b->stream));
+    SB_CHECK(launch_mass(b->g, b->f, b->storage, b->stream));
     b->launches += 1;
     SB_CHECK(cudaStreamSynchronize(b->stream));
     return SB_OK;
@@ -799,7 +865,13 @@ int sb_write_thickness_exr(sb_bubble* b, const char* path, int* broken) {
     SB_CHECK(cudaSetDevice(b->device));
     const size_t N = (size_t)b->g.N;
     std::vector<float> eta(N);
-    SB_CHECK(cudaMemcpyAsync(eta.data(), b->f.eta, N * 4, cudaMemcpyDeviceToHost, b->stream));
+    const float* src = reinterpret_cast<const float*>(b->f.eta);
+    if (b->storage != kStoreF32) {
+        int rc = load_to_staging(b, b->f.eta, N);
+        if (rc != SB_OK) return rc;
+        src = staging(b);
+    }
+    SB_CHECK(cudaMemcpyAsync(eta.data(), src, N * 4, cudaMemcpyDeviceToHost, b->stream));
     SB_CHECK(cudaStreamSynchronize(b->stream));
     // Solver::write_thickness_img (kernel/solver.cu:541-593)
     const double ratio = 2e5;
@@ -926,6 +998,7 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     B->device = bubbles[0]->device;
     SbStepPlan& P = B->plan;
     P.solver = bubbles[0]->solver;
+    P.storage = bubbles[0]->storage;
     for (int k = 0; k < n; ++k) {
         sb_bubble* b = bubbles[k];
         if (!b || b->device != B->device) {
@@ -937,6 +1010,10 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
             c.tol != P.solver.tol || c.precond != P.solver.precond) {
             delete B;
             return fail(SB_ERR_INVALID, "batch members must share one solver configuration");
+        }
+        if (b->storage != P.storage) {
+            delete B;
+            return fail(SB_ERR_INVALID, "batch members must share one field storage");
         }
         B->m.push_back(b);
         if (b->g.nP > P.maxNP) P.maxNP = b->g.nP;

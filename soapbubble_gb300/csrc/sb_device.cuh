@@ -21,7 +21,10 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <cuda_bf16.h>
+
 #include "sb_fastmath.cuh"
+#include "sb_internal.h"
 #include "sb_types.h"
 
 // Inlining of the geometry helpers: the slerp and the map lookup are inlined
@@ -478,6 +481,32 @@ __device__ __forceinline__ SStencil sstencil_of(const SbGrid& g, const CStencil&
 
 __device__ __forceinline__ SStencil scalar_stencil(const SbGrid& g, Pos q) {
     return sstencil_of(g, centred_stencil(g, q, 0.0f));
+}
+
+// A thickness or surfactant field in its storage type T (float or
+// __nv_bfloat16): loads widen to FP32, stores round to nearest even.
+template <class T>
+__device__ __forceinline__ float ld_s(const SbScalar* p, int i) {
+    return (float)reinterpret_cast<const T*>(p)[i];
+}
+template <>
+__device__ __forceinline__ float ld_s<__nv_bfloat16>(const SbScalar* p, int i) {
+    return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(p)[i]);
+}
+template <class T>
+__device__ __forceinline__ void st_s(SbScalar* p, int i, float v) {
+    reinterpret_cast<T*>(p)[i] = v;
+}
+template <>
+__device__ __forceinline__ void st_s<__nv_bfloat16>(SbScalar* p, int i, float v) {
+    reinterpret_cast<__nv_bfloat16*>(p)[i] = __float2bfloat16_rn(v);
+}
+
+template <class T>
+__device__ __forceinline__ float gather_s(const SbScalar* f, const SStencil& s) {
+    const float l = blerp(ld_s<T>(f, s.i00), ld_s<T>(f, s.i01), s.b);
+    const float u = blerp(ld_s<T>(f, s.i10), ld_s<T>(f, s.i11), s.b);
+    return blerp(l, u, s.a);
 }
 
 __device__ __forceinline__ float gather(const float* __restrict__ f, const SStencil& s) {

@@ -38,11 +38,21 @@ __host__ __device__ inline SbFactorBlob factor_blob(int n) {
 // Every device array of one bubble.  Fields are FP32, row-major [theta][phi]
 // with row stride nPhi; u_theta has nTheta-1 rows.  "A" buffers hold the
 // state between steps, "adv" buffers the advected intermediate state.
+// The thickness and surfactant fields that persist between steps (eta,
+// gamma and the BIMOCQ reference fields eta/gamma_init and _initL) are
+// stored as FP32 or, per bubble, as BF16 (SbScalar: an opaque element
+// type; kernels read and write them through ld_s / st_s with the storage
+// type as a template argument and do their arithmetic in FP32).  The BIMOCQ
+// change accumulators (the _delta buffers) stay FP32 in both: they grow by
+// small increments every step, which BF16 would round away.
+struct SbScalar;
+
 struct SbFields {
-    float *eta, *gam, *uth, *uph;                  // state
+    SbScalar *eta, *gam;                           // state (stored type)
+    float *uth, *uph;
     float *eta_adv, *gam_adv, *uth_adv, *uph_adv;  // after advection
-    float *eta_init, *eta_delta, *eta_initL, *eta_deltaL;
-    float *gam_init, *gam_delta, *gam_initL, *gam_deltaL;
+    SbScalar *eta_init, *eta_initL, *gam_init, *gam_initL;
+    float *eta_delta, *eta_deltaL, *gam_delta, *gam_deltaL;
     float2 *fwd[2], *bwd[2], *bwdprev;             // map offsets (ping-pong)
     float *uair_init, *vair_init, *corr_u, *corr_v;
     float *uair, *vair;                            // N+1, Nv+1 (last element 0)
@@ -101,7 +111,10 @@ enum SbStage {
 };
 
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s);
-cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s);
+cudaError_t launch_mass(const SbGrid& g, const SbFields& f, int storage, cudaStream_t s);
+// FP32 <-> stored thickness / surfactant field (n elements).
+cudaError_t launch_store(SbScalar* dst, const float* src, int n, int storage, cudaStream_t s);
+cudaError_t launch_load(float* dst, const SbScalar* src, int n, int storage, cudaStream_t s);
 
 // Scalars of one system of a solve, written by the block that completes the
 // system's last row in a phase and read in the next phase (double buffered).
@@ -159,6 +172,7 @@ struct SbStepPlan {
     SbSolveSet set;              // every bubble's implicit system
     int maxNP;                   // widest grid of the set
     SolverConfig solver;
+    int storage;                 // SB_STORE_FP32 or SB_STORE_BF16 (the same for every bubble)
     const SbBubbleDesc* one;     // host copy of the descriptor of a set of one bubble, else null
 };
 

@@ -53,6 +53,7 @@ __device__ __forceinline__ Pos pos_of(const Frame& F, const Trace& T, const SbGr
 }
 
 // ---------------------------------------------------------------------------
+template <class T>
 __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
     (void)ph;
@@ -79,7 +80,7 @@ __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& 
     const CStencil cb = centred_stencil(g, pos_of(F, Tb, g), 0.0f);
     const f3 db = map_at_stencil(f.bwd[cur], F, cb, g.nT, g.h);
     f.bwd[cur ^ 1][idx] = map_entry_from_disp(g, F, db);
-    f.gam_adv[idx] = gather(f.gam, sstencil_of(g, cb));
+    f.gam_adv[idx] = gather_s<T>(f.gam, sstencil_of(g, cb));
 
     // air flow = initial wind + corridor(t); NaN -> 0
     const float wg = f.step->windg;
@@ -138,12 +139,13 @@ __device__ __forceinline__ void velocity_cell(const SbGrid& g, const SbPhys& ph,
 
 // BIMOCQ thickness: compose the new backward map with the previous one and
 // blend the two reconstructions (MULTISAMPLE, 5 samples).
+template <class T>
 __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
     (void)ph;
     (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
-    if (f.eta[idx] == 0.0f) {
+    if (ld_s<T>(f.eta, idx) == 0.0f) {
         f.eta_adv[idx] = 0.0f;
         return;
     }
@@ -161,8 +163,8 @@ __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, c
         const SStencil s2 = scalar_stencil(g, q2);
         const float sDelta = gather(f.eta_delta, s1);
         attrib += (1.0f - blend) * kW5[k] *
-                  (gather(f.eta_initL, s2) + sDelta + gather(f.eta_deltaL, s2));
-        attrib += blend * kW5[k] * (gather(f.eta_init, s1) + sDelta);
+                  (gather_s<T>(f.eta_initL, s2) + sDelta + gather(f.eta_deltaL, s2));
+        attrib += blend * kW5[k] * (gather_s<T>(f.eta_init, s1) + sDelta);
     }
     f.eta_adv[idx] = fmaxf(0.0f, attrib);
 }
@@ -309,6 +311,7 @@ __device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, floa
     return (ca ? gmax : xa) - (cb ? gmax : xb);
 }
 
+template <class T>
 __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
     (void)ph;
@@ -321,12 +324,12 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
     const float gNew = f.x[idx];
     float mdtdiv;  // -dt * div
     if (gamma_clamped(gNew, gmax)) {
-        f.gam[idx] = gmax;
+        st_s<T>(f.gam, idx, gmax);
         f.d_gam[idx] = gmax - gOld;
         mdtdiv = -1.0f;
     } else {
         const float dx = f.dx[idx];
-        f.gam[idx] = gNew;
+        st_s<T>(f.gam, idx, gNew);
         f.d_gam[idx] = dx;
         // div = (1 - min(gNew, 2 gOld) / gOld) / dt
         mdtdiv = (gNew > 2.0f * gOld) ? 1.0f : dx / gOld;
@@ -335,10 +338,10 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
     const float e = f.eta_adv[idx];
     const float de = e * mdtdiv + f.step->evapDt;
     if (e + de >= 0.0f) {
-        f.eta[idx] = e + de;
+        st_s<T>(f.eta, idx, e + de);
         f.d_eta[idx] = de;
     } else {
-        f.eta[idx] = 0.0f;
+        st_s<T>(f.eta, idx, 0.0f);
         f.d_eta[idx] = -e;
     }
 
@@ -387,6 +390,7 @@ __device__ __forceinline__ float warp_max(float v) {
 // fields at the same five points): the error is formed every step, and the
 // re-initialisation, when the distortion calls for it, only corrects.
 // returns the cell's distortion (0 outside the grid)
+template <class T>
 __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                            int idx) {
     (void)ph;
@@ -403,13 +407,13 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
         const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
         ed += kW5[k] * gather(f.d_eta, s);
         gd += kW5[k] * gather(f.d_gam, s);
-        th += kW5[k] * gather(f.eta, s);
-        gm += kW5[k] * gather(f.gam, s);
+        th += kW5[k] * gather_s<T>(f.eta, s);
+        gm += kW5[k] * gather_s<T>(f.gam, s);
     }
     f.eta_delta[idx] = ed;
     f.gam_delta[idx] = gd;
-    f.err_eta[idx] = (th - ed - f.eta_init[idx]) * 0.5f;
-    f.err_gam[idx] = (gm - gd - f.gam_init[idx]) * 0.5f;
+    f.err_eta[idx] = (th - ed - ld_s<T>(f.eta_init, idx)) * 0.5f;
+    f.err_gam[idx] = (gm - gd - ld_s<T>(f.gam_init, idx)) * 0.5f;
     // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
     float2 m = fwd[idx];
     const float d1 = dist_from_disp(sample_map(g, bwd, F, frame_pos(F, m.x, m.y)), g.invh);
@@ -451,29 +455,43 @@ __device__ __forceinline__ const SbBubbleDesc& stage_tile_desc(SbBubbleDesc* con
     return *s_d;
 }
 
+// Kernels whose cells touch the stored thickness / surfactant fields are
+// instantiated per storage type T (float or __nv_bfloat16); a plan launches
+// the instantiation of its bubbles' storage.
+#define SB_CELL_KERNEL_BODY(call)                                                      \
+    __shared__ __align__(16) SbBubbleDesc s_d;                                         \
+    const int2 t = tiles[blockIdx.x];                                                  \
+    const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);                         \
+    const int idx = t.y + threadIdx.x;                                                 \
+    if (idx < d.g.N) call(d.g, d.ph, d.f, d.cur, idx);
+
 #define SB_CELL_KERNEL(name)                                                           \
     __global__ void __launch_bounds__(256) k_##name(SbBubbleDesc* const* __restrict__ descs, \
                                                     const int2* __restrict__ tiles) {  \
-        __shared__ __align__(16) SbBubbleDesc s_d;                                     \
-        const int2 t = tiles[blockIdx.x];                                              \
-        const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);                     \
-        const int idx = t.y + threadIdx.x;                                             \
-        if (idx < d.g.N) name##_cell(d.g, d.ph, d.f, d.cur, idx);                     \
+        SB_CELL_KERNEL_BODY(name##_cell)                                               \
     }
 
-SB_CELL_KERNEL(advect_maps)
-SB_CELL_KERNEL(velocity)
-SB_CELL_KERNEL(bimocq)
-SB_CELL_KERNEL(assemble)
-SB_CELL_KERNEL(post)
+#define SB_CELL_KERNEL_T(name)                                                         \
+    template <class T>                                                                 \
+    __global__ void __launch_bounds__(256) k_##name(SbBubbleDesc* const* __restrict__ descs, \
+                                                    const int2* __restrict__ tiles) {  \
+        SB_CELL_KERNEL_BODY(name##_cell<T>)                                            \
+    }
 
+SB_CELL_KERNEL_T(advect_maps)
+SB_CELL_KERNEL(velocity)
+SB_CELL_KERNEL_T(bimocq)
+SB_CELL_KERNEL(assemble)
+SB_CELL_KERNEL_T(post)
+
+template <class T>
 __global__ void __launch_bounds__(256) k_accum(SbBubbleDesc* const* __restrict__ descs,
                                                const int2* __restrict__ tiles) {
     __shared__ __align__(16) SbBubbleDesc s_d;
     const int2 t = tiles[blockIdx.x];
     const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);
     const int idx = t.y + threadIdx.x;
-    const float dist = idx < d.g.N ? accum_cell(d.g, d.ph, d.f, d.cur, idx) : 0.0f;
+    const float dist = idx < d.g.N ? accum_cell<T>(d.g, d.ph, d.f, d.cur, idx) : 0.0f;
     block_max_distortion(dist, d.f.stats);
 }
 
@@ -492,11 +510,12 @@ __device__ __forceinline__ int nb_index(const SbGrid& g, int i, int j) {
 // correctCentered2: subtract the error pulled back through the backward map,
 // clamp to the 3x3 range of the uncorrected field, keep non-negative.  The
 // result goes to the *_adv buffers and is committed in the next phase.
+template <class T>
 __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbFields& f, int cur, int idx) {
     const int i = idx >> g.logP, j = idx & g.maskP;
     const Frame F = cell_frame(g, i, j);
     const float2* bwd = f.bwd[cur ^ 1];
-    float th = f.eta[idx], gm = f.gam[idx];
+    float th = ld_s<T>(f.eta, idx), gm = ld_s<T>(f.gam, idx);
     f3 ds[5];
     sample_map_multi5(g, bwd, F, ds);
 #pragma unroll
@@ -505,11 +524,11 @@ __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbFields& 
         th -= kW5[k] * gather(f.err_eta, s);
         gm -= kW5[k] * gather(f.err_gam, s);
     }
-    float emin = f.eta[idx], emax = emin, gmin = f.gam[idx], gmx = gmin;
+    float emin = ld_s<T>(f.eta, idx), emax = emin, gmin = ld_s<T>(f.gam, idx), gmx = gmin;
     for (int t = -1; t <= 1; ++t)
         for (int p = -1; p <= 1; ++p) {
             const int n = nb_index(g, i + t, j + p);
-            const float ev = f.eta[n], gv = f.gam[n];
+            const float ev = ld_s<T>(f.eta, n), gv = ld_s<T>(f.gam, n);
             emin = fminf(emin, ev); emax = fmaxf(emax, ev);
             gmin = fminf(gmin, gv); gmx = fmaxf(gmx, gv);
         }
@@ -520,17 +539,18 @@ __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbFields& 
 }
 
 // Commit the correction, rotate the BIMOCQ buffers and reset the maps.
+template <class T>
 __device__ __forceinline__ void reinit_commit(const SbFields& f, int cur, int idx) {
     const float e = f.eta_adv[idx], gm = f.gam_adv[idx];
-    f.eta[idx] = e;
-    f.gam[idx] = gm;
-    f.eta_initL[idx] = f.eta_init[idx];
+    st_s<T>(f.eta, idx, e);
+    st_s<T>(f.gam, idx, gm);
+    st_s<T>(f.eta_initL, idx, ld_s<T>(f.eta_init, idx));
     f.eta_deltaL[idx] = f.eta_delta[idx];
-    f.gam_initL[idx] = f.gam_init[idx];
+    st_s<T>(f.gam_initL, idx, ld_s<T>(f.gam_init, idx));
     f.gam_deltaL[idx] = f.gam_delta[idx];
-    f.eta_init[idx] = e;
+    st_s<T>(f.eta_init, idx, e);
     f.eta_delta[idx] = 0.0f;
-    f.gam_init[idx] = gm;
+    st_s<T>(f.gam_init, idx, gm);
     f.gam_delta[idx] = 0.0f;
     f.bwdprev[idx] = f.bwd[cur ^ 1][idx];
     f.fwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
@@ -545,6 +565,7 @@ __device__ __forceinline__ void reinit_commit(const SbFields& f, int cur, int id
 // needed; every block reads every bubble's decision, so all blocks agree on
 // whether any phase runs, and without a re-initialisation they return at
 // once.
+template <class T>
 __global__ void __launch_bounds__(kBlock)
 k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict__ tiles,
          int ntiles) {
@@ -566,7 +587,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
                 d.f.stats->reinit = 1;
                 d.f.stats->reinit_total += 1;
             }
-            reinit_correct(d.g, d.f, d.cur, idx);
+            reinit_correct<T>(d.g, d.f, d.cur, idx);
         }
     }
     grid.sync();
@@ -575,7 +596,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
         const SbBubbleDesc& d = *descs[tl.x];
         if (!reinit_now(d.f.stats)) continue;
         for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
-            reinit_commit(d.f, d.cur, idx);
+            reinit_commit<T>(d.f, d.cur, idx);
     }
 }
 
@@ -600,13 +621,14 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // Mass integrals sum(eta sin theta), sum(gamma sin theta) for conservation checks.
+template <class T>
 __global__ void k_mass(SbGrid g, SbFields f) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     double me = 0.0, mg = 0.0;
     if (idx < g.N) {
         const double s = (double)g.sin_c[idx >> g.logP];
-        me = (double)f.eta[idx] * s;
-        mg = (double)f.gam[idx] * s;
+        me = (double)ld_s<T>(f.eta, idx) * s;
+        mg = (double)ld_s<T>(f.gam, idx) * s;
     }
     me = warp_sum_d(me);
     mg = warp_sum_d(mg);
@@ -616,16 +638,32 @@ __global__ void k_mass(SbGrid g, SbFields f) {
     }
 }
 
-// Co-resident grid of the cooperative re-initialisation kernel.
+// FP32 <-> stored type of a thickness or surfactant field (uploads and
+// downloads of BF16-stored fields convert on the device).
+template <class T>
+__global__ void k_store(SbScalar* __restrict__ dst, const float* __restrict__ src, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) st_s<T>(dst, i, src[i]);
+}
+template <class T>
+__global__ void k_load(float* __restrict__ dst, const SbScalar* __restrict__ src, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = ld_s<T>(src, i);
+}
+
+// Co-resident grid of the cooperative re-initialisation kernel (both
+// instantiations have the same resources; the smaller count is used).
 int reinit_blocks() {
     static int cache[16] = {0};
     int dev = 0;
     cudaGetDevice(&dev);
     int& b = cache[dev & 15];
     if (b == 0) {
-        int sms = 0, per = 0;
+        int sms = 0, p32 = 0, p16 = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_reinit, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p32, k_reinit<float>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p16, k_reinit<__nv_bfloat16>, kBlock, 0);
+        const int per = p32 < p16 ? p32 : p16;
         b = sms * (per > 0 ? per : 1);
     }
     return b;
@@ -645,16 +683,29 @@ cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s) {
     const int n = P.ntiles[k], block = kTileSizes[k];
     SbBubbleDesc* const* d = P.descs;
     const int2* t = P.tiles[k];
+    const bool bf = P.storage == kStoreBF16;
     switch (stage) {
-        case STAGE_MAPS: k_advect_maps<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_MAPS:
+            if (bf) k_advect_maps<__nv_bfloat16><<<n, block, 0, s>>>(d, t);
+            else k_advect_maps<float><<<n, block, 0, s>>>(d, t);
+            break;
         case STAGE_VELOCITY: k_velocity<<<n, block, 0, s>>>(d, t); break;
-        case STAGE_BIMOCQ: k_bimocq<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_BIMOCQ:
+            if (bf) k_bimocq<__nv_bfloat16><<<n, block, 0, s>>>(d, t);
+            else k_bimocq<float><<<n, block, 0, s>>>(d, t);
+            break;
         case STAGE_ASSEMBLE: k_assemble<<<n, block, 0, s>>>(d, t); break;
         case STAGE_SOLVE:
             return P.one ? launch_solve_one(P.one->g, P.one->f, P.set, P.solver, s)
                          : launch_solve(P.set, P.maxNP, P.solver, s);
-        case STAGE_POST: k_post<<<n, block, 0, s>>>(d, t); break;
-        case STAGE_ACCUM: k_accum<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_POST:
+            if (bf) k_post<__nv_bfloat16><<<n, block, 0, s>>>(d, t);
+            else k_post<float><<<n, block, 0, s>>>(d, t);
+            break;
+        case STAGE_ACCUM:
+            if (bf) k_accum<__nv_bfloat16><<<n, block, 0, s>>>(d, t);
+            else k_accum<float><<<n, block, 0, s>>>(d, t);
+            break;
         case STAGE_REINIT: {
             // the re-initialisation works on kBlock-cell tiles
             SbBubbleDesc* const* dd = P.descs;
@@ -662,8 +713,8 @@ cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s) {
             const int2* tt = P.tiles[1];
             int nt = P.ntiles[1];
             void* args[] = {&dd, &nb, &tt, &nt};
-            return cudaLaunchCooperativeKernel((const void*)k_reinit, dim3(reinit_blocks()),
-                                               dim3(kBlock), args, 0, s);
+            const void* fn = bf ? (const void*)k_reinit<__nv_bfloat16> : (const void*)k_reinit<float>;
+            return cudaLaunchCooperativeKernel(fn, dim3(reinit_blocks()), dim3(kBlock), args, 0, s);
         }
         default: return cudaErrorInvalidValue;
     }
@@ -688,10 +739,26 @@ cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_mass(const SbGrid& g, const SbFields& f, cudaStream_t s) {
+cudaError_t launch_mass(const SbGrid& g, const SbFields& f, int storage, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(&f.stats->mass_eta, 0, 2 * sizeof(double), s);
     if (e != cudaSuccess) return e;
-    k_mass<<<(g.N + kBlock - 1) / kBlock, kBlock, 0, s>>>(g, f);
+    const int nb = (g.N + kBlock - 1) / kBlock;
+    if (storage == kStoreBF16) k_mass<__nv_bfloat16><<<nb, kBlock, 0, s>>>(g, f);
+    else k_mass<float><<<nb, kBlock, 0, s>>>(g, f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_store(SbScalar* dst, const float* src, int n, int storage, cudaStream_t s) {
+    const int nb = (n + kBlock - 1) / kBlock;
+    if (storage == kStoreBF16) k_store<__nv_bfloat16><<<nb, kBlock, 0, s>>>(dst, src, n);
+    else k_store<float><<<nb, kBlock, 0, s>>>(dst, src, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_load(float* dst, const SbScalar* src, int n, int storage, cudaStream_t s) {
+    const int nb = (n + kBlock - 1) / kBlock;
+    if (storage == kStoreBF16) k_load<__nv_bfloat16><<<nb, kBlock, 0, s>>>(dst, src, n);
+    else k_load<float><<<nb, kBlock, 0, s>>>(dst, src, n);
     return cudaGetLastError();
 }
 

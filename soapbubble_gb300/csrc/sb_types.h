@@ -29,6 +29,10 @@ struct SbStepParams {
     float pad;
 };
 
+// Storage of the thickness and surfactant fields (the values of
+// SB_STORE_FP32 / SB_STORE_BF16 in the public header).
+enum { kStoreF32 = 0, kStoreBF16 = 1 };
+
 // Constant physical coefficients of one bubble.
 struct SbPhys {
     float M, Cr, gs, gmax, blend, evap;

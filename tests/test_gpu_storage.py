@@ -1,0 +1,144 @@
+"""GPU checks of the BF16 storage of the thickness and surfactant fields
+(SB_STORE_BF16: eta, gamma and the BIMOCQ reference fields in BF16 between
+steps, the BIMOCQ change accumulators in FP32, FP32 arithmetic).
+
+BF16 keeps 8 significant bits (unit roundoff 2^-9 ~ 2e-3), so the storage
+variant is compared against the FP64 oracle at that precision, not at the
+1e-5 of the FP32 path: after one step from identical inputs every stored
+field carries at most one BF16 rounding (plus FP32 noise).
+"""
+import numpy as np
+import pytest
+
+import _parity as P
+
+pytestmark = pytest.mark.gpu
+
+U_BF16 = 2.0 ** -8   # BF16 spacing relative to the value (rounding error <= half of it)
+
+
+def bf16_round(x):
+    """Round FP32 values to BF16 (nearest, ties to even), returned as FP32."""
+    a = np.asarray(x, dtype=np.float32).copy()
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16 << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+def _bubble(nT, recipe, seed, storage, **kw):
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    dt = {"c0": 0.005, "c1": 0.002, "c2": 0.001}[recipe]
+    f = synth.make_fields(recipe, nT, seed)
+    gb = GpuBubble(make_params(nT, dt, storage=storage, **kw))
+    gb.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    return gb, dt
+
+
+def test_bf16_fields_round_trip_and_memory(gpulib):
+    from soapbubble_gb300.bubble import bytes_required, make_params
+    gb, _ = _bubble(64, "c0", 3, 1)
+    try:
+        x = np.random.default_rng(0).uniform(0.1, 3.0, gb.nTheta * gb.nPhi)
+        gb.upload("gamma_init", x)
+        np.testing.assert_array_equal(gb.download("gamma_init").ravel(),
+                                      bf16_round(x.astype(np.float32)).astype(np.float64))
+        # the FP32 entry points convert on the device too
+        y = np.random.default_rng(1).uniform(0.1, 3.0, gb.nTheta * gb.nPhi).astype(np.float32)
+        gb.upload_f32("eta", y)
+        out = np.zeros_like(y)
+        gb.download_f32("eta", out)
+        gb.synchronize()
+        np.testing.assert_array_equal(out, bf16_round(y))
+    finally:
+        gb.close()
+    # six fields of nTheta x nPhi elements shrink from 4 to 2 bytes
+    n = 256 * 512
+    saved = bytes_required(make_params(256, 0.005)) - bytes_required(make_params(256, 0.005,
+                                                                                 storage=1))
+    assert saved >= 6 * n * 2 - 6 * 256 and saved <= 6 * n * 2 + 6 * 256, saved
+
+
+@pytest.mark.parametrize("case", [("c0", 64, 0.005, 5, 1.0, 1234), ("c2", 128, 0.001, 5, 0.5, 78)],
+                         ids=lambda c: f"{c[0]}-{c[1]}")
+def test_bf16_step_matches_oracle_at_bf16_precision(oracle, gpulib, case):
+    """One step from identical (BF16-representable) state: thickness and
+    surfactant within a BF16 rounding of the FP64 oracle, velocities close."""
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    recipe, nT, dt, pre, t, seed = case
+    f = synth.make_fields(recipe, nT, seed)
+    op = oracle.default_params(nT, dt_s=dt)
+    op.t = t
+    ob = oracle.OracleBubble(op, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    for _ in range(pre):
+        ob.step()
+    gb = GpuBubble(make_params(nT, dt, solver_tol=1e-10, solver_max_iter=2000, storage=1))
+    try:
+        P.sync_state(gb, ob)  # the oracle continues from the BF16-rounded state
+        gb.step(1, t, dt)
+        ob.step()
+        err = P.compare(gb, ob, ["eta", "gamma", "u_theta", "u_phi"])
+        assert err["eta"] <= U_BF16, err
+        assert err["gamma"] <= U_BF16, err
+        assert err["u_theta"] <= 1e-2 and err["u_phi"] <= 1e-2, err
+        assert gb.stats().solver_converged == 1
+    finally:
+        gb.close()
+
+
+def test_bf16_run_stays_finite_and_near_fp32(gpulib):
+    """Twenty steps in each storage.  The surfactant of the c0 recipe is
+    1 + 0.01 U(-1, 1), and BF16's spacing at 1 is 2^-7 = 0.0078: the upload
+    itself quantises most of that perturbation, so the runs differ by
+    percents (velocities, driven by surfactant gradients, by more); the
+    BF16 run stays finite, converges, and keeps thickness and surfactant
+    within 10 % of the FP32 run."""
+    a, dt = _bubble(64, "c0", 9, 0)
+    b, _ = _bubble(64, "c0", 9, 1)
+    try:
+        for k in range(20):
+            a.step(1, (k // 10) * 10 * dt, dt)
+            b.step(1, (k // 10) * 10 * dt, dt)
+        for name in ("eta", "gamma", "u_theta", "u_phi"):
+            assert np.isfinite(b.download(name)).all(), name
+        for name in ("eta", "gamma"):
+            x, y = a.download(name), b.download(name)
+            assert P.rel_err(y, x) <= 0.1, (name, P.rel_err(y, x))
+        assert b.stats().solver_converged == 1
+    finally:
+        a.close()
+        b.close()
+
+
+def test_bf16_batch_matches_members_stepped_alone(gpulib):
+    from soapbubble_gb300.bubble import GpuBatch
+    specs = [(32, "c0", 41), (64, "c0", 42), (16, "c0", 43)]
+    a = [_bubble(*s, 1)[0] for s in specs]
+    b = [_bubble(*s, 1)[0] for s in specs]
+    try:
+        with GpuBatch(a) as batch:
+            for k in range(12):
+                batch.step(1, (k // 5) * 5 * 0.005, 0.005)
+                for g in b:
+                    g.step(1, (k // 5) * 5 * 0.005, 0.005)
+            batch.synchronize()
+        for ga, gb in zip(a, b):
+            for name in ("eta", "gamma", "u_theta", "u_phi", "eta_delta", "gamma_init", "bwd_t"):
+                np.testing.assert_array_equal(ga.download(name), gb.download(name), err_msg=name)
+    finally:
+        for g in a + b:
+            g.close()
+
+
+def test_batch_rejects_mixed_storage(gpulib):
+    from soapbubble_gb300._lib import SoapBubbleError
+    from soapbubble_gb300.bubble import GpuBatch
+    a, _ = _bubble(16, "c0", 1, 0)
+    b, _ = _bubble(16, "c0", 2, 1)
+    try:
+        with pytest.raises(SoapBubbleError, match="storage"):
+            GpuBatch([a, b])
+    finally:
+        a.close()
+        b.close()
