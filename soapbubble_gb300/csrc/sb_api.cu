@@ -301,17 +301,49 @@ int upload_f32(sb_bubble* b, float* dst, const double* src, size_t n) {
 // uploads and downloads run between steps on the bubble's stream.
 float* staging(sb_bubble* b) { return b->f.err_eta; }
 
+// Offset of a stored field (its family's base: eta or gamma).
+float base_of(const sb_bubble* b, const SbScalar* p) {
+    const SbFields& f = b->f;
+    const bool gam = p == f.gam || p == f.gam_init || p == f.gam_initL;
+    return gam ? b->ph.base_gam : b->ph.base_eta;
+}
+
 // FP32 data already on the device (staging) into a stored field.
 int store_from_staging(sb_bubble* b, SbScalar* dst, size_t n) {
-    SB_CHECK(launch_store(dst, staging(b), (int)n, b->storage, b->stream));
+    SB_CHECK(launch_store(dst, staging(b), (int)n, base_of(b, dst), b->storage, b->stream));
     b->launches += 1;
     return SB_OK;
 }
 
 // A stored field as FP32 into the staging array.
 int load_to_staging(sb_bubble* b, const SbScalar* src, size_t n) {
-    SB_CHECK(launch_load(staging(b), src, (int)n, b->storage, b->stream));
+    SB_CHECK(launch_load(staging(b), src, (int)n, base_of(b, src), b->storage, b->stream));
     b->launches += 1;
+    return SB_OK;
+}
+
+// v rounded to the nearest BF16 number (ties to even), as a float.
+float bf16_round(float v) {
+    uint32_t u;
+    std::memcpy(&u, &v, 4);
+    u = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
+    std::memcpy(&v, &u, 4);
+    return v;
+}
+
+// BF16 storage: the base of a field family becomes the mean of the values
+// about to be stored (a BF16 number, so that 0 and the base stay exact);
+// the kernels read it from the device descriptor.
+int set_base(sb_bubble* b, bool gamma, const double* v, size_t n) {
+    if (b->storage != kStoreBF16) return SB_OK;
+    double s = 0.0;
+    for (size_t i = 0; i < n; ++i) s += v[i];
+    const float base = bf16_round(n ? (float)(s / (double)n) : 0.0f);
+    (gamma ? b->ph.base_gam : b->ph.base_eta) = base;
+    b->desc.ph = b->ph;
+    SB_CHECK(cudaMemcpyAsync(&b->f.self->ph, &b->ph, sizeof(SbPhys), cudaMemcpyHostToDevice,
+                             b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
     return SB_OK;
 }
 
@@ -389,6 +421,9 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     b->solver.precond = 1;
     b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
     b->storage = p->storage;
+    // BF16 storage: offsets of the initial fields (eta = 0.5, gamma = 1)
+    b->ph.base_eta = b->storage == kStoreBF16 ? 0.5f : 0.0f;
+    b->ph.base_gam = b->storage == kStoreBF16 ? 1.0f : 0.0f;
 
     ArenaPlan a = plan_arena(g, p->storage);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
@@ -652,7 +687,9 @@ int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma, const
     SB_CHECK(cudaSetDevice(b->device));
     const size_t N = (size_t)b->g.N, Nv = (size_t)b->g.Nv;
     int rc = SB_OK;
+    if (eta && rc == SB_OK) rc = set_base(b, false, eta, N);
     if (eta && rc == SB_OK) rc = upload_scalar(b, b->f.eta, eta, N);
+    if (gamma && rc == SB_OK) rc = set_base(b, true, gamma, N);
     if (gamma && rc == SB_OK) rc = upload_scalar(b, b->f.gam, gamma, N);
     if (u_theta && rc == SB_OK) rc = upload_f32(b, b->f.uth, u_theta, Nv);
     if (u_phi && rc == SB_OK) rc = upload_f32(b, b->f.uph, u_phi, N);
@@ -854,7 +891,7 @@ int sb_get_stats(sb_bubble* b, sb_stats* out) {
 int sb_update_mass(sb_bubble* b) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     SB_CHECK(cudaSetDevice(b->device));
-    SB_CHECK(launch_mass(b->g, b->f, b->storage, b->stream));
+    SB_CHECK(launch_mass(b->g, b->ph, b->f, b->storage, b->stream));
     b->launches += 1;
     SB_CHECK(cudaStreamSynchronize(b->stream));
     return SB_OK;

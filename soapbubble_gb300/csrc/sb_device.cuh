@@ -483,29 +483,41 @@ __device__ __forceinline__ SStencil scalar_stencil(const SbGrid& g, Pos q) {
     return sstencil_of(g, centred_stencil(g, q, 0.0f));
 }
 
-// A thickness or surfactant field in its storage type T (float or
-// __nv_bfloat16): loads widen to FP32, stores round to nearest even.
+// A thickness or surfactant field in its storage type T.  FP32 fields hold
+// the values.  BF16 fields hold the deviation from a per-field base value
+// (the field's mean at upload, itself a BF16 number, so that 0 and the base
+// are exact): loads return base + deviation in FP32, stores round
+// value - base to nearest even.  Fields of order one with perturbations of
+// a few percent keep about three significant digits of the perturbation
+// instead of the 2^-8 absolute spacing of BF16 values near one.
 template <class T>
-__device__ __forceinline__ float ld_s(const SbScalar* p, int i) {
-    return (float)reinterpret_cast<const T*>(p)[i];
+__device__ __forceinline__ float ld_s(const SbScalar* p, int i, float base) {
+    (void)base;
+    return reinterpret_cast<const float*>(p)[i];
 }
 template <>
-__device__ __forceinline__ float ld_s<__nv_bfloat16>(const SbScalar* p, int i) {
-    return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(p)[i]);
+__device__ __forceinline__ float ld_s<__nv_bfloat16>(const SbScalar* p, int i, float base) {
+    return base + __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(p)[i]);
 }
 template <class T>
-__device__ __forceinline__ void st_s(SbScalar* p, int i, float v) {
-    reinterpret_cast<T*>(p)[i] = v;
+__device__ __forceinline__ void st_s(SbScalar* p, int i, float v, float base) {
+    (void)base;
+    reinterpret_cast<float*>(p)[i] = v;
 }
 template <>
-__device__ __forceinline__ void st_s<__nv_bfloat16>(SbScalar* p, int i, float v) {
-    reinterpret_cast<__nv_bfloat16*>(p)[i] = __float2bfloat16_rn(v);
+__device__ __forceinline__ void st_s<__nv_bfloat16>(SbScalar* p, int i, float v, float base) {
+    reinterpret_cast<__nv_bfloat16*>(p)[i] = __float2bfloat16_rn(v - base);
+}
+// Element copy between two fields of the same base (exact).
+template <class T>
+__device__ __forceinline__ void cp_s(SbScalar* dst, const SbScalar* src, int i) {
+    reinterpret_cast<T*>(dst)[i] = reinterpret_cast<const T*>(src)[i];
 }
 
 template <class T>
-__device__ __forceinline__ float gather_s(const SbScalar* f, const SStencil& s) {
-    const float l = blerp(ld_s<T>(f, s.i00), ld_s<T>(f, s.i01), s.b);
-    const float u = blerp(ld_s<T>(f, s.i10), ld_s<T>(f, s.i11), s.b);
+__device__ __forceinline__ float gather_s(const SbScalar* f, const SStencil& s, float base) {
+    const float l = blerp(ld_s<T>(f, s.i00, base), ld_s<T>(f, s.i01, base), s.b);
+    const float u = blerp(ld_s<T>(f, s.i10, base), ld_s<T>(f, s.i11, base), s.b);
     return blerp(l, u, s.a);
 }
 

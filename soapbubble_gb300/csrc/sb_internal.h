@@ -111,10 +111,13 @@ enum SbStage {
 };
 
 cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s);
-cudaError_t launch_mass(const SbGrid& g, const SbFields& f, int storage, cudaStream_t s);
-// FP32 <-> stored thickness / surfactant field (n elements).
-cudaError_t launch_store(SbScalar* dst, const float* src, int n, int storage, cudaStream_t s);
-cudaError_t launch_load(float* dst, const SbScalar* src, int n, int storage, cudaStream_t s);
+cudaError_t launch_mass(const SbGrid& g, const SbPhys& ph, const SbFields& f, int storage,
+                        cudaStream_t s);
+// FP32 <-> stored thickness / surfactant field (n elements, offset `base`).
+cudaError_t launch_store(SbScalar* dst, const float* src, int n, float base, int storage,
+                         cudaStream_t s);
+cudaError_t launch_load(float* dst, const SbScalar* src, int n, float base, int storage,
+                        cudaStream_t s);
 
 // Scalars of one system of a solve, written by the block that completes the
 // system's last row in a phase and read in the next phase (double buffered).

@@ -56,7 +56,6 @@ __device__ __forceinline__ Pos pos_of(const Frame& F, const Trace& T, const SbGr
 template <class T>
 __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
-    (void)ph;
     (void)cur;
     if (idx == 0) {
         f.stats->distortion_bits = 0u;
@@ -80,7 +79,7 @@ __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& 
     const CStencil cb = centred_stencil(g, pos_of(F, Tb, g), 0.0f);
     const f3 db = map_at_stencil(f.bwd[cur], F, cb, g.nT, g.h);
     f.bwd[cur ^ 1][idx] = map_entry_from_disp(g, F, db);
-    f.gam_adv[idx] = gather_s<T>(f.gam, sstencil_of(g, cb));
+    f.gam_adv[idx] = gather_s<T>(f.gam, sstencil_of(g, cb), ph.base_gam);
 
     // air flow = initial wind + corridor(t); NaN -> 0
     const float wg = f.step->windg;
@@ -142,10 +141,10 @@ __device__ __forceinline__ void velocity_cell(const SbGrid& g, const SbPhys& ph,
 template <class T>
 __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
-    (void)ph;
     (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
-    if (ld_s<T>(f.eta, idx) == 0.0f) {
+    const float be = ph.base_eta;
+    if (ld_s<T>(f.eta, idx, be) == 0.0f) {
         f.eta_adv[idx] = 0.0f;
         return;
     }
@@ -163,8 +162,8 @@ __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, c
         const SStencil s2 = scalar_stencil(g, q2);
         const float sDelta = gather(f.eta_delta, s1);
         attrib += (1.0f - blend) * kW5[k] *
-                  (gather_s<T>(f.eta_initL, s2) + sDelta + gather(f.eta_deltaL, s2));
-        attrib += blend * kW5[k] * (gather_s<T>(f.eta_init, s1) + sDelta);
+                  (gather_s<T>(f.eta_initL, s2, be) + sDelta + gather(f.eta_deltaL, s2));
+        attrib += blend * kW5[k] * (gather_s<T>(f.eta_init, s1, be) + sDelta);
     }
     f.eta_adv[idx] = fmaxf(0.0f, attrib);
 }
@@ -314,7 +313,6 @@ __device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, floa
 template <class T>
 __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
-    (void)ph;
     (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
     const int nP = g.nP;
@@ -324,12 +322,12 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
     const float gNew = f.x[idx];
     float mdtdiv;  // -dt * div
     if (gamma_clamped(gNew, gmax)) {
-        st_s<T>(f.gam, idx, gmax);
+        st_s<T>(f.gam, idx, gmax, ph.base_gam);
         f.d_gam[idx] = gmax - gOld;
         mdtdiv = -1.0f;
     } else {
         const float dx = f.dx[idx];
-        st_s<T>(f.gam, idx, gNew);
+        st_s<T>(f.gam, idx, gNew, ph.base_gam);
         f.d_gam[idx] = dx;
         // div = (1 - min(gNew, 2 gOld) / gOld) / dt
         mdtdiv = (gNew > 2.0f * gOld) ? 1.0f : dx / gOld;
@@ -338,10 +336,10 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
     const float e = f.eta_adv[idx];
     const float de = e * mdtdiv + f.step->evapDt;
     if (e + de >= 0.0f) {
-        st_s<T>(f.eta, idx, e + de);
+        st_s<T>(f.eta, idx, e + de, ph.base_eta);
         f.d_eta[idx] = de;
     } else {
-        st_s<T>(f.eta, idx, 0.0f);
+        st_s<T>(f.eta, idx, 0.0f, ph.base_eta);
         f.d_eta[idx] = -e;
     }
 
@@ -393,7 +391,6 @@ __device__ __forceinline__ float warp_max(float v) {
 template <class T>
 __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                            int idx) {
-    (void)ph;
     const int i = idx >> g.logP, j = idx & g.maskP;
     const Frame F = cell_frame(g, i, j);
     const float2* fwd = f.fwd[cur ^ 1];
@@ -407,13 +404,13 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
         const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
         ed += kW5[k] * gather(f.d_eta, s);
         gd += kW5[k] * gather(f.d_gam, s);
-        th += kW5[k] * gather_s<T>(f.eta, s);
-        gm += kW5[k] * gather_s<T>(f.gam, s);
+        th += kW5[k] * gather_s<T>(f.eta, s, ph.base_eta);
+        gm += kW5[k] * gather_s<T>(f.gam, s, ph.base_gam);
     }
     f.eta_delta[idx] = ed;
     f.gam_delta[idx] = gd;
-    f.err_eta[idx] = (th - ed - ld_s<T>(f.eta_init, idx)) * 0.5f;
-    f.err_gam[idx] = (gm - gd - ld_s<T>(f.gam_init, idx)) * 0.5f;
+    f.err_eta[idx] = (th - ed - ld_s<T>(f.eta_init, idx, ph.base_eta)) * 0.5f;
+    f.err_gam[idx] = (gm - gd - ld_s<T>(f.gam_init, idx, ph.base_gam)) * 0.5f;
     // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
     float2 m = fwd[idx];
     const float d1 = dist_from_disp(sample_map(g, bwd, F, frame_pos(F, m.x, m.y)), g.invh);
@@ -511,11 +508,13 @@ __device__ __forceinline__ int nb_index(const SbGrid& g, int i, int j) {
 // clamp to the 3x3 range of the uncorrected field, keep non-negative.  The
 // result goes to the *_adv buffers and is committed in the next phase.
 template <class T>
-__device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbFields& f, int cur, int idx) {
+__device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
+                                               int idx) {
     const int i = idx >> g.logP, j = idx & g.maskP;
     const Frame F = cell_frame(g, i, j);
     const float2* bwd = f.bwd[cur ^ 1];
-    float th = ld_s<T>(f.eta, idx), gm = ld_s<T>(f.gam, idx);
+    const float be = ph.base_eta, bg = ph.base_gam;
+    float th = ld_s<T>(f.eta, idx, be), gm = ld_s<T>(f.gam, idx, bg);
     f3 ds[5];
     sample_map_multi5(g, bwd, F, ds);
 #pragma unroll
@@ -524,11 +523,11 @@ __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbFields& 
         th -= kW5[k] * gather(f.err_eta, s);
         gm -= kW5[k] * gather(f.err_gam, s);
     }
-    float emin = ld_s<T>(f.eta, idx), emax = emin, gmin = ld_s<T>(f.gam, idx), gmx = gmin;
+    float emin = ld_s<T>(f.eta, idx, be), emax = emin, gmin = ld_s<T>(f.gam, idx, bg), gmx = gmin;
     for (int t = -1; t <= 1; ++t)
         for (int p = -1; p <= 1; ++p) {
             const int n = nb_index(g, i + t, j + p);
-            const float ev = ld_s<T>(f.eta, n), gv = ld_s<T>(f.gam, n);
+            const float ev = ld_s<T>(f.eta, n, be), gv = ld_s<T>(f.gam, n, bg);
             emin = fminf(emin, ev); emax = fmaxf(emax, ev);
             gmin = fminf(gmin, gv); gmx = fmaxf(gmx, gv);
         }
@@ -540,17 +539,17 @@ __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbFields& 
 
 // Commit the correction, rotate the BIMOCQ buffers and reset the maps.
 template <class T>
-__device__ __forceinline__ void reinit_commit(const SbFields& f, int cur, int idx) {
+__device__ __forceinline__ void reinit_commit(const SbPhys& ph, const SbFields& f, int cur, int idx) {
     const float e = f.eta_adv[idx], gm = f.gam_adv[idx];
-    st_s<T>(f.eta, idx, e);
-    st_s<T>(f.gam, idx, gm);
-    st_s<T>(f.eta_initL, idx, ld_s<T>(f.eta_init, idx));
+    st_s<T>(f.eta, idx, e, ph.base_eta);
+    st_s<T>(f.gam, idx, gm, ph.base_gam);
+    cp_s<T>(f.eta_initL, f.eta_init, idx);
     f.eta_deltaL[idx] = f.eta_delta[idx];
-    st_s<T>(f.gam_initL, idx, ld_s<T>(f.gam_init, idx));
+    cp_s<T>(f.gam_initL, f.gam_init, idx);
     f.gam_deltaL[idx] = f.gam_delta[idx];
-    st_s<T>(f.eta_init, idx, e);
+    st_s<T>(f.eta_init, idx, e, ph.base_eta);
     f.eta_delta[idx] = 0.0f;
-    st_s<T>(f.gam_init, idx, gm);
+    st_s<T>(f.gam_init, idx, gm, ph.base_gam);
     f.gam_delta[idx] = 0.0f;
     f.bwdprev[idx] = f.bwd[cur ^ 1][idx];
     f.fwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
@@ -587,7 +586,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
                 d.f.stats->reinit = 1;
                 d.f.stats->reinit_total += 1;
             }
-            reinit_correct<T>(d.g, d.f, d.cur, idx);
+            reinit_correct<T>(d.g, d.ph, d.f, d.cur, idx);
         }
     }
     grid.sync();
@@ -596,7 +595,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
         const SbBubbleDesc& d = *descs[tl.x];
         if (!reinit_now(d.f.stats)) continue;
         for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
-            reinit_commit<T>(d.f, d.cur, idx);
+            reinit_commit<T>(d.ph, d.f, d.cur, idx);
     }
 }
 
@@ -622,13 +621,13 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 
 // Mass integrals sum(eta sin theta), sum(gamma sin theta) for conservation checks.
 template <class T>
-__global__ void k_mass(SbGrid g, SbFields f) {
+__global__ void k_mass(SbGrid g, SbPhys ph, SbFields f) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     double me = 0.0, mg = 0.0;
     if (idx < g.N) {
         const double s = (double)g.sin_c[idx >> g.logP];
-        me = (double)ld_s<T>(f.eta, idx) * s;
-        mg = (double)ld_s<T>(f.gam, idx) * s;
+        me = (double)ld_s<T>(f.eta, idx, ph.base_eta) * s;
+        mg = (double)ld_s<T>(f.gam, idx, ph.base_gam) * s;
     }
     me = warp_sum_d(me);
     mg = warp_sum_d(mg);
@@ -641,14 +640,14 @@ __global__ void k_mass(SbGrid g, SbFields f) {
 // FP32 <-> stored type of a thickness or surfactant field (uploads and
 // downloads of BF16-stored fields convert on the device).
 template <class T>
-__global__ void k_store(SbScalar* __restrict__ dst, const float* __restrict__ src, int n) {
+__global__ void k_store(SbScalar* __restrict__ dst, const float* __restrict__ src, int n, float base) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) st_s<T>(dst, i, src[i]);
+    if (i < n) st_s<T>(dst, i, src[i], base);
 }
 template <class T>
-__global__ void k_load(float* __restrict__ dst, const SbScalar* __restrict__ src, int n) {
+__global__ void k_load(float* __restrict__ dst, const SbScalar* __restrict__ src, int n, float base) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = ld_s<T>(src, i);
+    if (i < n) dst[i] = ld_s<T>(src, i, base);
 }
 
 // Co-resident grid of the cooperative re-initialisation kernel (both
@@ -739,26 +738,29 @@ cudaError_t launch_reset_maps(const SbGrid& g, const SbFields& f, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_mass(const SbGrid& g, const SbFields& f, int storage, cudaStream_t s) {
+cudaError_t launch_mass(const SbGrid& g, const SbPhys& ph, const SbFields& f, int storage,
+                        cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(&f.stats->mass_eta, 0, 2 * sizeof(double), s);
     if (e != cudaSuccess) return e;
     const int nb = (g.N + kBlock - 1) / kBlock;
-    if (storage == kStoreBF16) k_mass<__nv_bfloat16><<<nb, kBlock, 0, s>>>(g, f);
-    else k_mass<float><<<nb, kBlock, 0, s>>>(g, f);
+    if (storage == kStoreBF16) k_mass<__nv_bfloat16><<<nb, kBlock, 0, s>>>(g, ph, f);
+    else k_mass<float><<<nb, kBlock, 0, s>>>(g, ph, f);
     return cudaGetLastError();
 }
 
-cudaError_t launch_store(SbScalar* dst, const float* src, int n, int storage, cudaStream_t s) {
+cudaError_t launch_store(SbScalar* dst, const float* src, int n, float base, int storage,
+                         cudaStream_t s) {
     const int nb = (n + kBlock - 1) / kBlock;
-    if (storage == kStoreBF16) k_store<__nv_bfloat16><<<nb, kBlock, 0, s>>>(dst, src, n);
-    else k_store<float><<<nb, kBlock, 0, s>>>(dst, src, n);
+    if (storage == kStoreBF16) k_store<__nv_bfloat16><<<nb, kBlock, 0, s>>>(dst, src, n, base);
+    else k_store<float><<<nb, kBlock, 0, s>>>(dst, src, n, base);
     return cudaGetLastError();
 }
 
-cudaError_t launch_load(float* dst, const SbScalar* src, int n, int storage, cudaStream_t s) {
+cudaError_t launch_load(float* dst, const SbScalar* src, int n, float base, int storage,
+                        cudaStream_t s) {
     const int nb = (n + kBlock - 1) / kBlock;
-    if (storage == kStoreBF16) k_load<__nv_bfloat16><<<nb, kBlock, 0, s>>>(dst, src, n);
-    else k_load<float><<<nb, kBlock, 0, s>>>(dst, src, n);
+    if (storage == kStoreBF16) k_load<__nv_bfloat16><<<nb, kBlock, 0, s>>>(dst, src, n, base);
+    else k_load<float><<<nb, kBlock, 0, s>>>(dst, src, n, base);
     return cudaGetLastError();
 }
 

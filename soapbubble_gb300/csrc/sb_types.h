@@ -36,6 +36,7 @@ enum { kStoreF32 = 0, kStoreBF16 = 1 };
 // Constant physical coefficients of one bubble.
 struct SbPhys {
     float M, Cr, gs, gmax, blend, evap;
+    float base_eta, base_gam;  // BF16 storage: offsets of the eta and gamma fields (else 0)
 };
 
 // Per-step diagnostics written by the kernels.

@@ -2,10 +2,12 @@
 (SB_STORE_BF16: eta, gamma and the BIMOCQ reference fields in BF16 between
 steps, the BIMOCQ change accumulators in FP32, FP32 arithmetic).
 
-BF16 keeps 8 significant bits (unit roundoff 2^-9 ~ 2e-3), so the storage
-variant is compared against the FP64 oracle at that precision, not at the
-1e-5 of the FP32 path: after one step from identical inputs every stored
-field carries at most one BF16 rounding (plus FP32 noise).
+A BF16 field holds the deviation from a per-field base (the BF16-rounded
+mean at upload), so it keeps 8 significant bits of the deviation, not of
+the value.  The storage variant is compared against the FP64 oracle at that
+precision, not at the 1e-5 of the FP32 path: after one step from identical
+inputs every stored field carries at most one BF16 rounding of its
+deviation (plus FP32 noise).
 """
 import numpy as np
 import pytest
@@ -32,24 +34,41 @@ def _bubble(nT, recipe, seed, storage, **kw):
     f = synth.make_fields(recipe, nT, seed)
     gb = GpuBubble(make_params(nT, dt, storage=storage, **kw))
     gb.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    gb.fields = f
     return gb, dt
+
+
+def stored(v, base):
+    """What a BF16 field holds for FP32 values v with offset `base`:
+    base + bf16(v - base), in FP32 arithmetic."""
+    v = np.asarray(v, dtype=np.float32)
+    return (bf16_round(v - np.float32(base)) + np.float32(base)).astype(np.float32)
 
 
 def test_bf16_fields_round_trip_and_memory(gpulib):
     from soapbubble_gb300.bubble import bytes_required, make_params
     gb, _ = _bubble(64, "c0", 3, 1)
     try:
-        x = np.random.default_rng(0).uniform(0.1, 3.0, gb.nTheta * gb.nPhi)
+        # the offsets are the BF16-rounded means of the uploaded fields
+        base_g = bf16_round(np.float32(np.mean(gb.fields.gamma)))
+        base_e = bf16_round(np.float32(np.mean(gb.fields.eta)))
+        x = np.random.default_rng(0).uniform(0.9, 1.1, gb.nTheta * gb.nPhi)
         gb.upload("gamma_init", x)
         np.testing.assert_array_equal(gb.download("gamma_init").ravel(),
-                                      bf16_round(x.astype(np.float32)).astype(np.float64))
+                                      stored(x, base_g).astype(np.float64))
         # the FP32 entry points convert on the device too
-        y = np.random.default_rng(1).uniform(0.1, 3.0, gb.nTheta * gb.nPhi).astype(np.float32)
+        y = np.random.default_rng(1).uniform(0.8, 1.2, gb.nTheta * gb.nPhi).astype(np.float32)
         gb.upload_f32("eta", y)
         out = np.zeros_like(y)
         gb.download_f32("eta", out)
         gb.synchronize()
-        np.testing.assert_array_equal(out, bf16_round(y))
+        np.testing.assert_array_equal(out, stored(y, base_e))
+        # a vanished film stays exactly zero
+        z = np.zeros_like(y)
+        gb.upload_f32("eta", z)
+        gb.download_f32("eta", out)
+        gb.synchronize()
+        assert not out.any()
     finally:
         gb.close()
     # six fields of nTheta x nPhi elements shrink from 4 to 2 bytes
@@ -87,13 +106,9 @@ def test_bf16_step_matches_oracle_at_bf16_precision(oracle, gpulib, case):
         gb.close()
 
 
-def test_bf16_run_stays_finite_and_near_fp32(gpulib):
-    """Twenty steps in each storage.  The surfactant of the c0 recipe is
-    1 + 0.01 U(-1, 1), and BF16's spacing at 1 is 2^-7 = 0.0078: the upload
-    itself quantises most of that perturbation, so the runs differ by
-    percents (velocities, driven by surfactant gradients, by more); the
-    BF16 run stays finite, converges, and keeps thickness and surfactant
-    within 10 % of the FP32 run."""
+def test_bf16_run_stays_near_fp32(gpulib):
+    """Twenty steps in each storage: the BF16 run stays finite, converges,
+    and tracks the FP32 run (thickness and surfactant within 1 %)."""
     a, dt = _bubble(64, "c0", 9, 0)
     b, _ = _bubble(64, "c0", 9, 1)
     try:
@@ -104,7 +119,7 @@ def test_bf16_run_stays_finite_and_near_fp32(gpulib):
             assert np.isfinite(b.download(name)).all(), name
         for name in ("eta", "gamma"):
             x, y = a.download(name), b.download(name)
-            assert P.rel_err(y, x) <= 0.1, (name, P.rel_err(y, x))
+            assert P.rel_err(y, x) <= 1e-2, (name, P.rel_err(y, x))
         assert b.stats().solver_converged == 1
     finally:
         a.close()
