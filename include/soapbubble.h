@@ -122,6 +122,27 @@ int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma,
                      const double* u_theta, const double* u_phi,
                      const double* uair_init, const double* vair_init);
 
+/* Replaces Solver::initThicknessfromPic (kernel/initializer.cu:50-99):
+ * thickness from the first channel (B) of an uncompressed scanline EXR,
+ * resampled to nPhi x nTheta with half-pixel-centred bilinear weights
+ * (cv::resize INTER_LINEAR), rescaled as eta = (C - 0.5) * 0.3 + 0.5; the
+ * BIMOCQ buffers and the maps restart from it.  An empty path keeps
+ * eta = 0.5 (SB_OK); an unreadable file keeps the current thickness and
+ * returns SB_ERR_IO (the reference prints a message and continues). */
+int sb_init_thickness_from_exr(sb_bubble* b, const char* path);
+
+/* Replaces Solver::initAirflowfromPic (kernel/initializer.cu:101-135): the
+ * initial wind from channels G (phi) and R (theta) of the resampled
+ * texture, averaged onto the u_phi and u_theta faces and scaled by the
+ * radius: uair = 0.5 (G(j,i) + G(j,i-1)) r, vair = -0.5 (R(j,i) + R(j+1,i)) r.
+ * Empty path: zero wind (SB_OK); unreadable file: SB_ERR_IO, wind kept. */
+int sb_init_airflow_from_exr(sb_bubble* b, const char* path);
+
+/* Host utility (no device work): one channel of an uncompressed EXR
+ * resampled to width x height as above, into out (width * height values). */
+int sb_exr_load_resized(const char* path, const char* channel, int width, int height,
+                        double* out);
+
 /* Replaces Quantity::copyToGPU for any single buffer (kernel/quantity.cu:3-11),
  * including BIMOCQ buffers and maps (absolute grid coordinates theta/h,
  * phi/h as the reference's forward_t/forward_p).  n = element count. */

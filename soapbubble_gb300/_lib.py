@@ -110,12 +110,16 @@ def lib() -> C.CDLL:
     L.sb_batch_synchronize.argtypes = [H]
     L.sb_batch_stream.argtypes = [H]
     L.sb_batch_stream.restype = C.c_void_p
+    L.sb_init_thickness_from_exr.argtypes = [H, C.c_char_p]
+    L.sb_init_airflow_from_exr.argtypes = [H, C.c_char_p]
+    L.sb_exr_load_resized.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, dp]
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
                  "sb_download_field", "sb_step", "sb_step_timed", "sb_autotune", "sb_upload_field_f32",
                  "sb_download_field_f32", "sb_synchronize", "sb_get_stats",
                  "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
-                 "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize"):
+                 "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
+                 "sb_init_thickness_from_exr", "sb_init_airflow_from_exr", "sb_exr_load_resized"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -134,4 +138,5 @@ EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_run", "sb_write_exr_gray", "sb_mass_integrals_noalloc", "sb_bytes_required",
            "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",
            "sb_batch_step_timed", "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
-           "sb_batch_stream"]
+           "sb_batch_stream", "sb_init_thickness_from_exr", "sb_init_airflow_from_exr",
+           "sb_exr_load_resized"]

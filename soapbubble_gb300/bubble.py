@@ -123,6 +123,16 @@ class GpuBubble:
         check(lib().sb_autotune(self.h, t, dt, out), "sb_autotune")
         return list(out)
 
+    def init_thickness_from_exr(self, path: str) -> None:
+        """Solver::initThicknessfromPic: eta from channel B of an EXR texture
+        (resampled, eta = (C - 0.5) 0.3 + 0.5); '' keeps eta = 0.5."""
+        check(lib().sb_init_thickness_from_exr(self.h, path.encode()), "sb_init_thickness_from_exr")
+
+    def init_airflow_from_exr(self, path: str) -> None:
+        """Solver::initAirflowfromPic: the initial wind from channels G, R of
+        an EXR texture; '' gives zero wind."""
+        check(lib().sb_init_airflow_from_exr(self.h, path.encode()), "sb_init_airflow_from_exr")
+
     def upload_f32(self, name: str, a: np.ndarray) -> None:
         """Asynchronous FP32 upload from a host buffer the caller keeps alive."""
         assert a.dtype == np.float32 and a.flags.c_contiguous
@@ -220,6 +230,15 @@ class GpuBatch:
 
 def stage_names() -> list:
     return [lib().sb_stage_name(i).decode() for i in range(lib().sb_stage_count())]
+
+
+def exr_load_resized(path: str, channel: str, width: int, height: int) -> np.ndarray:
+    """One channel of an uncompressed EXR, resampled to width x height with
+    the bilinear weights the reference's textures go through (host only)."""
+    out = np.zeros((height, width))
+    check(lib().sb_exr_load_resized(path.encode(), channel.encode(), width, height, _dp(out)),
+          "sb_exr_load_resized")
+    return out
 
 
 def bytes_required(params: SbParams) -> int:

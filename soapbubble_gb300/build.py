@@ -28,7 +28,9 @@ LIB_SOURCES = ["sb_step.cu", "sb_solver.cu", "sb_api.cu", "sb_exr.cpp", "sb_noal
 # kernel is instantiated per row width of the largest system it serves, and
 # contraction choices may differ between instantiations, while a bubble must
 # get bit-identical results alone and inside any batch.
-EXTRA_FLAGS = {"sb_solver.cu": ["-fmad=false"]}
+EXTRA_FLAGS = {"sb_solver.cu": ["-fmad=false"],
+               # texture resampling: the same float rounding on x86 and Arm hosts
+               "sb_exr.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 CLI_SOURCES = ["sb_bubble.cpp", "sb_main.cpp"]
 
 

@@ -681,6 +681,63 @@ int sb_download_field(sb_bubble* b, sb_field which, double* dst, size_t n) {
     return SB_OK;
 }
 
+int sb_exr_load_resized(const char* path, const char* channel, int width, int height,
+                        double* out) {
+    if (!path || !channel || !out || width <= 0 || height <= 0)
+        return fail(SB_ERR_INVALID, "bad argument");
+    int w = 0, h = 0;
+    std::vector<float> img;
+    std::string err;
+    if (!read_exr_channel(path, channel, &w, &h, img, err)) return fail(SB_ERR_IO, err);
+    std::vector<float> r((size_t)width * height);
+    resize_linear(img.data(), w, h, r.data(), width, height);
+    for (size_t i = 0; i < r.size(); ++i) out[i] = (double)r[i];
+    return SB_OK;
+}
+
+int sb_init_thickness_from_exr(sb_bubble* b, const char* path) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    if (!path || !*path) return SB_OK;  // eta = 0.5 from sb_create
+    const int nT = b->g.nT, nP = b->g.nP;
+    std::vector<double> c((size_t)nT * nP);
+    int rc = sb_exr_load_resized(path, "B", nP, nT, c.data());
+    if (rc != SB_OK) return rc;
+    for (double& v : c) v = (v - 0.5) * 0.3 + 0.5;  // initializer.cu:74-75
+    SB_CHECK(cudaSetDevice(b->device));
+    rc = set_base(b, false, c.data(), c.size());
+    if (rc == SB_OK) rc = upload_scalar(b, b->f.eta, c.data(), c.size());
+    if (rc == SB_OK) rc = reset_bimocq(b);
+    if (rc == SB_OK) {
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "thickness init");
+    }
+    return rc;
+}
+
+int sb_init_airflow_from_exr(sb_bubble* b, const char* path) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    const int nT = b->g.nT, nP = b->g.nP;
+    const size_t N = (size_t)nT * nP, Nv = (size_t)(nT - 1) * nP;
+    std::vector<double> u(N, 0.0), v(Nv, 0.0);
+    if (path && *path) {
+        std::vector<double> G(N), R(N);
+        int rc = sb_exr_load_resized(path, "G", nP, nT, G.data());
+        if (rc == SB_OK) rc = sb_exr_load_resized(path, "R", nP, nT, R.data());
+        if (rc != SB_OK) return rc;
+        const double r = b->params.radius;
+        for (int j = 0; j < nT; ++j)
+            for (int i = 0; i < nP; ++i) {
+                const size_t c = (size_t)j * nP + i;
+                u[c] = 0.5 * (G[c] + G[(size_t)j * nP + (i + nP - 1) % nP]) * r;
+                if (j < nT - 1) v[c] = -0.5 * (R[c] + R[c + nP]) * r;
+            }
+    }
+    SB_CHECK(cudaSetDevice(b->device));
+    int rc = upload_f32(b, b->f.uair_init, u.data(), N);
+    if (rc == SB_OK) rc = upload_f32(b, b->f.vair_init, v.data(), Nv);
+    return rc;
+}
+
 int sb_upload_fields(sb_bubble* b, const double* eta, const double* gamma, const double* u_theta,
                      const double* u_phi, const double* uair_init, const double* vair_init) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");

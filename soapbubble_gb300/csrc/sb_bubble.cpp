@@ -1,4 +1,5 @@
 // Bubble class and config.txt reader over the C ABI.
+#include <cstdio>
 #include <fstream>
 #include <stdexcept>
 #include <string>
@@ -35,14 +36,20 @@ Bubble::Bubble(double radius, double H, double U, double c_m, double Gamma_m, do
     params_.frames = frames;
     params_.device = device;
     params_.blendCoeff = blendCoeff;
-    if (!thicknessImage_.empty())
-        throw std::runtime_error("thickness images are not supported yet: " + thicknessImage_);
     check(sb_create(&params_, &handle_), "sb_create");
 }
 
 Bubble::~Bubble() { sb_destroy(handle_); }
 
 void Bubble::run() {
+    // Bubble::run initialises from the textures first (kernel/bubble.cu:2640-2641);
+    // like the reference, a missing texture leaves the defaults in place
+    if (sb_init_thickness_from_exr(handle_, thicknessImage_.c_str()) != SB_OK)
+        std::fprintf(stderr, "No thickness image provided, initialize with eta = 0.5 (%s)\n",
+                     sb_last_error());
+    if (sb_init_airflow_from_exr(handle_, "../init/velocityfield_512.exr") != SB_OK)
+        std::fprintf(stderr, "No airflow image provided, initialize with zero (%s)\n",
+                     sb_last_error());
     if (!outputDir_.empty()) {
         // create the output directory (one level), as the reference does
         mkdir(outputDir_.c_str(), 0755);
