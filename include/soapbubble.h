@@ -69,6 +69,12 @@ typedef struct {
                              and surfactant fields between steps (eta, gamma and the BIMOCQ
                              reference fields *_init, *_init_last; the *_delta accumulators
                              stay FP32); arithmetic is FP32 either way */
+    /* the reference's compile-time switches as runtime options (include/header.cuh:89-97) */
+    int plain_advection;      /* 1: as without BIMOCQ: thickness advected like gamma
+                                 (advectionAllCentered, kernel/bubble.cu:937-961), no
+                                 characteristic maps updated, no re-initialisation */
+    int single_step_velocity; /* 1: as without RUNGE_KUTTA: the velocity advection traces in
+                                 one step (kernel/bubble.cu:689-730 skipped) */
 } sb_params;
 
 enum { SB_STORE_FP32 = 0, SB_STORE_BF16 = 1 };

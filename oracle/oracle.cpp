@@ -460,10 +460,12 @@ void updateMappingKernel(const sb_oracle_params* p, const Ctx& c, const double* 
 }
 
 // Shared body of advectionVSpherePhiKernel (bubble.cu:639-768) and
-// advectionVSphereThetaKernel (bubble.cu:775-904): RUNGE_KUTTA great-circle
-// backtrace with parallel transport of the sampled velocity.
+// advectionVSphereThetaKernel (bubble.cu:775-904): great-circle backtrace
+// with parallel transport of the sampled velocity; with RUNGE_KUTTA (rk2) the
+// direction is corrected at the half step first (bubble.cu:689-730).
 double advectVelocity(const Ctx& c, const double* velPhiInput, const double* velThetaInput,
-                      double dt, d2 gId, double guTheta, double guPhi, bool outPhi) {
+                      double dt, d2 gId, double guTheta, double guPhi, bool outPhi,
+                      bool rk2) {
     d2 gCoord = gId * c.gridLen;
     double sinTheta = std::sin(gCoord.x), cosTheta = std::cos(gCoord.x);
     double sinPhi = std::sin(gCoord.y), cosPhi = std::cos(gCoord.y);
@@ -476,22 +478,24 @@ double advectVelocity(const Ctx& c, const double* velPhiInput, const double* vel
     u = guTheta * eTheta + guPhi * ePhi;
     u_norm = length(u);
     if (u_norm > 0) { u_ = normalize(u); v_ = cross(w_, u_); } else { return u_norm; }
-    deltaS = -0.5 * u_norm * dt;
-    d3 midx = u_ * std::sin(deltaS) + w_ * std::cos(deltaS);
-    d2 midCoord = {safe_acos(midx.z), std::atan2(midx.y, midx.x)};
-    d2 midId = midCoord * c.invGridLen;
-    double muTheta = sampleVTheta(c, velThetaInput, midId, pitch);
-    double muPhi = sampleVPhi(c, velPhiInput, midId, pitch);
-    d3 mu = {muTheta * std::cos(midCoord.x) * std::cos(midCoord.y) - muPhi * std::sin(midCoord.y),
-             muTheta * std::cos(midCoord.x) * std::sin(midCoord.y) + muPhi * std::cos(midCoord.y),
-             -muTheta * std::sin(midCoord.x)};
-    d3 uCircleMid_ = u_ * std::cos(deltaS) - w_ * std::sin(deltaS);
-    d3 vCircleMid_ = cross(midx, uCircleMid_);
-    double mguTheta = dot(mu, vCircleMid_);
-    double mguPhi = dot(mu, uCircleMid_);
-    u = mguPhi * u_ + mguTheta * v_;
-    u_norm = length(u);
-    if (u_norm > 0) { u_ = normalize(u); v_ = cross(w_, u_); } else { return u_norm; }
+    if (rk2) {
+        deltaS = -0.5 * u_norm * dt;
+        d3 midx = u_ * std::sin(deltaS) + w_ * std::cos(deltaS);
+        d2 midCoord = {safe_acos(midx.z), std::atan2(midx.y, midx.x)};
+        d2 midId = midCoord * c.invGridLen;
+        double muTheta = sampleVTheta(c, velThetaInput, midId, pitch);
+        double muPhi = sampleVPhi(c, velPhiInput, midId, pitch);
+        d3 mu = {muTheta * std::cos(midCoord.x) * std::cos(midCoord.y) - muPhi * std::sin(midCoord.y),
+                 muTheta * std::cos(midCoord.x) * std::sin(midCoord.y) + muPhi * std::cos(midCoord.y),
+                 -muTheta * std::sin(midCoord.x)};
+        d3 uCircleMid_ = u_ * std::cos(deltaS) - w_ * std::sin(deltaS);
+        d3 vCircleMid_ = cross(midx, uCircleMid_);
+        double mguTheta = dot(mu, vCircleMid_);
+        double mguPhi = dot(mu, uCircleMid_);
+        u = mguPhi * u_ + mguTheta * v_;
+        u_norm = length(u);
+        if (u_norm > 0) { u_ = normalize(u); v_ = cross(w_, u_); } else { return u_norm; }
+    }
     deltaS = -u_norm * dt;
     d3 px = u_ * std::sin(deltaS) + w_ * std::cos(deltaS);
     d2 pCoord = {safe_acos(px.z), std::atan2(px.y, px.x)};
@@ -1081,28 +1085,40 @@ void sb_oracle_advection(const sb_oracle_params* p, sb_oracle_state* s) {
     const double dt = p->dt;
     const double* uth = s->uth;
     const double* uph = s->uph;
+    const bool rk2 = !p->single_step_velocity;
     CELL_LOOP(p->nTheta - 1, {
         d2 gId = d2{(double)thetaId, (double)phiId} + d2{1.0, 0.0};
         double guTheta = uth[cell];
         double guPhi = sampleVPhi(c, uph, gId, (size_t)nP);
-        uthN[cell] = advectVelocity(c, uph, uth, dt, gId, guTheta, guPhi, false);
+        uthN[cell] = advectVelocity(c, uph, uth, dt, gId, guTheta, guPhi, false, rk2);
     })
     CELL_LOOP(p->nTheta, {
         d2 gId = d2{(double)thetaId, (double)phiId} + d2{0.5, -0.5};
         double guTheta = sampleVTheta(c, uth, gId, (size_t)nP);
         double guPhi = uph[cell];
-        uphN[cell] = advectVelocity(c, uph, uth, dt, gId, guTheta, guPhi, true);
+        uphN[cell] = advectVelocity(c, uph, uth, dt, gId, guTheta, guPhi, true, rk2);
     })
-    advectionCenteredBimocq(p, c, etaN.data(), s->eta, s->eta_init, s->eta_delta,
-                            s->eta_initLast, s->eta_deltaLast, s->bwd_t, s->bwd_p,
-                            s->bwdprev_t, s->bwdprev_p);
-    // bubble.cu:910-931: concentration without BIMOCQ
     const double* gam = s->gamma;
-    CELL_LOOP(p->nTheta, {
-        d2 gId = d2{(double)thetaId, (double)phiId} + d2{0.5, 0.0};
-        d2 traceId = traceGreatCircle(c, uth, uph, dt, gId, (size_t)nP);
-        gamN[cell] = sampleCentered(c, gam, traceId, (size_t)nP);
-    })
+    if (p->plain_advection) {
+        // advectionAllCentered (bubble.cu:937-961): both scalars at the trace
+        const double* eta = s->eta;
+        CELL_LOOP(p->nTheta, {
+            d2 gId = d2{(double)thetaId, (double)phiId} + d2{0.5, 0.0};
+            d2 traceId = traceGreatCircle(c, uth, uph, dt, gId, (size_t)nP);
+            etaN[cell] = sampleCentered(c, eta, traceId, (size_t)nP);
+            gamN[cell] = sampleCentered(c, gam, traceId, (size_t)nP);
+        })
+    } else {
+        advectionCenteredBimocq(p, c, etaN.data(), s->eta, s->eta_init, s->eta_delta,
+                                s->eta_initLast, s->eta_deltaLast, s->bwd_t, s->bwd_p,
+                                s->bwdprev_t, s->bwdprev_p);
+        // bubble.cu:910-931: concentration without BIMOCQ
+        CELL_LOOP(p->nTheta, {
+            d2 gId = d2{(double)thetaId, (double)phiId} + d2{0.5, 0.0};
+            d2 traceId = traceGreatCircle(c, uth, uph, dt, gId, (size_t)nP);
+            gamN[cell] = sampleCentered(c, gam, traceId, (size_t)nP);
+        })
+    }
     std::memcpy(s->uth, uthN.data(), Nv * 8);
     std::memcpy(s->uph, uphN.data(), N * 8);
     std::memcpy(s->eta, etaN.data(), N * 8);
@@ -1209,14 +1225,19 @@ void sb_oracle_reinit(const sb_oracle_params* p, sb_oracle_state* s) {
     initMapping(p->nTheta, p->nPhi, s->bwd_t, s->bwd_p);
 }
 
-// Solver::stepForward (kernel/solver.cu:260-292)
+// Solver::stepForward (kernel/solver.cu:260-292); without BIMOCQ the maps
+// are neither updated nor checked for distortion (solver.cu:265-288), while
+// bodyforce still accumulates the changes through the (identity) maps
 int sb_oracle_step(const sb_oracle_params* p, sb_oracle_state* s, sb_oracle_stats* st) {
     sb_oracle_stats local{};
-    sb_oracle_update_maps(p, s);
+    if (!p->plain_advection) sb_oracle_update_maps(p, s);
     sb_oracle_advection(p, s);
     int rc = sb_oracle_bodyforce(p, s, &local);
-    sb_oracle_distortion(p, s, &local);
-    bool re = p->force_reinit < 0 ? (local.distortion > 4.f) : (p->force_reinit != 0);
+    bool re = false;
+    if (!p->plain_advection) {
+        sb_oracle_distortion(p, s, &local);
+        re = p->force_reinit < 0 ? (local.distortion > 4.f) : (p->force_reinit != 0);
+    }
     if (re) sb_oracle_reinit(p, s);
     local.reinit = re ? 1 : 0;
     if (st) *st = local;

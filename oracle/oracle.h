@@ -43,6 +43,9 @@ typedef struct {
     double solver_tol;   /* relative residual target of the implicit solve */
     int solver_max_iter;
     int nthreads;        /* OpenMP threads (0 = default) */
+    /* the reference's compile-time switches (include/header.cuh:89, 96) */
+    int plain_advection;       /* 1: BIMOCQ undefined (advectionAllCentered, no maps) */
+    int single_step_velocity;  /* 1: RUNGE_KUTTA undefined (velocity traced in one step) */
 } sb_oracle_params;
 
 typedef struct {

@@ -31,7 +31,7 @@ class Params(C.Structure):
         ("gammaMax", C.c_double), ("evapRate", C.c_double), ("W1", C.c_double),
         ("W2", C.c_double), ("blend", C.c_double), ("U", C.c_double), ("strict", C.c_int),
         ("force_reinit", C.c_int), ("solver_tol", C.c_double), ("solver_max_iter", C.c_int),
-        ("nthreads", C.c_int),
+        ("nthreads", C.c_int), ("plain_advection", C.c_int), ("single_step_velocity", C.c_int),
     ]
 
 

@@ -30,7 +30,8 @@ class SbParams(C.Structure):
         ("blendCoeff", C.c_double), ("device", C.c_int),
         ("gs_scale", C.c_double), ("M_scale", C.c_double), ("solver_mode", C.c_int),
         ("solver_tol", C.c_double), ("solver_max_iter", C.c_int), ("force_reinit", C.c_int),
-        ("nu_scale", C.c_double), ("storage", C.c_int),
+        ("nu_scale", C.c_double), ("storage", C.c_int), ("plain_advection", C.c_int),
+        ("single_step_velocity", C.c_int),
     ]
 
 

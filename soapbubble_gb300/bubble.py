@@ -33,7 +33,8 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
                 DT: Optional[float] = None, frames: int = 1, solver_mode: int = 0,
                 solver_tol: float = 1e-6, solver_max_iter: int = 1000, force_reinit: int = 0,
                 gs_scale: float = 0.0, M_scale: float = 0.0, nu_scale: float = 0.0,
-                device: int = 0, storage: int = 0) -> SbParams:
+                device: int = 0, storage: int = 0, plain_advection: int = 0,
+                single_step_velocity: int = 0) -> SbParams:
     p = default_params()
     p.nTheta, p.dt, p.radius, p.H, p.Gamma_m, p.T = nTheta, dt, radius, H, Gamma_m, T
     p.blendCoeff = blendCoeff
@@ -43,6 +44,8 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
     p.force_reinit, p.gs_scale, p.M_scale, p.device = force_reinit, gs_scale, M_scale, device
     p.nu_scale = nu_scale
     p.storage = storage  # 0: FP32, 1: BF16 thickness / surfactant fields
+    p.plain_advection = plain_advection            # 1: BIMOCQ off
+    p.single_step_velocity = single_step_velocity  # 1: RUNGE_KUTTA off
     return p
 
 

@@ -421,6 +421,9 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     b->solver.precond = 1;
     b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
     b->storage = p->storage;
+    b->ph.plain_adv = p->plain_advection ? 1 : 0;
+    b->ph.single_step = p->single_step_velocity ? 1 : 0;
+    if (b->ph.plain_adv) b->force_reinit = 0;  // no maps: nothing to re-initialise
     // BF16 storage: offsets of the initial fields (eta = 0.5, gamma = 1)
     b->ph.base_eta = b->storage == kStoreBF16 ? 0.5f : 0.0f;
     b->ph.base_gam = b->storage == kStoreBF16 ? 1.0f : 0.0f;

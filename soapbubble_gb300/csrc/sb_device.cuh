@@ -410,10 +410,13 @@ struct Trace {
 };
 
 // traceGreatCircle (kernel/bubble.cu:416-506) from the frame base with the
-// base velocity (gt, gp) already known.  dt > 0 traces backward.
+// base velocity (gt, gp) already known.  dt > 0 traces backward.  rk2: the
+// direction is first corrected with the velocity at the half step (the
+// scalar traces always; the velocity advection under RUNGE_KUTTA,
+// bubble.cu:689-730).
 __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restrict__ uth,
                                           const float* __restrict__ uph, const Frame& F,
-                                          float gt, float gp, float dt) {
+                                          float gt, float gp, float dt, bool rk2 = true) {
     Trace T;
     T.moved = false;
     T.fail = 0.0f;
@@ -426,28 +429,30 @@ __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restri
     if (!(un > 0.0f)) { T.fail = un; return T; }
     f3 u_ = (1.0f / un) * u;
     f3 v_ = cross3(w, u_);
-    float dS = -0.5f * un * dt;
-    float sd, sh, ch;
-    fsincos(0.5f * dS, &sh, &ch);
-    sd = 2.0f * sh * ch;
-    float cdm1 = -2.0f * sh * sh;
-    const f3 dmid = sd * u_ + cdm1 * w;
-    const f3 midx = w + dmid;
-    const Pos qm = pos_from_disp(F, dmid, g.invh, g.nT);
-    float mt, mp;
-    velocity_at(g, uth, uph, qm, mt, mp);
-    f3 beth, beph;
-    basis_at(midx, beth, beph);
-    const f3 mu = mt * beth + mp * beph;
-    const f3 uCircleMid = (1.0f + cdm1) * u_ - sd * w;
-    const f3 vCircleMid = cross3(midx, uCircleMid);
-    const float mgt = dot3(mu, vCircleMid);
-    const float mgp = dot3(mu, uCircleMid);
-    u = mgp * u_ + mgt * v_;
-    un = len3(u);
-    if (!(un > 0.0f)) { T.fail = un; return T; }
-    u_ = (1.0f / un) * u;
-    v_ = cross3(w, u_);
+    float dS, sd, sh, ch, cdm1;
+    if (rk2) {
+        dS = -0.5f * un * dt;
+        fsincos(0.5f * dS, &sh, &ch);
+        sd = 2.0f * sh * ch;
+        cdm1 = -2.0f * sh * sh;
+        const f3 dmid = sd * u_ + cdm1 * w;
+        const f3 midx = w + dmid;
+        const Pos qm = pos_from_disp(F, dmid, g.invh, g.nT);
+        float mt, mp;
+        velocity_at(g, uth, uph, qm, mt, mp);
+        f3 beth, beph;
+        basis_at(midx, beth, beph);
+        const f3 mu = mt * beth + mp * beph;
+        const f3 uCircleMid = (1.0f + cdm1) * u_ - sd * w;
+        const f3 vCircleMid = cross3(midx, uCircleMid);
+        const float mgt = dot3(mu, vCircleMid);
+        const float mgp = dot3(mu, uCircleMid);
+        u = mgp * u_ + mgt * v_;
+        un = len3(u);
+        if (!(un > 0.0f)) { T.fail = un; return T; }
+        u_ = (1.0f / un) * u;
+        v_ = cross3(w, u_);
+    }
     dS = -un * dt;
     fsincos(0.5f * dS, &sh, &ch);
     sd = 2.0f * sh * ch;

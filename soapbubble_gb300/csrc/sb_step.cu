@@ -69,17 +69,26 @@ __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& 
     float gt, gp;
     velocity_at(g, f.uth, f.uph, q0, gt, gp);
 
-    // forward map: trace forward in time (negative step), sample the old map
-    const Trace Tf = trace_gc(g, f.uth, f.uph, F, gt, gp, -dt);
-    const f3 df = sample_map(g, f.fwd[cur], F, pos_of(F, Tf, g));
-    f.fwd[cur ^ 1][idx] = map_entry_from_disp(g, F, df);
+    if (ph.plain_adv) {
+        // advectionAllCentered (bubble.cu:937-961): thickness and gamma at the
+        // backward trace; the maps are not used
+        const Trace Tb = trace_gc(g, f.uth, f.uph, F, gt, gp, dt);
+        const SStencil sb = sstencil_of(g, centred_stencil(g, pos_of(F, Tb, g), 0.0f));
+        f.eta_adv[idx] = gather_s<T>(f.eta, sb, ph.base_eta);
+        f.gam_adv[idx] = gather_s<T>(f.gam, sb, ph.base_gam);
+    } else {
+        // forward map: trace forward in time (negative step), sample the old map
+        const Trace Tf = trace_gc(g, f.uth, f.uph, F, gt, gp, -dt);
+        const f3 df = sample_map(g, f.fwd[cur], F, pos_of(F, Tf, g));
+        f.fwd[cur ^ 1][idx] = map_entry_from_disp(g, F, df);
 
-    // backward map and gamma share the backward trace
-    const Trace Tb = trace_gc(g, f.uth, f.uph, F, gt, gp, dt);
-    const CStencil cb = centred_stencil(g, pos_of(F, Tb, g), 0.0f);
-    const f3 db = map_at_stencil(f.bwd[cur], F, cb, g.nT, g.h);
-    f.bwd[cur ^ 1][idx] = map_entry_from_disp(g, F, db);
-    f.gam_adv[idx] = gather_s<T>(f.gam, sstencil_of(g, cb), ph.base_gam);
+        // backward map and gamma share the backward trace
+        const Trace Tb = trace_gc(g, f.uth, f.uph, F, gt, gp, dt);
+        const CStencil cb = centred_stencil(g, pos_of(F, Tb, g), 0.0f);
+        const f3 db = map_at_stencil(f.bwd[cur], F, cb, g.nT, g.h);
+        f.bwd[cur ^ 1][idx] = map_entry_from_disp(g, F, db);
+        f.gam_adv[idx] = gather_s<T>(f.gam, sstencil_of(g, cb), ph.base_gam);
+    }
 
     // air flow = initial wind + corridor(t); NaN -> 0
     const float wg = f.step->windg;
@@ -94,11 +103,12 @@ __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& 
 // Velocity self-advection with parallel transport (RUNGE_KUTTA path).
 __device__ __forceinline__ float advect_velocity(const SbGrid& g, const float* __restrict__ uth,
                                                  const float* __restrict__ uph, const Frame& F,
-                                                 float gt, float gp, float dt, bool outPhi) {
+                                                 float gt, float gp, float dt, bool outPhi,
+                                                 bool rk2) {
     const f3 w = {F.s0, 0.0f, F.c0};
     // a zero or NaN speed stops the trace; the reference then writes that
     // speed (bubble.cu:689-692, 727-730)
-    const Trace T = trace_gc(g, uth, uph, F, gt, gp, dt);
+    const Trace T = trace_gc(g, uth, uph, F, gt, gp, dt, rk2);
     if (!T.moved) return T.fail;
     const f3 P = w + T.d;
     const Pos qp = pos_from_disp(F, T.d, g.invh, g.nT);
@@ -118,7 +128,6 @@ __device__ __forceinline__ float advect_velocity(const SbGrid& g, const float* _
 
 __device__ __forceinline__ void velocity_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
-    (void)ph;
     (void)cur;
     const int i = idx >> g.logP, j = idx & g.maskP;
     const float dt = f.step->dt;
@@ -126,13 +135,13 @@ __device__ __forceinline__ void velocity_cell(const SbGrid& g, const SbPhys& ph,
         const Frame F = face_frame_uphi(g, i, j);
         const float gp = f.uph[idx];
         const float gt = sample_utheta(g, f.uth, frame_pos(F, 0.0f, 0.0f));
-        f.uph_adv[idx] = advect_velocity(g, f.uth, f.uph, F, gt, gp, dt, true);
+        f.uph_adv[idx] = advect_velocity(g, f.uth, f.uph, F, gt, gp, dt, true, !ph.single_step);
     }
     if (i < g.nT - 1) {
         const Frame F = face_frame_utheta(g, i, j);
         const float gt = f.uth[idx];
         const float gp = sample_uphi(g, f.uph, frame_pos(F, 0.0f, 0.0f));
-        f.uth_adv[idx] = advect_velocity(g, f.uth, f.uph, F, gt, gp, dt, false);
+        f.uth_adv[idx] = advect_velocity(g, f.uth, f.uph, F, gt, gp, dt, false, !ph.single_step);
     }
 }
 
@@ -142,6 +151,7 @@ template <class T>
 __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
     (void)cur;
+    if (ph.plain_adv) return;  // thickness advected by k_advect_maps
     const int i = idx >> g.logP, j = idx & g.maskP;
     const float be = ph.base_eta;
     if (ld_s<T>(f.eta, idx, be) == 0.0f) {

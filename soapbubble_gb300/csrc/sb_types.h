@@ -37,6 +37,8 @@ enum { kStoreF32 = 0, kStoreBF16 = 1 };
 struct SbPhys {
     float M, Cr, gs, gmax, blend, evap;
     float base_eta, base_gam;  // BF16 storage: offsets of the eta and gamma fields (else 0)
+    int plain_adv;    // 1: thickness advected like gamma, no characteristic maps (BIMOCQ off)
+    int single_step;  // 1: velocity traced in one step (RUNGE_KUTTA off)
 };
 
 // Per-step diagnostics written by the kernels.

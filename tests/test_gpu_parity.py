@@ -185,3 +185,41 @@ def test_uniform_film_without_forcing_is_steady(gpulib):
         np.testing.assert_allclose(gb.download("gamma"), 1.3, atol=2e-7)
         assert np.max(np.abs(gb.download("u_theta"))) < 1e-6
         assert np.max(np.abs(gb.download("u_phi"))) < 1e-6
+
+
+# The reference's compile-time switches as runtime options: BIMOCQ off
+# (advectionAllCentered, no maps) and RUNGE_KUTTA off (one-step velocity
+# trace), alone and together, against the oracle built with the same
+# switches.
+SWITCHES = [(1, 0), (0, 1), (1, 1)]
+
+
+@pytest.mark.parametrize("sw", SWITCHES, ids=lambda s: f"plain{s[0]}-single{s[1]}")
+def test_switch_variants_match_oracle(oracle, gpulib, sw):
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    plain, single = sw
+    nT, dt, seed = 64, 0.005, 4321
+    f = synth.make_fields("c0", nT, seed)
+    op = oracle.default_params(nT, dt_s=dt)
+    op.t = 0.5
+    op.plain_advection, op.single_step_velocity = plain, single
+    ob = oracle.OracleBubble(op, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    for _ in range(5):
+        ob.step()
+    gb = GpuBubble(make_params(nT, dt, solver_tol=1e-10, solver_max_iter=2000,
+                               plain_advection=plain, single_step_velocity=single))
+    try:
+        P.sync_state(gb, ob)
+        for k in range(3):
+            gb.step(1, 0.5, dt)
+            ob.step()
+            err = P.compare(gb, ob, list(PHYS))
+            for name in PHYS:
+                assert err[name] <= TOL_FIELD, (k, name, err[name])
+        if plain:
+            # no maps: they stay the identity, and nothing is re-initialised
+            assert err["fwd"] <= TOL_MAP_CELLS and err["bwd"] <= TOL_MAP_CELLS
+            assert gb.stats().reinits == 0
+    finally:
+        gb.close()
