@@ -745,28 +745,34 @@ __device__ __forceinline__ void acc_zero(unsigned long long* a, int n, int tid, 
     for (int k = tid; k < n; k += nthreads) a[k] = 0ull;
 }
 
-// Rows r0, r0 + stride, ... (n of them) of system b were computed by this
-// block; warp w left its share of the k-th in s_part[k][w].  Folds each
-// row's warp shares in warp order and adds the row's partials into the
-// phase's accumulator buffer.
-__device__ __forceinline__ void publish_rows(const SbSolveSet& S, int b, int p, int n,
-                                             ff (*s_part)[kWarps][3]) {
+// Values of the dot products a phase produces: q = A p gives one (p.q, or
+// |r|^2 of the refinement check), the preconditioner two (r.z, r.r), the
+// set-up three (r.z, r.r, |b|^2).
+__device__ __forceinline__ int phase_values(int p) { return p == 0 ? 3 : (p & 1) ? 1 : 2; }
+
+// A row of system b is done: every thread left its shares of the phase's
+// values in tpart[v][thread].  Warp v sums value v over the block in a fixed
+// order (each lane 8 threads' shares, then the lanes by shuffle tree) and
+// adds the row's partial into the phase's exact accumulator.
+__device__ __forceinline__ void reduce_row(const SbSolveSet& S, int b, int p, const ff* tpart) {
     __syncthreads();
-    if (threadIdx.x < 3 * n) {
-        const int k = threadIdx.x / 3, v = threadIdx.x - 3 * k;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < phase_values(p)) {
+        const ff* t = tpart + warp * kSolveBlock;
         ff x = ff_zero();
 #pragma unroll
-        for (int w = 0; w < kWarps; ++w) x = ff_add(x, s_part[k][w][v]);
-        acc_add_ff(acc_buf(S, b, p), v, x);
+        for (int k = 0; k < kWarps; ++k) x = ff_add(x, t[lane + 32 * k]);
+        x = ff_warp_sum(x);
+        if (lane == 0) acc_add_ff(acc_buf(S, b, p), warp, x);
     }
     __syncthreads();
 }
 
 // Counts n finished rows of system b; returns (in every thread) whether
-// they were the system's last.  The accumulator updates of the block come
-// first.
+// they were the system's last.  The accumulator updates of the block (lane
+// 0 of the first warps) come first.
 __device__ __forceinline__ bool count_rows(const SbSolveSet& S, int b, int nT, int n, int* s_last) {
-    if (threadIdx.x < 3 * n) __threadfence();
+    if ((threadIdx.x & 31) == 0 && threadIdx.x < 32 * 3) __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         const int old = atomicAdd(&S.cnt[b], n);
@@ -882,13 +888,18 @@ __device__ __forceinline__ bool transition(SbSolveRec& rc, int p, ff A, ff B, ff
 // every block of the grid would queue on the same few lines), threads 0..2
 // convert one value each; the sums land in out[0..2] (shared memory) for
 // every thread after the call.
+// Warp 0 only (the sums are in out[] for warp 0 afterwards).
+__device__ __forceinline__ void acc_sums_warp0(const unsigned long long* ab,
+                                               unsigned long long* s_w, ff* out) {
+    for (int k = threadIdx.x; k < kAccBuf; k += 32) s_w[k] = __ldcg(ab + k);
+    __syncwarp();
+    if (threadIdx.x < 3) out[threadIdx.x] = acc_ff(s_w + threadIdx.x * kAccWords);
+    __syncwarp();
+}
+
 __device__ __forceinline__ void acc_sums(const unsigned long long* ab, unsigned long long* s_w,
                                          ff* out) {
-    if (threadIdx.x < 32) {
-        for (int k = threadIdx.x; k < kAccBuf; k += 32) s_w[k] = __ldcg(ab + k);
-        __syncwarp();
-        if (threadIdx.x < 3) out[threadIdx.x] = acc_ff(s_w + threadIdx.x * kAccWords);
-    }
+    if (threadIdx.x < 32) acc_sums_warp0(ab, s_w, out);
     __syncthreads();
 }
 
@@ -977,14 +988,13 @@ __device__ __forceinline__ void stage_desc(const SbSolveSet& S, int b, SbBubbleD
 
 // The work of phase p on theta row i of one system: set-up and build
 // (p = 0), q = A p or the true residual (odd p), update and preconditioner
-// or restart (even p).  The warp's share of the row's dot products goes to
-// out[0..2] (lane 0); warps move on to their next row without a block
-// barrier (the preconditioner synchronises the block internally).
+// or restart (even p).  Each thread's shares of the row's dot products go to
+// the block's work arrays for reduce_row.
 template <bool MIXED, int PER>
 __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
                                           const SolverConfig& cfg, int i, int p, int state,
                                           float beta, ff alpha, float* pA, const float* pB,
-                                          Stage& St, ff* out) {
+                                          Stage& St) {
     ff a = ff_zero(), b2 = ff_zero(), c2 = ff_zero();
     float rv[PER];
     if (p == 0) {
@@ -1000,15 +1010,12 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
         else row_load_r<PER>(g, f, i, rv);
         precondition_row<MIXED, PER, false>(g, f, cfg, i, St, rv, a, b2);
     }
-    // warp sums of the values the phase produces (the others are zero)
-    a = ff_warp_sum(a);
-    if (!(p & 1)) b2 = ff_warp_sum(b2);
-    if (p == 0) c2 = ff_warp_sum(c2);
-    if ((threadIdx.x & 31) == 0) {
-        out[0] = a;
-        out[1] = b2;
-        out[2] = c2;
-    }
+    // this thread's shares of the values the phase produces, for reduce_row
+    // (the work arrays are free: the preconditioner ends with a barrier)
+    ff* tpart = reinterpret_cast<ff*>(St.work);
+    tpart[threadIdx.x] = a;
+    if (!(p & 1)) tpart[kSolveBlock + threadIdx.x] = b2;
+    if (p == 0) tpart[2 * kSolveBlock + threadIdx.x] = c2;
 }
 
 // The solve of a set of systems: phase 0 sets up and builds the
@@ -1028,7 +1035,6 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     __shared__ __align__(8) uint64_t bar;
     __shared__ __align__(16) SbBubbleDesc s_d;
     __shared__ unsigned s_pre[kMaxSystems + 1];
-    __shared__ ff s_part[kRowChunk][kWarps][3];
     __shared__ int s_last;
     __shared__ unsigned long long s_w[kAccBuf];
     __shared__ ff s_sums[3];
@@ -1038,7 +1044,6 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     Stage St;
     stage_init(St, &bar, sm, cfg.blob);
     const unsigned G = gridDim.x;
-    const int warp = threadIdx.x >> 5;
 
     for (int p = 0;; ++p) {
         const unsigned W = active_prefix(S, p, s_pre);
@@ -1087,14 +1092,11 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             bool last = false;
             for (int i = i0; i < i1; ++i) {
                 const int k = (i - i0) % kRowChunk;
-                row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St,
-                                      s_part[k][warp]);
-                // publish and count every kRowChunk rows and at the end; the
-                // block that completes the system advances it
-                if (k == kRowChunk - 1 || i == i1 - 1) {
-                    publish_rows(S, b, p, k + 1, s_part);
-                    last = count_rows(S, b, nT, k + 1, &s_last);
-                }
+                row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St);
+                reduce_row(S, b, p, reinterpret_cast<const ff*>(St.work));
+                // count every kRowChunk rows and at the end; the block that
+                // completes the system advances it
+                if (k == kRowChunk - 1 || i == i1 - 1) last = count_rows(S, b, nT, k + 1, &s_last);
             }
             if (last) {
                 __threadfence();
@@ -1136,7 +1138,6 @@ __global__ void __launch_bounds__(kSolveBlock, 4)
 k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     extern __shared__ __align__(16) float sm[];
     __shared__ __align__(8) uint64_t bar;
-    __shared__ ff s_part[kRowChunk][kWarps][3];
     cg::grid_group grid = cg::this_grid();
     Stage St;
     stage_init(St, &bar, sm, cfg.blob);
@@ -1145,13 +1146,16 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     __shared__ unsigned long long s_w[kAccBuf];
     __shared__ ff s_sums[3];
     const int G = gridDim.x, nT = g.nT;
-    const int warp = threadIdx.x >> 5;
     for (int p = 0;; ++p) {
         if (p > 0) {
-            acc_sums(acc_buf(S, 0, p - 1), s_w, s_sums);
-            if (threadIdx.x == 0) {
-                s_done = transition<MIXED>(s_rc, p - 1, s_sums[0], s_sums[1], s_sums[2], cfg) ? 1 : 0;
-                if (s_done && blockIdx.x == 0) write_stats(f.stats, s_rc);
+            // warp 0 reads the sums and advances the scalars; one barrier
+            if (threadIdx.x < 32) {
+                acc_sums_warp0(acc_buf(S, 0, p - 1), s_w, s_sums);
+                if (threadIdx.x == 0) {
+                    s_done = transition<MIXED>(s_rc, p - 1, s_sums[0], s_sums[1], s_sums[2], cfg)
+                                 ? 1 : 0;
+                    if (s_done && blockIdx.x == 0) write_stats(f.stats, s_rc);
+                }
             }
             __syncthreads();
             if (s_done) break;  // same decision in every block
@@ -1163,15 +1167,9 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
         const ff alpha = to_ff(s_rc.alpha);
         float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
         float* pB = (it & 1) ? f.p : f.q;  // p_old
-        int k = 0;
         for (int i = blockIdx.x; i < nT; i += G) {
-            row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St,
-                                  s_part[k][warp]);
-            ++k;
-            if (k == kRowChunk || i + G >= nT) {
-                publish_rows(S, 0, p, k, s_part);
-                k = 0;
-            }
+            row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St);
+            reduce_row(S, 0, p, reinterpret_cast<const ff*>(St.work));
         }
         grid.sync();
     }
@@ -1212,11 +1210,15 @@ int per_of(int nP) {
 }
 
 // Dynamic shared memory of one solve block for rows of up to nP columns:
-// the factor blob of one row and the four nP-float work arrays of the
-// preconditioner build (the replay needs 1.5 nP floats).  For nP = 1024
-// that is 47 KB, so four 256-thread blocks share an SM next to their
-// static shared memory.
-size_t solve_smem(int nP) { return (size_t)factor_blob(nP).bytes + 16 * (size_t)nP; }
+// the factor blob of one row and the work arrays: the four nP-float arrays
+// of the preconditioner build (the replay needs 1.5 nP floats), which also
+// hold the threads' dot-product shares (3 x 256 float-float).  For
+// nP = 1024 that is 47 KB, so four 256-thread blocks share an SM next to
+// their static shared memory.
+size_t solve_smem(int nP) {
+    const size_t work = std::max<size_t>(16 * (size_t)nP, 3 * kSolveBlock * sizeof(ff));
+    return (size_t)factor_blob(nP).bytes + work;
+}
 
 const void* kernel_for(int per, int mode, bool one) {
     if (one) return mode == 1 ? solve_one_kernel<true>(per) : solve_one_kernel<false>(per);
