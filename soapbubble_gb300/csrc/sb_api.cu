@@ -145,7 +145,7 @@ struct ArenaPlan {
     size_t fwd[2], bwd[2], bwdprev;
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
     size_t div, d_eta, d_gam, err_eta, err_gam;
-    size_t dmass, cE, cS, rhs, r0, x, dx, r, z, p, q, xff, pcr, pcr_levels, step, stats;
+    size_t dmass, cE, cS, rhs, r0, x, dx, r, z, z1, p, q, xff, pcr, pcr_levels, step, stats;
     size_t self, self_list, roff, done_at, cnt, rec, acc;  // the bubble's solve set
     size_t tiles[3];                                           // its cell tiles
 };
@@ -175,7 +175,7 @@ ArenaPlan plan_arena(const SbGrid& g, int storage) {
     a.dmass = a.L.take(N * F); a.cE = a.L.take(N * F); a.cS = a.L.take(N * F);
     a.rhs = a.L.take(N * F); a.r0 = a.L.take(N * F); a.x = a.L.take(N * F); a.dx = a.L.take(N * F);
     a.r = a.L.take(N * F);
-    a.z = a.L.take(N * F); a.p = a.L.take(N * F); a.q = a.L.take(N * F);
+    a.z = a.L.take(N * F); a.z1 = a.L.take(N * F); a.p = a.L.take(N * F); a.q = a.L.take(N * F);
     a.xff = a.L.take(N * 8);
     a.pcr = a.L.take((size_t)g.nT * factor_blob(g.nP).bytes);
     a.pcr_levels = a.L.take((size_t)g.nT * 4);
@@ -463,7 +463,8 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.div = F32(a.div); f.d_eta = F32(a.d_eta); f.d_gam = F32(a.d_gam);
     f.err_eta = F32(a.err_eta); f.err_gam = F32(a.err_gam);
     f.dmass = F32(a.dmass); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs); f.r0 = F32(a.r0);
-    f.x = F32(a.x); f.dx = F32(a.dx); f.r = F32(a.r); f.z = F32(a.z); f.p = F32(a.p); f.q = F32(a.q);
+    f.x = F32(a.x); f.dx = F32(a.dx); f.r = F32(a.r); f.z = F32(a.z); f.z1 = F32(a.z1);
+    f.p = F32(a.p); f.q = F32(a.q);
     f.xff = (float2*)(A + a.xff);
     f.pcr = (float*)(A + a.pcr);
     f.pcr_levels = (int*)(A + a.pcr_levels);

@@ -62,7 +62,7 @@ struct SbFields {
     // the east (cE) and south (cS) neighbours; r = b - A gamma_adv formed
     // analytically; rhs = b (for the norm only)
     float *dmass, *cE, *cS, *rhs, *r0;
-    float *x, *dx, *r, *z, *p, *q;                 // solver vectors
+    float *x, *dx, *r, *z, *z1, *p, *q;            // solver vectors
     float2 *xff;                                   // mixed-precision iterate (float-float)
     float *pcr;                                    // phi-line factors, one blob per row
     int *pcr_levels;                               // reduction levels per row
@@ -126,7 +126,8 @@ cudaError_t launch_load(float* dst, const SbScalar* src, int n, float base, int 
 struct SbSolveRec {
     float2 rz, rr, bb, tol2, alpha;  // r.z, r.r, |b|^2, target for r.r, step length
     float beta;
-    int state;  // iterate, or check the true residual / restart (mixed mode)
+    int kind;   // the kind of the system's next phase (sb_solver.cu)
+    int fresh;  // the next r.z starts a new search direction
     int it;
     int conv;
 };

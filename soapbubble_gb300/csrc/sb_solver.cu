@@ -16,15 +16,22 @@
 // distributed or in which order blocks add: a bubble solved alone and
 // inside a batch gives bit-identical results.
 //
-// Preconditioner: exact solve of each theta row's periodic tridiagonal block
-// (phi couplings; the theta couplings stay on its diagonal).  Near the poles
-// the phi couplings carry 1/sin(theta) and dominate the diagonal by 1e4-1e5,
-// which is what makes point Jacobi slow there.  The row solve is parallel
-// cyclic reduction in shared memory, written in "excess" form: each equation
-// keeps (excess e, |lower|, |upper|, rhs) with diagonal = e + |lower| + |upper|,
-// and every update adds positive terms, so FP32 keeps full relative accuracy
-// even when the diagonal exceeds the off-diagonal sum by a factor 1 + 1e-5
-// (the Grassmann-Taksar-Heyman idea applied to cyclic reduction).
+// Preconditioner: a two-term Neumann series M^-1 = B^-1 + B^-1 C B^-1 of the
+// splitting A = B - C, B the exact solve of each theta row's periodic
+// tridiagonal block (phi couplings; the theta couplings stay on its
+// diagonal), C the theta couplings.  Near the poles the phi couplings carry
+// 1/sin(theta) and dominate the diagonal by 1e4-1e5, which is what makes
+// point Jacobi slow there; where the film has ruptured the theta couplings
+// matter too, and the second term halves the iterations.  The row solve is
+// cyclic / parallel cyclic reduction in shared memory, written in "excess"
+// form: each equation keeps (excess e, |lower|, |upper|, rhs) with
+// diagonal = e + |lower| + |upper|, and every update adds positive terms,
+// so FP32 keeps full relative accuracy even when the diagonal exceeds the
+// off-diagonal sum by a factor 1 + 1e-5 (the Grassmann-Taksar-Heyman idea
+// applied to cyclic reduction).
+//
+// Phases of one CG iteration (each ends at a grid barrier): q = A p; the
+// update of x and r with z1 = B^-1 r; z = z1 + B^-1 C z1 with r.z and r.r.
 //
 // Modes: plain FP32 (FP32 iterate, float products), or mixed precision
 // (FP32 SpMV and preconditioner, float-float iterate, exact products in the
@@ -48,11 +55,25 @@ namespace sb {
 namespace {
 
 constexpr int kSolveBlock = 256;
-constexpr int kWarps = kSolveBlock / 32;  // row partials per row: one per warp
+constexpr int kWarps = kSolveBlock / 32;
 constexpr int kWaitPolls = 1 << 22;   // mbarrier polls before a copy counts as lost
 constexpr int kMaxSystems = 1024;     // systems of one solve set
-constexpr int kRowChunk = 16;         // rows a block publishes at a time
-enum { ST_ITER = 0, ST_CHECK = 1 };
+constexpr int kRowChunk = 16;         // rows a block counts at a time (sets)
+// Phase kinds of the solve (what every row does in a phase):
+//   K_SETUP    x = 0, r = r0, the preconditioner's factors, z1 = B^-1 r; |b|^2
+//   K_NEUMANN  z = z1 + B^-1 (C z1) (C: the theta couplings); r.z, r.r
+//   K_Q        p = z + beta p_old, q = A p; p.q
+//   K_UPDATE   x += alpha p, r -= alpha q, z1 = B^-1 r
+//   K_CHECK    r = r0 - A x of the float-float iterate (mixed mode); |r|^2
+//   K_RESTART  z1 = B^-1 r from the refined iterate's residual
+enum { K_SETUP = 0, K_NEUMANN = 1, K_Q = 2, K_UPDATE = 3, K_CHECK = 4, K_RESTART = 5 };
+
+// Dot-product values a phase kind produces (bit v: accumulator value v):
+// the set-up |b|^2 (value 2), the Neumann phase r.z and r.r (0, 1), q = A p
+// and the refinement check one value each.
+__host__ __device__ inline int kind_values(int kind) {
+    return kind == K_SETUP ? 4 : kind == K_NEUMANN ? 3 : (kind == K_Q || kind == K_CHECK) ? 1 : 0;
+}
 
 // ---------------------------------------------------------------------------
 // Shared-memory copy of one row's preconditioner factors.  A block keeps
@@ -161,10 +182,11 @@ __device__ __forceinline__ ff acc(ff s, float a, float b) {
 // Column of element k of this thread in a row.
 __device__ __forceinline__ int col_of(int k) { return threadIdx.x + k * kSolveBlock; }
 
-// z = M^-1 r on theta row i: Jacobi, or the exact solve of the row's
-// periodic tridiagonal block (phi couplings; the theta couplings stay on its
-// diagonal).  rv[k] holds r at column col_of(k) (this thread's elements).
-// Adds the row's r.z and r.r to rz, rr.  PER = equations per thread
+// y = B_i^-1 v on theta row i: the exact solve of the row's periodic
+// tridiagonal block B_i (phi couplings; the theta couplings stay on its
+// diagonal).  rv[k] holds v at column col_of(k) (this thread's elements);
+// the result is left in the block's work array D = S.work (D[j] for
+// column j) for the caller.  PER = equations per thread
 // (nP <= PER * kSolveBlock).
 //
 // Row solve of n = nP equations (indices mod n) in excess form: equation j
@@ -193,30 +215,11 @@ __device__ __forceinline__ int col_of(int k) { return threadIdx.x + k * kSolveBl
 // records the levels of step 3 in f.pcr_levels; later applications replay
 // the right-hand-side updates with the factors (fetched by stage_fetch
 // unless the block still holds them), with the same arithmetic.
-template <bool MIXED, int PER, bool BUILD>
-__device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f,
-                                                 const SolverConfig& cfg, int i, Stage& S,
-                                                 const float (&rv)[PER], ff& rz, ff& rr) {
+template <int PER, bool BUILD>
+__device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f, int i,
+                                                 Stage& S, const float (&rv)[PER]) {
     const int nP = g.nP, nT = g.nT, mask = g.maskP;
     const int row = i * nP;
-    if (cfg.precond == 0) {
-#pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int j = col_of(k);
-            if (j < nP) {
-                const int c = row + j;
-                float dg = f.dmass[c] + f.cE[c] + f.cE[row + ((j - 1) & mask)];
-                if (i < nT - 1) dg += f.cS[c];
-                if (i > 0) dg += f.cS[c - nP];
-                const float rc = rv[k];
-                const float zc = rc / dg;
-                f.z[c] = zc;
-                rz = acc<MIXED>(rz, rc, zc);
-                rr = acc<MIXED>(rr, rc, rc);
-            }
-        }
-        return;
-    }
     constexpr int H = PER >= 2 ? PER / 2 : 1;  // items per thread of the n/2-item steps
     constexpr int Q = PER >= 4 ? PER / 4 : 1;  // and of the n/4-item steps
     const SbFactorBlob B = factor_blob(nP);
@@ -442,17 +445,6 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         }
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
-        if (j < n) {
-            const float zj = D[j];
-            const float rc = rv[k];
-            f.z[row + j] = zj;
-            rz = acc<MIXED>(rz, rc, zj);
-            rr = acc<MIXED>(rr, rc, rc);
-        }
-    }
     if (BUILD) {
         // the row's factors to its global slot, for fetches by any block in
         // later phases; the blob is the block's resident copy
@@ -466,7 +458,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         asm volatile("fence.proxy.async.global;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    __syncthreads();  // blob and work arrays are free again
+    __syncthreads();  // the blob is free again; D holds the result
 }
 
 // Global slot of row i's factors.
@@ -745,19 +737,16 @@ __device__ __forceinline__ void acc_zero(unsigned long long* a, int n, int tid, 
     for (int k = tid; k < n; k += nthreads) a[k] = 0ull;
 }
 
-// Values of the dot products a phase produces: q = A p gives one (p.q, or
-// |r|^2 of the refinement check), the preconditioner two (r.z, r.r), the
-// set-up three (r.z, r.r, |b|^2).
-__device__ __forceinline__ int phase_values(int p) { return p == 0 ? 3 : (p & 1) ? 1 : 2; }
-
 // A row of system b is done: every thread left its shares of the phase's
-// values in tpart[v][thread].  Warp v sums value v over the block in a fixed
-// order (each lane 8 threads' shares, then the lanes by shuffle tree) and
-// adds the row's partial into the phase's exact accumulator.
-__device__ __forceinline__ void reduce_row(const SbSolveSet& S, int b, int p, const ff* tpart) {
+// values (bit v of vals: value v) in tpart[v][thread].  Warp v sums value v
+// over the block in a fixed order (each lane 8 threads' shares, then the
+// lanes by shuffle tree) and adds the row's partial into the phase's exact
+// accumulator.
+__device__ __forceinline__ void reduce_row(const SbSolveSet& S, int b, int p, int vals,
+                                           const ff* tpart) {
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp < phase_values(p)) {
+    if (warp < 3 && ((vals >> warp) & 1)) {
         const ff* t = tpart + warp * kSolveBlock;
         ff x = ff_zero();
 #pragma unroll
@@ -797,7 +786,8 @@ __device__ __forceinline__ SbSolveRec load_rec(const SbSolveRec* p) {
     r.tol2 = __ldcg(&p->tol2);
     r.alpha = __ldcg(&p->alpha);
     r.beta = __ldcg(&p->beta);
-    r.state = __ldcg(&p->state);
+    r.kind = __ldcg(&p->kind);
+    r.fresh = __ldcg(&p->fresh);
     r.it = __ldcg(&p->it);
     r.conv = __ldcg(&p->conv);
     return r;
@@ -812,9 +802,9 @@ __device__ __forceinline__ void write_stats(SbDevStats* st, const SbSolveRec& rc
     st->solver_converged = rc.conv;
 }
 
-// The loop head of CG: iteration limit, NaN, target reached (mixed mode
-// then checks the true residual first).  Returns true when the system is
-// finished.
+// The loop head of CG after r.z and r.r are known: iteration limit, NaN,
+// target reached (mixed mode then checks the true residual first), else the
+// next q = A p.  Returns true when the system is finished.
 template <bool MIXED>
 __device__ __forceinline__ bool loop_head(SbSolveRec& rc, const SolverConfig& cfg) {
     if (rc.it >= cfg.max_iter || !(rc.rr.x == rc.rr.x)) return true;
@@ -823,64 +813,69 @@ __device__ __forceinline__ bool loop_head(SbSolveRec& rc, const SolverConfig& cf
             rc.conv = 1;
             return true;
         }
-        rc.state = ST_CHECK;
+        rc.kind = K_CHECK;
         return false;
     }
-    rc.state = ST_ITER;
+    rc.kind = K_Q;
     return false;
 }
 
-// Advances a system's scalars past phase p with its exact sums (A, B, C);
-// returns true when the system is finished.
-//   p = 0 (set-up): A = r.z, B = r.r, C = |b|^2
-//   odd p:  iterate -> A = p.q;   check -> A = |r_true|^2
-//   even p: iterate -> A = r.z, B = r.r (after the update); restart -> same
-// Every path that advances a system (one block for a batch, every block
-// for a single system) runs this same function on the same sums.
+// Advances a system's scalars past a phase of kind rc.kind with its exact
+// sums (A, B, C: the values kind_values names) and sets the next kind;
+// returns true when the system is finished.  Every path that advances a
+// system (one block for a set, every block for a single system) runs this
+// same function on the same sums.
 template <bool MIXED>
-__device__ __forceinline__ bool transition(SbSolveRec& rc, int p, ff A, ff B, ff C,
+__device__ __forceinline__ bool transition(SbSolveRec& rc, ff A, ff B, ff C,
                                            const SolverConfig& cfg) {
-    if (p == 0) {
-        const ff bb = C.hi > 0.0f ? C : ff{1.0f, 0.0f};
-        rc.bb = to_f2(bb);
-        // tol2f = tol^2 (plain) or (0.8 tol)^2 (mixed: the float-float
-        // iterate is driven below tol so that the returned FP32 gamma, whose
-        // rounding adds up to a few percent, still meets tol)
-        rc.tol2 = to_f2(ff_mul_f(bb, cfg.tol2f));
-        rc.rz = to_f2(A);
-        rc.rr = to_f2(B);
-        rc.alpha = make_float2(0.0f, 0.0f);
-        rc.beta = 0.0f;
-        rc.it = 0;
-        rc.conv = 0;
-        rc.state = ST_ITER;
-        return loop_head<MIXED>(rc, cfg);
-    }
-    if (p & 1) {
-        if (rc.state == ST_ITER) {
-            if (!(A.hi > 0.0f)) return true;  // breakdown: keep the current iterate
-            rc.alpha = to_f2(ff_div(to_ff(rc.rz), A));
+    switch (rc.kind) {
+        case K_SETUP: {
+            const ff bb = C.hi > 0.0f ? C : ff{1.0f, 0.0f};
+            rc.bb = to_f2(bb);
+            // tol2f = tol^2 (plain) or (0.8 tol)^2 (mixed: the float-float
+            // iterate is driven below tol so that the returned FP32 gamma, whose
+            // rounding adds up to a few percent, still meets tol)
+            rc.tol2 = to_f2(ff_mul_f(bb, cfg.tol2f));
+            rc.alpha = make_float2(0.0f, 0.0f);
+            rc.beta = 0.0f;
+            rc.it = 0;
+            rc.conv = 0;
+            rc.fresh = 1;
+            rc.kind = K_NEUMANN;
             return false;
         }
-        rc.rr = to_f2(A);
-        if (ff_le(A, to_ff(rc.tol2))) {
-            rc.conv = 1;
-            return true;
-        }
-        return false;  // restart from the refined iterate
+        case K_NEUMANN:
+            if (rc.fresh) {
+                rc.beta = 0.0f;  // a new search direction (start or restart)
+                rc.fresh = 0;
+            } else {
+                rc.beta = ff_to_f(ff_div(A, to_ff(rc.rz)));
+                ++rc.it;
+            }
+            rc.rz = to_f2(A);
+            rc.rr = to_f2(B);
+            return loop_head<MIXED>(rc, cfg);
+        case K_Q:
+            if (!(A.hi > 0.0f)) return true;  // breakdown: keep the current iterate
+            rc.alpha = to_f2(ff_div(to_ff(rc.rz), A));
+            rc.kind = K_UPDATE;
+            return false;
+        case K_UPDATE:
+            rc.kind = K_NEUMANN;
+            return false;
+        case K_CHECK:
+            rc.rr = to_f2(A);
+            if (ff_le(A, to_ff(rc.tol2))) {
+                rc.conv = 1;
+                return true;
+            }
+            rc.kind = K_RESTART;
+            return false;
+        default:  // K_RESTART
+            rc.fresh = 1;
+            rc.kind = K_NEUMANN;
+            return false;
     }
-    if (rc.state == ST_ITER) {
-        rc.beta = ff_to_f(ff_div(A, to_ff(rc.rz)));
-        rc.rz = to_f2(A);
-        rc.rr = to_f2(B);
-        ++rc.it;
-        return loop_head<MIXED>(rc, cfg);
-    }
-    rc.rz = to_f2(A);
-    rc.rr = to_f2(B);
-    rc.beta = 0.0f;
-    rc.state = ST_ITER;
-    return false;
 }
 
 // The three sums of buffer ab, for a whole block: warp 0 copies the buffer
@@ -911,7 +906,8 @@ template <bool MIXED>
 __device__ __forceinline__ void advance(const SbSolveSet& S, int b, int p, const ff* sums,
                                         const SolverConfig& cfg) {
     SbSolveRec rc = load_rec(S.rec + (p & 1) * S.nb + b);
-    if (transition<MIXED>(rc, p, sums[0], sums[1], sums[2], cfg)) {
+    if (p == 0) rc.kind = K_SETUP;
+    if (transition<MIXED>(rc, sums[0], sums[1], sums[2], cfg)) {
         write_stats(S.descs[b]->f.stats, rc);
         S.done_at[b] = p + 1;
         // retired: this block was the only reader of the system's buffers
@@ -986,41 +982,120 @@ __device__ __forceinline__ void stage_desc(const SbSolveSet& S, int b, SbBubbleD
     __syncthreads();
 }
 
-// The work of phase p on theta row i of one system: set-up and build
-// (p = 0), q = A p or the true residual (odd p), update and preconditioner
-// or restart (even p).  Each thread's shares of the row's dot products go to
-// the block's work arrays for reduce_row.
-template <bool MIXED, int PER>
-__device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
-                                          const SolverConfig& cfg, int i, int p, int state,
-                                          float beta, ff alpha, float* pA, const float* pB,
-                                          Stage& St) {
-    ff a = ff_zero(), b2 = ff_zero(), c2 = ff_zero();
-    float rv[PER];
-    if (p == 0) {
-        row_init<MIXED, PER>(g, f, i, rv, c2);
-        precondition_row<MIXED, PER, true>(g, f, cfg, i, St, rv, a, b2);
-    } else if (p & 1) {
-        if (state == ST_ITER) a = row_spmv<MIXED, PER>(g, f, i, beta, pB, pA);
-        else if (MIXED) a = row_true_residual<PER>(g, f, i);
-    } else {
-        // the row's factors travel while the update runs
-        if (cfg.precond != 0) stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
-        if (state == ST_ITER) row_update<MIXED, PER>(g, f, i, alpha, pA, rv);
-        else row_load_r<PER>(g, f, i, rv);
-        precondition_row<MIXED, PER, false>(g, f, cfg, i, St, rv, a, b2);
+// Stores the preconditioner's result D (in the block's work array) as this
+// thread's columns of row i of z1.
+template <int PER>
+__device__ __forceinline__ void store_z1(const SbGrid& g, const SbFields& f, int i,
+                                         const Stage& St) {
+    const int row = i * g.nP;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        if (j < g.nP) f.z1[row + j] = St.work[j];
     }
-    // this thread's shares of the values the phase produces, for reduce_row
-    // (the work arrays are free: the preconditioner ends with a barrier)
-    ff* tpart = reinterpret_cast<ff*>(St.work);
-    tpart[threadIdx.x] = a;
-    if (!(p & 1)) tpart[kSolveBlock + threadIdx.x] = b2;
-    if (p == 0) tpart[2 * kSolveBlock + threadIdx.x] = c2;
 }
 
-// The solve of a set of systems: phase 0 sets up and builds the
-// preconditioner; odd phases form q = A p (or the true residual); even
-// phases update the iterate and apply the preconditioner (or restart).  In
+// w = C z1 on row i: the theta couplings (weights cS of the faces north and
+// south of each cell) applied to the neighbouring rows of z1; z1 of the row
+// itself is returned in zo.
+template <int PER>
+__device__ __forceinline__ void row_theta_coupling(const SbGrid& g, const SbFields& f, int i,
+                                                   float (&w)[PER], float (&zo)[PER]) {
+    const int nP = g.nP, nT = g.nT, row = i * nP;
+    const float* __restrict__ z1 = f.z1;
+    const float* __restrict__ cS = f.cS;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        w[k] = 0.0f;
+        zo[k] = 0.0f;
+        if (j < nP) {
+            const int c = row + j;
+            float v = 0.0f;
+            if (i < nT - 1) v = cS[c] * z1[c + nP];
+            if (i > 0) v += cS[c - nP] * z1[c - nP];
+            w[k] = v;
+            zo[k] = z1[c];
+        }
+    }
+}
+
+// The work of a phase of kind `kind` on theta row i of one system (see the
+// kinds above).  The preconditioner is a two-term Neumann series of the
+// phi-line splitting A = B - C (C: the theta couplings, non-negative):
+// M^-1 = B^-1 + B^-1 C B^-1, symmetric and positive definite because the
+// splitting of this M-matrix is regular (spectral radius of B^-1 C below
+// one).  Against B^-1 alone it halves the iterations on ruptured films (an
+// offline study on oracle states: 29 -> 15 at step 600 of c1) at the cost
+// of one more phase per iteration.  Each thread's shares of the row's dot
+// products go to the block's work arrays (after the preconditioner's D)
+// for reduce_row.
+template <bool MIXED, int PER>
+__device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
+                                          const SolverConfig& cfg, int i, int kind,
+                                          float beta, ff alpha, float* pA, const float* pB,
+                                          Stage& St) {
+    (void)cfg;
+    ff a = ff_zero(), b2 = ff_zero(), c2 = ff_zero();
+    float rv[PER];
+    switch (kind) {
+        case K_SETUP:
+            row_init<MIXED, PER>(g, f, i, rv, c2);
+            precondition_row<PER, true>(g, f, i, St, rv);
+            store_z1<PER>(g, f, i, St);
+            break;
+        case K_NEUMANN: {
+            stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
+            float z1v[PER];
+            row_theta_coupling<PER>(g, f, i, rv, z1v);
+            precondition_row<PER, false>(g, f, i, St, rv);
+            const int row = i * g.nP;
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int j = col_of(k);
+                if (j < g.nP) {
+                    const int c = row + j;
+                    const float z = z1v[k] + St.work[j];
+                    const float r = f.r[c];
+                    f.z[c] = z;
+                    a = acc<MIXED>(a, r, z);
+                    b2 = acc<MIXED>(b2, r, r);
+                }
+            }
+            break;
+        }
+        case K_Q:
+            a = row_spmv<MIXED, PER>(g, f, i, beta, pB, pA);
+            break;
+        case K_UPDATE:
+            // the row's factors travel while the update runs
+            stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
+            row_update<MIXED, PER>(g, f, i, alpha, pA, rv);
+            precondition_row<PER, false>(g, f, i, St, rv);
+            store_z1<PER>(g, f, i, St);
+            break;
+        case K_CHECK:
+            if (MIXED) a = row_true_residual<PER>(g, f, i);
+            break;
+        default:  // K_RESTART
+            stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
+            row_load_r<PER>(g, f, i, rv);
+            precondition_row<PER, false>(g, f, i, St, rv);
+            store_z1<PER>(g, f, i, St);
+            break;
+    }
+    // this thread's shares of the values the kind produces, for reduce_row
+    // (after D: the other threads may still read their D entries)
+    const int vals = kind_values(kind);
+    ff* tpart = reinterpret_cast<ff*>(St.work + g.nP);
+    if (vals & 1) tpart[threadIdx.x] = a;
+    if (vals & 2) tpart[kSolveBlock + threadIdx.x] = b2;
+    if (vals & 4) tpart[2 * kSolveBlock + threadIdx.x] = c2;
+}
+
+// The solve of a set of systems: each system runs the phase kinds of its
+// record (set-up, then per iteration q = A p, update, Neumann term; in
+// mixed mode the refinement check and restart).  In
 // every phase the rows of the systems still iterating are split into G
 // contiguous ranges of equal work weight, one per block, so a block meets
 // one or two systems per phase and a system that iterates longer than the
@@ -1063,13 +1138,13 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             // grid reads the same record), staged with the descriptor
             if (threadIdx.x == 0) {
                 SbSolveRec rc;
-                rc.state = ST_ITER;
+                rc.kind = K_SETUP;
                 rc.it = 0;
                 rc.beta = 0.0f;
                 rc.alpha = make_float2(0.0f, 0.0f);
                 if (p > 0) {
                     const SbSolveRec* rp = S.rec + (p & 1) * S.nb + b;
-                    rc.state = __ldcg(&rp->state);
+                    rc.kind = __ldcg(&rp->kind);
                     rc.it = __ldcg(&rp->it);
                     rc.beta = __ldcg(&rp->beta);
                     rc.alpha = __ldcg(&rp->alpha);
@@ -1082,7 +1157,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             } else {
                 __syncthreads();
             }
-            const int state = s_rc.state, it = s_rc.it;
+            const int kind = s_rc.kind, it = s_rc.it, vals = kind_values(kind);
             const float beta = s_rc.beta;
             const ff alpha = to_ff(s_rc.alpha);
             const SbGrid& g = s_d.g;
@@ -1092,8 +1167,8 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             bool last = false;
             for (int i = i0; i < i1; ++i) {
                 const int k = (i - i0) % kRowChunk;
-                row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St);
-                reduce_row(S, b, p, reinterpret_cast<const ff*>(St.work));
+                row_phase<MIXED, PER>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
+                if (vals) reduce_row(S, b, p, vals, reinterpret_cast<const ff*>(St.work + g.nP));
                 // count every kRowChunk rows and at the end; the block that
                 // completes the system advances it
                 if (k == kRowChunk - 1 || i == i1 - 1) last = count_rows(S, b, nT, k + 1, &s_last);
@@ -1139,12 +1214,13 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     extern __shared__ __align__(16) float sm[];
     __shared__ __align__(8) uint64_t bar;
     cg::grid_group grid = cg::this_grid();
-    Stage St;
-    stage_init(St, &bar, sm, cfg.blob);
     __shared__ SbSolveRec s_rc;  // the system's scalars (the same in every block)
     __shared__ int s_done;
     __shared__ unsigned long long s_w[kAccBuf];
     __shared__ ff s_sums[3];
+    if (threadIdx.x == 0) s_rc.kind = K_SETUP;
+    Stage St;
+    stage_init(St, &bar, sm, cfg.blob);  // (its barrier publishes s_rc.kind)
     const int G = gridDim.x, nT = g.nT;
     for (int p = 0;; ++p) {
         if (p > 0) {
@@ -1152,8 +1228,7 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
             if (threadIdx.x < 32) {
                 acc_sums_warp0(acc_buf(S, 0, p - 1), s_w, s_sums);
                 if (threadIdx.x == 0) {
-                    s_done = transition<MIXED>(s_rc, p - 1, s_sums[0], s_sums[1], s_sums[2], cfg)
-                                 ? 1 : 0;
+                    s_done = transition<MIXED>(s_rc, s_sums[0], s_sums[1], s_sums[2], cfg) ? 1 : 0;
                     if (s_done && blockIdx.x == 0) write_stats(f.stats, s_rc);
                 }
             }
@@ -1162,14 +1237,14 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
         }
         // the buffer of phase p + 1 was last read at the start of phase p - 1
         if (blockIdx.x == 0) acc_zero(acc_buf(S, 0, p + 1), kAccBuf, threadIdx.x, blockDim.x);
-        const int state = s_rc.state, it = s_rc.it;
+        const int kind = s_rc.kind, it = s_rc.it, vals = kind_values(kind);
         const float beta = s_rc.beta;
         const ff alpha = to_ff(s_rc.alpha);
         float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
         float* pB = (it & 1) ? f.p : f.q;  // p_old
         for (int i = blockIdx.x; i < nT; i += G) {
-            row_phase<MIXED, PER>(g, f, cfg, i, p, state, beta, alpha, pA, pB, St);
-            reduce_row(S, 0, p, reinterpret_cast<const ff*>(St.work));
+            row_phase<MIXED, PER>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
+            if (vals) reduce_row(S, 0, p, vals, reinterpret_cast<const ff*>(St.work + g.nP));
         }
         grid.sync();
     }
@@ -1212,11 +1287,13 @@ int per_of(int nP) {
 // Dynamic shared memory of one solve block for rows of up to nP columns:
 // the factor blob of one row and the work arrays: the four nP-float arrays
 // of the preconditioner build (the replay needs 1.5 nP floats), which also
-// hold the threads' dot-product shares (3 x 256 float-float).  For
+// hold the result D (nP floats) followed by the threads' dot-product shares
+// (3 x 256 float-float).  For
 // nP = 1024 that is 47 KB, so four 256-thread blocks share an SM next to
 // their static shared memory.
 size_t solve_smem(int nP) {
-    const size_t work = std::max<size_t>(16 * (size_t)nP, 3 * kSolveBlock * sizeof(ff));
+    const size_t work =
+        std::max<size_t>(16 * (size_t)nP, 4 * (size_t)nP + 3 * kSolveBlock * sizeof(ff));
     return (size_t)factor_blob(nP).bytes + work;
 }
 
