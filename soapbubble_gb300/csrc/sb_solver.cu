@@ -996,19 +996,23 @@ __device__ __forceinline__ void store_z1(const SbGrid& g, const SbFields& f, int
 }
 
 // w = C z1 on row i: the theta couplings (weights cS of the faces north and
-// south of each cell) applied to the neighbouring rows of z1; z1 of the row
-// itself is returned in zo.
+// south of each cell) applied to the neighbouring rows of z1; z1 and r of
+// the row itself are returned in zo and ro (loaded with the rest, before
+// the row solve that w feeds).
 template <int PER>
 __device__ __forceinline__ void row_theta_coupling(const SbGrid& g, const SbFields& f, int i,
-                                                   float (&w)[PER], float (&zo)[PER]) {
+                                                   float (&w)[PER], float (&zo)[PER],
+                                                   float (&ro)[PER]) {
     const int nP = g.nP, nT = g.nT, row = i * nP;
     const float* __restrict__ z1 = f.z1;
     const float* __restrict__ cS = f.cS;
+    const float* __restrict__ r = f.r;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int j = col_of(k);
         w[k] = 0.0f;
         zo[k] = 0.0f;
+        ro[k] = 0.0f;
         if (j < nP) {
             const int c = row + j;
             float v = 0.0f;
@@ -1016,6 +1020,7 @@ __device__ __forceinline__ void row_theta_coupling(const SbGrid& g, const SbFiel
             if (i > 0) v += cS[c - nP] * z1[c - nP];
             w[k] = v;
             zo[k] = z1[c];
+            ro[k] = r[c];
         }
     }
 }
@@ -1046,8 +1051,8 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
             break;
         case K_NEUMANN: {
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
-            float z1v[PER];
-            row_theta_coupling<PER>(g, f, i, rv, z1v);
+            float z1v[PER], r0v[PER];
+            row_theta_coupling<PER>(g, f, i, rv, z1v, r0v);
             precondition_row<PER, false>(g, f, i, St, rv);
             const int row = i * g.nP;
 #pragma unroll
@@ -1056,7 +1061,7 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
                 if (j < g.nP) {
                     const int c = row + j;
                     const float z = z1v[k] + St.work[j];
-                    const float r = f.r[c];
+                    const float r = r0v[k];
                     f.z[c] = z;
                     a = acc<MIXED>(a, r, z);
                     b2 = acc<MIXED>(b2, r, r);
@@ -1175,7 +1180,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             }
             if (last) {
                 __threadfence();
-                acc_sums(acc_buf(S, b, p), s_w, s_sums);
+                if (vals) acc_sums(acc_buf(S, b, p), s_w, s_sums);
                 if (threadIdx.x == 0) advance<MIXED>(S, b, p, s_sums, cfg);
             }
             __syncthreads();  // s_d and s_last are reused
@@ -1224,9 +1229,10 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     const int G = gridDim.x, nT = g.nT;
     for (int p = 0;; ++p) {
         if (p > 0) {
-            // warp 0 reads the sums and advances the scalars; one barrier
+            // warp 0 reads the sums (if the phase produced any) and advances
+            // the scalars; one barrier
             if (threadIdx.x < 32) {
-                acc_sums_warp0(acc_buf(S, 0, p - 1), s_w, s_sums);
+                if (kind_values(s_rc.kind)) acc_sums_warp0(acc_buf(S, 0, p - 1), s_w, s_sums);
                 if (threadIdx.x == 0) {
                     s_done = transition<MIXED>(s_rc, s_sums[0], s_sums[1], s_sums[2], cfg) ? 1 : 0;
                     if (s_done && blockIdx.x == 0) write_stats(f.stats, s_rc);
