@@ -55,11 +55,17 @@ ALG_BYTES_PER_CELL = {
                           # -> eta_delta,gamma_delta,err_eta,err_gamma
     "k_reinit": 0,        # no traffic unless re-initialising (about 1 step in 10)
 }
-PCG_BYTES_FIXED, PCG_BYTES_PER_ITER = 84, 80
+# The implicit solve, per cell.  Fixed: set-up (r0, rhs, dmass, cE, cS ->
+# x (float-float), r, q, z1 = 40), the first Neumann phase (16), the final
+# true-residual check (x, r0, dmass, cE, cS -> r = 28) and the result
+# (x, gamma_adv -> dx, gamma = 20).  Per CG iteration: Neumann phase (z1, cS,
+# r -> z = 16), q = A p (z, p, dmass, cE, cS -> p, q = 28), update and
+# preconditioner (p, r, q, x -> x, r, z1 = 36).
+PCG_BYTES_FIXED, PCG_BYTES_PER_ITER = 104, 80
 ROOFLINE_NOTES = {
     "k_solve": "latency-bound, not HBM-bound: the solve's vectors and factors stay in L2 and in "
                "shared memory across its iterations (DRAM traffic per launch is their first touch "
-               "and does not grow with the iteration count); two grid barriers per CG iteration",
+               "and does not grow with the iteration count); three grid barriers per CG iteration",
 }
 
 

@@ -75,6 +75,14 @@ typedef struct {
                                  characteristic maps updated, no re-initialisation */
     int single_step_velocity; /* 1: as without RUNGE_KUTTA: the velocity advection traces in
                                  one step (kernel/bubble.cu:689-730 skipped) */
+    int viscous;              /* 1: as with VISCOUS: viscous stress forces of the film
+                                 (kernel/bubble.cu:1218-1269, 1512-1816) enter the surfactant
+                                 system in place of the gravity term (1460-1466) and the
+                                 velocity update (1940-2038); gravity is part of the force */
+    int write_velocity_frames;      /* sb_run also writes vel%04d.exr (WRITE_VELOCITY_DATA,
+                                       kernel/bubble.cu:2646-2648, 2689-2691) */
+    int write_concentration_frames; /* sb_run also writes con%04d.exr (WRITE_CONCENTRATION_DATA,
+                                       kernel/bubble.cu:2649-2651, 2692-2694) */
 } sb_params;
 
 enum { SB_STORE_FP32 = 0, SB_STORE_BF16 = 1 };
@@ -209,6 +217,16 @@ int sb_update_mass(sb_bubble* b);
  * *broken when no cell has eta > 0. */
 int sb_write_thickness_exr(sb_bubble* b, const char* path, int* broken);
 
+/* Replaces Solver::write_velocity_image (kernel/solver.cu:388-497): a HALF
+ * EXR with R = u/2 + 0.5, G = v/2 + 0.5, B = 0.5, where u averages the u_phi
+ * faces west and east of each cell and v the u_theta faces north and south
+ * (next to a pole, 0.75 v - 0.25 v(phi + pi) of the nearest face row). */
+int sb_write_velocity_exr(sb_bubble* b, const char* path);
+
+/* Replaces Solver::write_concentration_image (kernel/solver.cu:500-538):
+ * three equal HALF channels (gamma - 0.9) / 0.2. */
+int sb_write_concentration_exr(sb_bubble* b, const char* path);
+
 /* Host-only: writes img (height rows of width floats) as the reference's
  * grayscale frame format: 3 equal HALF channels B, G, R, no compression
  * (Solver::write_image, kernel/solver.cu:338-385).  Needs no GPU. */
@@ -216,7 +234,8 @@ int sb_write_exr_gray(const char* path, int width, int height, const float* img)
 
 /* Replaces Bubble::run (kernel/bubble.cu:2607-2704): the frame loop with
  * full steps, a fractional last step per frame, and frame%04d.exr output
- * into out_dir (NULL: no output).  frames <= 0 uses p->frames. */
+ * (plus vel%04d.exr / con%04d.exr when the params ask for them) into
+ * out_dir (NULL: no output).  frames <= 0 uses p->frames. */
 int sb_run(sb_bubble* b, const char* out_dir, int frames);
 
 /* No counterpart in the reference.  The two mass integrals of
@@ -261,8 +280,9 @@ const char* sb_last_error(void);
  * batch exists, step its members only through it (sb_step on a member
  * would desynchronise the batch's view of its double-buffered maps).
  * Field I/O and statistics on members remain available after
- * sb_batch_synchronize.  All members share one solver configuration, the
- * first member's; the step time t and dt are common to all members.
+ * sb_batch_synchronize.  All members share one solver configuration, one
+ * field storage and one viscous switch (SB_ERR_INVALID otherwise); the step
+ * time t and dt are common to all members.
  * ------------------------------------------------------------------------ */
 typedef struct sb_batch sb_batch;
 

@@ -41,6 +41,7 @@ constexpr double kRho = 1e3;
 constexpr double kG = 9.8;
 constexpr double kRhoA = 1.184;
 constexpr double kNuA = 1.562e-5;
+constexpr double kNu = 1.25e-4;   // soap solution kinematic viscosity
 constexpr double kEvaporation = -0.00000003;
 constexpr double kThresh = 0.0;   // bubble.cu:27
 constexpr double kEps = 1e-7;     // bubble.cu:28
@@ -615,7 +616,7 @@ inline double scos(int strict, double x) { return strict ? (double)cosf((float)x
 void concentrationLinearSystem(const sb_oracle_params* p, const Ctx& c, const double* velPhi_a,
                                const double* velTheta_a, double* gamma_a, const double* eta_a,
                                const double* W, const double* uair, const double* vair,
-                               double* val, double* rhs) {
+                               const double* fu, const double* fv, double* val, double* rhs) {
     const long long nP = p->nPhi; const int nth = nthreads_of(p);
     const size_t pitch = (size_t)nP;
     const double dt = p->dt, t = p->t;
@@ -710,9 +711,22 @@ void concentrationLinearSystem(const sb_oracle_params* p, const Ctx& c, const do
                 (uAirEast / (etaRight / Cr * invDt + 1.0) - uAirWest / (etaLeft / Cr * invDt + 1.0) +
                  vAirSouth * sinThetaSouth / (etaDown / Cr * invDt + 1.0) -
                  vAirNorth * sinThetaNorth / (etaUp / Cr * invDt + 1.0));
-            sinThetaDiv += p->gs * c.invGridLen *
-                (sinThetaSouth * sinThetaSouth * etaDown / (invDt * etaDown + Cr) -
-                 sinThetaNorth * sinThetaNorth * etaUp / (invDt * etaUp + Cr));
+            if (p->viscous) {
+                // bubble.cu:1460-1466: the viscous forces (gravity inside fv)
+                double fuWest = fu[cell], fuEast = fu[(long long)thetaId * nP + phiIdEast];
+                double fvNorth = 0.0, fvSouth = 0.0;
+                if (thetaId != 0) fvNorth = fv[(long long)(thetaId - 1) * nP + phiId];
+                if ((size_t)thetaId != c.nTheta - 1) fvSouth = fv[cell];
+                sinThetaDiv += c.invGridLen *
+                    (sinThetaSouth * fvSouth * etaDown / (invDt * etaDown + Cr) -
+                     sinThetaNorth * fvNorth * etaUp / (invDt * etaUp + Cr) +
+                     fuEast * etaRight / (invDt * etaRight + Cr) -
+                     fuWest * etaLeft / (invDt * etaLeft + Cr));
+            } else {
+                sinThetaDiv += p->gs * c.invGridLen *
+                    (sinThetaSouth * sinThetaSouth * etaDown / (invDt * etaDown + Cr) -
+                     sinThetaNorth * sinThetaNorth * etaUp / (invDt * etaUp + Cr));
+            }
             rhs[idx] = sinTheta * invDt - sinThetaDiv;
         }
     })
@@ -910,6 +924,278 @@ void applyForceVelPhi(const sb_oracle_params* p, const Ctx& c, double* out, cons
     })
 }
 
+// ---------------------------------------------------------------------------
+// VISCOUS variant (include/header.cuh:98, off in the reference's build):
+// viscous stress forces fv (u_theta faces) and fu (u_phi faces) from the
+// advected velocities and thickness, fed to the surfactant system's
+// right-hand side in place of the gravity term and to the velocity update
+// (Solver::bodyforce, bubble.cu:2406-2420, 2454-2476).
+// ---------------------------------------------------------------------------
+
+// helper_math.h's clamp is fmaxf(a, fminf(f, b)) with float, int and uint
+// overloads only, so the reference's clamp(double, -0.1, 0.1) runs in float
+// (strict mode mimics the rounding); a NaN force comes out as 0.1 either way.
+inline double clamp_force(int strict, double v) {
+    if (strict) return (double)std::fmax(-0.1f, std::fmin((float)v, 0.1f));
+    return std::fmax(-0.1, std::fmin(v, 0.1));
+}
+
+// bubble.cu:1218-1269 (divergenceKernel): div u at the cell centres.
+void divergenceFromVelocity(const sb_oracle_params* p, const Ctx& c, double* div,
+                            const double* velPhi, const double* velTheta) {
+    const long long nP = p->nPhi; const int nth = nthreads_of(p);
+    const long long nT = p->nTheta;
+    CELL_LOOP(p->nTheta, {
+        double thetaCoord = ((double)thetaId + 0.5) * c.gridLen;
+        double halfStep = 0.5 * c.gridLen;
+        double uWest = velPhi[cell];
+        double uEast = velPhi[(long long)thetaId * nP + (phiId + 1) % nP];
+        double vNorth = 0.0, vSouth = 0.0;
+        if (thetaId != 0) vNorth = velTheta[(long long)(thetaId - 1) * nP + phiId];
+        if (thetaId != nT - 1) vSouth = velTheta[cell];
+        double invGridSine = 1.0 / ssin(c.strict, thetaCoord);
+        double sinNorth = ssin(c.strict, thetaCoord - halfStep);
+        double sinSouth = ssin(c.strict, thetaCoord + halfStep);
+        double factor = invGridSine * c.invGridLen;
+        double termTheta = factor * (vSouth * sinSouth - vNorth * sinNorth);
+        double termPhi = c.invGridLen * (uEast - uWest);
+        div[cell] = termTheta + termPhi;
+    })
+}
+
+// bubble.cu:1512-1643 (computeforcevelthetaKernel): fv on the u_theta faces,
+// gravity included.
+void computeForceVelTheta(const sb_oracle_params* p, const Ctx& c, double* fv,
+                          const double* velTheta, const double* velPhi, const double* thickness,
+                          const double* divCentered) {
+    const long long nP = p->nPhi; const int nth = nthreads_of(p);
+    const long long nT = p->nTheta;
+    const double ih = c.invGridLen;
+    CELL_LOOP(p->nTheta - 1, {
+        double gTheta = ((double)thetaId + 1.0) * c.gridLen;
+        long long tN = thetaId, tS = thetaId + 1;
+        long long pW = (phiId - 1 + nP) % nP, pE = (phiId + 1) % nP;
+        double u0 = velPhi[tN * nP + phiId], u1 = velPhi[tN * nP + pE];
+        double u2 = velPhi[tS * nP + phiId], u3 = velPhi[tS * nP + pE];
+        double divNorth = divCentered[tN * nP + phiId], divSouth = divCentered[tS * nP + phiId];
+        double EtaNorth = thickness[tN * nP + phiId], EtaSouth = thickness[tS * nP + phiId];
+        double invEta = 2. / (EtaNorth + EtaSouth);
+        if (std::isinf(invEta)) {
+            fv[cell] = NAN;
+        } else {
+            double div = 0.5 * (divNorth + divSouth);
+            double uPhi = 0.25 * (u0 + u1 + u2 + u3);
+            double d0 = thickness[tN * nP + pW], d1 = thickness[tN * nP + pE];
+            double d2 = thickness[tS * nP + pW], d3 = thickness[tS * nP + pE];
+            double pDpx = 0.25 * ih * (d1 + d3 - d0 - d2);
+            double pDpy = ih * (EtaSouth - EtaNorth);
+            double v1 = velTheta[cell];
+            double v3 = velTheta[tN * nP + pW], v4 = velTheta[tN * nP + pE];
+            long long opp = (phiId + nP / 2) % nP;
+            double v0, v2;
+            if (thetaId != 0) v0 = velTheta[(tN - 1) * nP + phiId];
+            else v0 = 0.5 * (velTheta[cell] - velTheta[tN * nP + opp]);
+            if (thetaId != nT - 2) v2 = velTheta[tS * nP + phiId];
+            else v2 = 0.5 * (velTheta[cell] - velTheta[tN * nP + opp]);
+            double pvpy = 0.5 * ih * (v2 - v0);
+            double pvpyNorth = ih * (v1 - v0);
+            double pvpySouth = ih * (v2 - v1);
+            double pvpx = 0.5 * ih * (v4 - v3);
+            double pupy = 0.5 * ih * (u2 + u3 - u0 - u1);
+            double pupx = 0.5 * ih * (u1 + u3 - u0 - u2);
+            double pupxy = ih * ih * (u0 + u3 - u1 - u2);
+            double pvpxx = ih * ih * (v3 + v4 - 2 * v1);
+            double sinTheta = std::sin(gTheta);
+            double cscTheta = 1. / sinTheta;
+            double cosTheta = std::cos(gTheta);
+            double cotTheta = cosTheta * cscTheta;
+            double sigma11North = 0. + 2. * (pvpyNorth + divNorth);
+            double sigma11South = 0. + 2. * (pvpySouth + divSouth);
+            double sigma22 = -2. * (pvpy - 2. * div);
+            double sigma12 = cscTheta * pvpx + pupy - uPhi * cotTheta;
+            double halfStep = 0.5 * c.gridLen;
+            double sinNorth = std::sin(gTheta - halfStep);
+            double sinSouth = std::sin(gTheta + halfStep);
+            double psspy = ih * (sigma11South * sinSouth - sigma11North * sinNorth);
+            double pspx = cscTheta * pvpxx + pupxy - cotTheta * pupx;
+            double f2 = p->re * cscTheta * invEta * pDpx * sigma12;
+            double f4 = p->re * invEta * pDpy * 2 * (div + pvpy);
+            double f5 = p->re * cscTheta * (psspy + pspx - cosTheta * sigma22);
+            double f7 = p->gs * sinTheta;
+            fv[cell] = clamp_force(c.strict, f2 + f5 + f4) + f7;
+            if (sinTheta < 0.1) fv[cell] = f7;
+        }
+    })
+}
+
+// bubble.cu:1647-1816 (computeforcevelphiKernel_viscous): fu on the u_phi
+// faces.
+void computeForceVelPhi(const sb_oracle_params* p, const Ctx& c, double* fu,
+                        const double* velPhi, const double* velTheta, const double* thickness,
+                        const double* divCentered) {
+    const long long nP = p->nPhi; const int nth = nthreads_of(p);
+    const long long nT = p->nTheta;
+    const double ih = c.invGridLen;
+    CELL_LOOP(p->nTheta, {
+        double gTheta = ((double)thetaId + 0.5) * c.gridLen;
+        long long t0 = thetaId;
+        long long pW = (phiId - 1 + nP) % nP;
+        long long oppW = (pW + nP / 2) % nP, opp = (phiId + nP / 2) % nP;
+        double divWest = divCentered[t0 * nP + pW], divEast = divCentered[cell];
+        double EtaWest = thickness[t0 * nP + pW], EtaEast = thickness[cell];
+        double v0, v1, v2, v3;
+        if (thetaId != 0) {
+            v0 = velTheta[(t0 - 1) * nP + pW];
+            v1 = velTheta[(t0 - 1) * nP + phiId];
+        } else {
+            v0 = 0.5 * (velTheta[t0 * nP + pW] - velTheta[t0 * nP + oppW]);
+            v1 = 0.5 * (velTheta[t0 * nP + phiId] - velTheta[t0 * nP + opp]);
+        }
+        if (thetaId != nT - 1) {
+            v2 = velTheta[t0 * nP + pW];
+            v3 = velTheta[t0 * nP + phiId];
+        } else {
+            v2 = 0.5 * (velTheta[(t0 - 1) * nP + pW] - velTheta[(t0 - 1) * nP + oppW]);
+            v3 = 0.5 * (velTheta[(t0 - 1) * nP + phiId] - velTheta[(t0 - 1) * nP + opp]);
+        }
+        double invEta = 2. / (EtaWest + EtaEast);
+        if (std::isinf(invEta)) {
+            fu[cell] = NAN;
+        } else {
+            double div = 0.5 * (divWest + divEast);
+            double pvpx = 0.5 * ih * (v1 + v3 - v0 - v2);
+            double pvpyWest = ih * (v2 - v0);
+            double pvpyEast = ih * (v3 - v1);
+            double pvpy = 0.5 * ih * (v2 + v3 - v0 - v1);
+            double pupyNorth = 0.0, pupySouth = 0.0;
+            double u1 = velPhi[cell], u3, u4;
+            if (thetaId != 0) {
+                u3 = velPhi[(t0 - 1) * nP + phiId];
+                pupyNorth = ih * (u1 - u3);
+            } else {
+                u3 = -velPhi[t0 * nP + opp];
+            }
+            if (thetaId != nT - 1) {
+                u4 = velPhi[(t0 + 1) * nP + phiId];
+                pupySouth = ih * (u4 - u1);
+            } else {
+                u4 = -velPhi[t0 * nP + opp];
+            }
+            double pupy = 0.5 * ih * (u4 - u3);
+            double sinTheta = std::sin(gTheta);
+            double cscTheta = 1. / sinTheta;
+            double cosTheta = std::cos(gTheta);
+            double cotTheta = cosTheta * cscTheta;
+            double sigma12 = cscTheta * pvpx + pupy - u1 * cotTheta;
+            double pDpx = ih * (EtaEast - EtaWest);
+            double d0, d1, d2, d3;
+            if (thetaId != 0) {
+                d0 = thickness[(t0 - 1) * nP + pW];
+                d2 = thickness[(t0 - 1) * nP + phiId];
+            } else {
+                d0 = thickness[t0 * nP + oppW];
+                d2 = thickness[t0 * nP + opp];
+            }
+            if (thetaId != nT - 1) {
+                d1 = thickness[(t0 + 1) * nP + pW];
+                d3 = thickness[(t0 + 1) * nP + phiId];
+            } else {
+                d1 = thickness[t0 * nP + oppW];
+                d3 = thickness[t0 * nP + opp];
+            }
+            double pDpy = 0.25 * ih * (d1 + d3 - d0 - d2);
+            double halfStep = 0.5 * c.gridLen;
+            double sinNorth = ssin(c.strict, gTheta - halfStep);
+            double sinSouth = ssin(c.strict, gTheta + halfStep);
+            double cosNorth = scos(c.strict, gTheta - halfStep);
+            double cosSouth = scos(c.strict, gTheta + halfStep);
+            double uNorth = 0.5 * (u3 + u1);
+            double uSouth = 0.5 * (u1 + u4);
+            if (thetaId == 0) uNorth = 0.5 * (u1 - u3);
+            if (thetaId == nT - 1) uSouth = 0.5 * (u1 - u4);
+            double psspy = ih * (ih * (v0 + v3 - v1 - v2) + sinSouth * pupySouth -
+                                 sinNorth * pupyNorth - cosSouth * uSouth + cosNorth * uNorth);
+            double sigma22West = 2 * (2 * divWest - pvpyWest);
+            double sigma22East = 2 * (2 * divEast - pvpyEast);
+            double pspx = ih * (sigma22East - sigma22West);
+            double f2 = p->re * invEta * pDpy * sigma12;
+            double f4 = p->re * invEta * cscTheta * pDpx * 2 * (2 * div - pvpy);
+            double f5 = p->re * cscTheta * (psspy + pspx + cosTheta * sigma12);
+            fu[cell] = clamp_force(c.strict, f2 + f4 + f5);
+            if (sinTheta < 0.1) fu[cell] = 0.;
+        }
+    })
+}
+
+// bubble.cu:1940-1983 (applyforcevelthetaKernel_viscous): backward Euler
+// with Marangoni, mirrored wind (flat index nPhi - phi) and fv.
+void applyForceVelThetaViscous(const sb_oracle_params* p, const Ctx& c, double* out,
+                               const double* in, const double* thickness, const double* conc,
+                               const double* vair, const double* fv) {
+    const long long nP = p->nPhi; const int nth = nthreads_of(p);
+    const double dt = p->dt, t = p->t;
+    CELL_LOOP(p->nTheta - 1, {
+        long long s = cell + nP;
+        double GammaNorth = conc[cell], GammaSouth = conc[s];
+        double EtaNorth = thickness[cell], EtaSouth = thickness[s];
+        double invEta = 2. / (EtaNorth + EtaSouth);
+        if (std::isinf(invEta)) {
+            out[cell] = NAN;
+        } else {
+            double v1 = in[cell];
+            double pGpy = c.invGridLen * (GammaSouth - GammaNorth);
+            double f3 = -p->M * invEta * pGpy;
+            long long opp = nP - phiId;
+            double vAir = 0.5 * (vair[(long long)thetaId * nP + phiId] * t / 12.0 -
+                                 vair[(long long)thetaId * nP + opp] * (1 - t / 12.0));
+            double f6 = p->Cr * invEta * vAir;
+            out[cell] = (v1 / dt + f3 + f6 + fv[cell]) / (1. / dt + p->Cr * invEta);
+        }
+    })
+}
+
+// bubble.cu:1987-2038 (applyforcevelphiKernel_viscous).
+void applyForceVelPhiViscous(const sb_oracle_params* p, const Ctx& c, double* out,
+                             const double* in, const double* thickness, const double* conc,
+                             const double* uair, const double* fu) {
+    const long long nP = p->nPhi; const int nth = nthreads_of(p);
+    const double dt = p->dt, t = p->t;
+    CELL_LOOP(p->nTheta, {
+        double gTheta = ((double)thetaId + 0.5) * c.gridLen;
+        long long w = (long long)thetaId * nP + (phiId - 1 + nP) % nP;
+        double EtaWest = thickness[w], EtaEast = thickness[cell];
+        double GammaWest = conc[w], GammaEast = conc[cell];
+        double invEta = 2. / (EtaWest + EtaEast);
+        if (std::isinf(invEta)) {
+            out[cell] = NAN;
+        } else {
+            double u1 = in[cell];
+            double cscTheta = 1. / std::sin(gTheta);
+            double pGpx = c.invGridLen * (GammaEast - GammaWest);
+            double f3 = -p->M * invEta * cscTheta * pGpx;
+            long long opp = nP - phiId;
+            double uAir = 0.5 * (uair[(long long)thetaId * nP + phiId] * t / 12.0 +
+                                 uair[(long long)thetaId * nP + opp] * (1 - t / 12.0));
+            double f6 = p->Cr * invEta * uAir;
+            out[cell] = (u1 / dt + f3 + f6 + fu[cell]) / (1. / dt + p->Cr * invEta);
+        }
+    })
+}
+
+// Solver::bodyforce under VISCOUS (bubble.cu:2406-2420): div u, then fv and
+// fu; empty vectors when the variant is off.
+void viscousForces(const sb_oracle_params* p, const Ctx& c, const sb_oracle_state* s,
+                   std::vector<double>& fu, std::vector<double>& fv) {
+    if (!p->viscous) return;
+    const size_t N = (size_t)p->nTheta * p->nPhi, Nv = N - (size_t)p->nPhi;
+    std::vector<double> div(N);
+    fu.assign(N, 0.0);
+    fv.assign(Nv, 0.0);
+    divergenceFromVelocity(p, c, div.data(), s->uph, s->uth);
+    computeForceVelTheta(p, c, fv.data(), s->uth, s->uph, s->eta, div.data());
+    computeForceVelPhi(p, c, fu.data(), s->uph, s->uth, s->eta, div.data());
+}
+
 // bubble.cu:2041-2063
 void applyForceThickness(const sb_oracle_params* p, double* out, const double* in, double* delta,
                          const double* div) {
@@ -1041,6 +1327,7 @@ void sb_oracle_default_params(sb_oracle_params* p, int nTheta, double radius, do
     p->M = Gamma_m * sigma_r / (3 * kRho * H * U * U);
     p->Cr = kRhoA * std::sqrt(kNuA * radius / U) / (kRho * H);
     p->gs = kG * radius / (U * U);
+    p->re = kNu / (U * radius);
     p->gammaMax = kSigmaA / sigma_r / Gamma_m;
     p->dt = dt_s * U / radius;
     p->evapRate = kEvaporation * radius / (H * U);
@@ -1057,6 +1344,15 @@ void sb_oracle_default_params(sb_oracle_params* p, int nTheta, double radius, do
 
 void sb_oracle_identity_map(int nTheta, int nPhi, double* map_t, double* map_p) {
     initMapping(nTheta, nPhi, map_t, map_p);
+}
+
+void sb_oracle_viscous_forces(const sb_oracle_params* p, const double* uth, const double* uph,
+                              const double* eta, double* div, double* fv, double* fu) {
+    std::atomic<long> oob{0};
+    Ctx c = make_ctx(p, &oob);
+    divergenceFromVelocity(p, c, div, uph, uth);
+    computeForceVelTheta(p, c, fv, uth, uph, eta, div);
+    computeForceVelPhi(p, c, fu, uph, uth, eta, div);
 }
 
 // Solver::updateForward / updateBackward (bubble.cu:1049-1116); the new map
@@ -1138,9 +1434,11 @@ void sb_oracle_assemble(const sb_oracle_params* p, const sb_oracle_state* s, dou
     Ctx c = make_ctx(p, &oob);
     const size_t N = (size_t)p->nTheta * p->nPhi;
     airFlow(p, c, s->uair_init, s->vair_init, uair, vair);
-    std::vector<double> W(N);
+    std::vector<double> W(N), fu, fv;
     vanDerWaals(p, W.data(), s->eta);
-    concentrationLinearSystem(p, c, s->uph, s->uth, gamma, s->eta, W.data(), uair, vair, val, rhs);
+    viscousForces(p, c, s, fu, fv);
+    concentrationLinearSystem(p, c, s->uph, s->uth, gamma, s->eta, W.data(), uair, vair,
+                              fu.data(), fv.data(), val, rhs);
 }
 
 int sb_oracle_solve(const sb_oracle_params* p, const double* val, const double* rhs, double* x,
@@ -1157,17 +1455,26 @@ int sb_oracle_bodyforce(const sb_oracle_params* p, sb_oracle_state* s, sb_oracle
     std::vector<double> uair(N + 1), vair(Nv + 1), W(N), val(5 * N), rhs(N);
     airFlow(p, c, s->uair_init, s->vair_init, uair.data(), vair.data());
     vanDerWaals(p, W.data(), s->eta);  // stored in thickness->NextStep by the reference
+    std::vector<double> fu, fv;
+    viscousForces(p, c, s, fu, fv);
     concentrationLinearSystem(p, c, s->uph, s->uth, s->gamma, s->eta, W.data(), uair.data(),
-                              vair.data(), val.data(), rhs.data());
+                              vair.data(), fu.data(), fv.data(), val.data(), rhs.data());
     std::vector<double> gamNext(s->gamma, s->gamma + N);
     double rel = 0.0;
     int iters = solveSystem(p, val.data(), rhs.data(), gamNext.data(), &rel);
     std::vector<double> div(N), uthN(Nv), uphN(N), tmp_t(N), tmp_p(N), etaN(N);
     divergenceFromGamma(p, div.data(), gamNext.data(), s->gamma);
-    applyForceVelTheta(p, c, uthN.data(), s->uth, tmp_t.data(), s->eta, W.data(), gamNext.data(),
-                       vair.data());
-    applyForceVelPhi(p, c, uphN.data(), s->uph, tmp_p.data(), s->eta, W.data(), gamNext.data(),
-                     uair.data());
+    if (p->viscous) {
+        applyForceVelThetaViscous(p, c, uthN.data(), s->uth, s->eta, gamNext.data(), vair.data(),
+                                  fv.data());
+        applyForceVelPhiViscous(p, c, uphN.data(), s->uph, s->eta, gamNext.data(), uair.data(),
+                                fu.data());
+    } else {
+        applyForceVelTheta(p, c, uthN.data(), s->uth, tmp_t.data(), s->eta, W.data(),
+                           gamNext.data(), vair.data());
+        applyForceVelPhi(p, c, uphN.data(), s->uph, tmp_p.data(), s->eta, W.data(),
+                         gamNext.data(), uair.data());
+    }
     applyForceThickness(p, etaN.data(), s->eta, tmp_t.data(), div.data());
     accumulateChangesCentered(p, c, s->eta_delta, tmp_t.data(), s->fwd_t, s->fwd_p);
     for (size_t i = 0; i < N; ++i) tmp_p[i] = gamNext[i] - s->gamma[i];

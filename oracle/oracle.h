@@ -46,6 +46,9 @@ typedef struct {
     /* the reference's compile-time switches (include/header.cuh:89, 96) */
     int plain_advection;       /* 1: BIMOCQ undefined (advectionAllCentered, no maps) */
     int single_step_velocity;  /* 1: RUNGE_KUTTA undefined (velocity traced in one step) */
+    int viscous;               /* 1: VISCOUS defined (include/header.cuh:98): viscous stress
+                                  forces in the system and the velocity update */
+    double re;                 /* reGlobal = nu / (U r), nu = 1.25e-4 (bubble.cu:2575) */
 } sb_oracle_params;
 
 typedef struct {
@@ -102,6 +105,10 @@ void sb_oracle_sample_mapping(const sb_oracle_params* p, const double* map_t,
 void sb_oracle_airflow(const sb_oracle_params* p, const double* uair_init,
                        const double* vair_init, double* uair, double* vair);
 void sb_oracle_identity_map(int nTheta, int nPhi, double* map_t, double* map_p);
+/* VISCOUS variant: div u (N), fv (Nv, gravity included) and fu (N) from the
+ * velocities and thickness (kernel/bubble.cu:1218-1269, 1512-1816). */
+void sb_oracle_viscous_forces(const sb_oracle_params* p, const double* uth, const double* uph,
+                              const double* eta, double* div, double* fv, double* fu);
 
 #ifdef __cplusplus
 }

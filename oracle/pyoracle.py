@@ -32,6 +32,7 @@ class Params(C.Structure):
         ("W2", C.c_double), ("blend", C.c_double), ("U", C.c_double), ("strict", C.c_int),
         ("force_reinit", C.c_int), ("solver_tol", C.c_double), ("solver_max_iter", C.c_int),
         ("nthreads", C.c_int), ("plain_advection", C.c_int), ("single_step_velocity", C.c_int),
+        ("viscous", C.c_int), ("re", C.c_double),
     ]
 
 
@@ -79,6 +80,7 @@ def lib():
         L.sb_oracle_sample_mapping.argtypes = [P, dp, dp, C.c_int, dp, dp]
         L.sb_oracle_airflow.argtypes = [P, dp, dp, dp, dp]
         L.sb_oracle_identity_map.argtypes = [C.c_int, C.c_int, dp, dp]
+        L.sb_oracle_viscous_forces.argtypes = [P, dp, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -211,3 +213,14 @@ def identity_map(nTheta: int):
     t, ph = np.zeros((nTheta, nPhi)), np.zeros((nTheta, nPhi))
     lib().sb_oracle_identity_map(nTheta, nPhi, _p(t), _p(ph))
     return t, ph
+
+
+def viscous_forces(params: Params, uth, uph, eta):
+    """div u, fv (u_theta faces, gravity included) and fu (u_phi faces) of the
+    VISCOUS variant."""
+    nT, nP = params.nTheta, params.nPhi
+    c = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (uth, uph, eta)]
+    div, fv, fu = np.zeros(nT * nP), np.zeros((nT - 1) * nP), np.zeros(nT * nP)
+    lib().sb_oracle_viscous_forces(C.byref(params), _p(c[0]), _p(c[1]), _p(c[2]), _p(div),
+                                   _p(fv), _p(fu))
+    return div.reshape(nT, nP), fv.reshape(nT - 1, nP), fu.reshape(nT, nP)

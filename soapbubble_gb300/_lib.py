@@ -31,7 +31,8 @@ class SbParams(C.Structure):
         ("gs_scale", C.c_double), ("M_scale", C.c_double), ("solver_mode", C.c_int),
         ("solver_tol", C.c_double), ("solver_max_iter", C.c_int), ("force_reinit", C.c_int),
         ("nu_scale", C.c_double), ("storage", C.c_int), ("plain_advection", C.c_int),
-        ("single_step_velocity", C.c_int),
+        ("single_step_velocity", C.c_int), ("viscous", C.c_int),
+        ("write_velocity_frames", C.c_int), ("write_concentration_frames", C.c_int),
     ]
 
 
@@ -114,13 +115,16 @@ def lib() -> C.CDLL:
     L.sb_init_thickness_from_exr.argtypes = [H, C.c_char_p]
     L.sb_init_airflow_from_exr.argtypes = [H, C.c_char_p]
     L.sb_exr_load_resized.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, dp]
+    L.sb_write_velocity_exr.argtypes = [H, C.c_char_p]
+    L.sb_write_concentration_exr.argtypes = [H, C.c_char_p]
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
                  "sb_download_field", "sb_step", "sb_step_timed", "sb_autotune", "sb_upload_field_f32",
                  "sb_download_field_f32", "sb_synchronize", "sb_get_stats",
                  "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
                  "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
-                 "sb_init_thickness_from_exr", "sb_init_airflow_from_exr", "sb_exr_load_resized"):
+                 "sb_init_thickness_from_exr", "sb_init_airflow_from_exr", "sb_exr_load_resized",
+                 "sb_write_velocity_exr", "sb_write_concentration_exr"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -140,4 +144,4 @@ EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",
            "sb_batch_step_timed", "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
            "sb_batch_stream", "sb_init_thickness_from_exr", "sb_init_airflow_from_exr",
-           "sb_exr_load_resized"]
+           "sb_exr_load_resized", "sb_write_velocity_exr", "sb_write_concentration_exr"]

@@ -34,7 +34,8 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
                 solver_tol: float = 1e-6, solver_max_iter: int = 1000, force_reinit: int = 0,
                 gs_scale: float = 0.0, M_scale: float = 0.0, nu_scale: float = 0.0,
                 device: int = 0, storage: int = 0, plain_advection: int = 0,
-                single_step_velocity: int = 0) -> SbParams:
+                single_step_velocity: int = 0, viscous: int = 0,
+                write_velocity_frames: int = 0, write_concentration_frames: int = 0) -> SbParams:
     p = default_params()
     p.nTheta, p.dt, p.radius, p.H, p.Gamma_m, p.T = nTheta, dt, radius, H, Gamma_m, T
     p.blendCoeff = blendCoeff
@@ -46,6 +47,9 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
     p.storage = storage  # 0: FP32, 1: BF16 thickness / surfactant fields
     p.plain_advection = plain_advection            # 1: BIMOCQ off
     p.single_step_velocity = single_step_velocity  # 1: RUNGE_KUTTA off
+    p.viscous = viscous                            # 1: VISCOUS on
+    p.write_velocity_frames = write_velocity_frames
+    p.write_concentration_frames = write_concentration_frames
     return p
 
 
@@ -165,6 +169,13 @@ class GpuBubble:
         check(lib().sb_write_thickness_exr(self.h, path.encode(), C.byref(broken)),
               "sb_write_thickness_exr")
         return bool(broken.value)
+
+    def write_velocity_exr(self, path: str) -> None:
+        check(lib().sb_write_velocity_exr(self.h, path.encode()), "sb_write_velocity_exr")
+
+    def write_concentration_exr(self, path: str) -> None:
+        check(lib().sb_write_concentration_exr(self.h, path.encode()),
+              "sb_write_concentration_exr")
 
     def run(self, out_dir: Optional[str], frames: int = 0) -> None:
         check(lib().sb_run(self.h, out_dir.encode() if out_dir else None, frames), "sb_run")

@@ -43,6 +43,7 @@ constexpr double kHalfPi = 1.57079632679489661923;
 // include/header.cuh:76-83, 93
 constexpr double kGasR = 8.3144598, kSigmaA = 0.07275, kRho = 1e3, kG = 9.8;
 constexpr double kRhoA = 1.184, kNuA = 1.562e-5, kEvaporation = -0.00000003;
+constexpr double kNu = 1.25e-4;  // soap solution kinematic viscosity (VISCOUS variant)
 
 struct Layout {
     size_t bytes = 0;
@@ -103,6 +104,8 @@ void derive_phys(const sb_params& p, SbPhys& ph) {
     const double nuA = kNuA * (p.nu_scale > 0 ? p.nu_scale : 1.0);
     ph.Cr = (float)(kRhoA * std::sqrt(nuA * p.radius / U) / (kRho * p.H));
     ph.gs = (float)gs;
+    ph.re = (float)(kNu / (U * p.radius));
+    ph.viscous = p.viscous ? 1 : 0;
     ph.gmax = (float)(kSigmaA / sigma_r / p.Gamma_m);
     ph.blend = (float)p.blendCoeff;
     ph.evap = (float)(kEvaporation * p.radius / (p.H * U));
@@ -567,6 +570,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
         P.maxNP = g.nP;
         P.solver = b->solver;
         P.storage = b->storage;
+        P.viscous = b->ph.viscous;
         b->desc = d;
         P.one = &b->desc;
         if (e != cudaSuccess) rc = cuda_fail(e, "step plan");
@@ -986,22 +990,76 @@ int sb_write_thickness_exr(sb_bubble* b, const char* path, int* broken) {
     return SB_OK;
 }
 
+int sb_write_velocity_exr(sb_bubble* b, const char* path) {
+    if (!b || !path) return fail(SB_ERR_INVALID, "null argument");
+    const int nT = b->g.nT, nP = b->g.nP;
+    std::vector<float> uph((size_t)nT * nP), uth((size_t)(nT - 1) * nP);
+    int rc = sb_download_field_f32(b, SB_UPHI, uph.data(), uph.size());
+    if (rc == SB_OK) rc = sb_download_field_f32(b, SB_UTHETA, uth.data(), uth.size());
+    if (rc != SB_OK) return rc;
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    // Solver::write_velocity_image (kernel/solver.cu:388-497): face velocities
+    // averaged to the cell centres; at the poles the missing face is
+    // extrapolated from the nearest face row and its opposite meridian
+    const size_t N = (size_t)nT * nP;
+    std::vector<float> R(N), G(N), B(N, 0.5f);
+    auto vt = [&](int t, int p) { return (double)uth[(size_t)t * nP + p]; };
+    for (int j = 0; j < nT; ++j)
+        for (int i = 0; i < nP; ++i) {
+            const int opp = (i + nP / 2) % nP;
+            const double uW = uph[(size_t)j * nP + i];
+            const double uE = uph[(size_t)j * nP + (i + 1) % nP];
+            const double vN = j != 0 ? vt(j - 1, i) : 0.75 * vt(j, i) - 0.25 * vt(j, opp);
+            const double vS = j != nT - 1 ? vt(j, i) : 0.75 * vt(j - 1, i) - 0.25 * vt(j - 1, opp);
+            const double u = 0.5 * (uW + uE), v = 0.5 * (vN + vS);
+            R[(size_t)j * nP + i] = (float)(u / 2 + 0.5);
+            G[(size_t)j * nP + i] = (float)(v / 2 + 0.5);
+        }
+    if (!write_exr_bgr(path, nP, nT, B.data(), G.data(), R.data()))
+        return fail(SB_ERR_IO, std::string("cannot write ") + path);
+    return SB_OK;
+}
+
+int sb_write_concentration_exr(sb_bubble* b, const char* path) {
+    if (!b || !path) return fail(SB_ERR_INVALID, "null argument");
+    const size_t N = (size_t)b->g.N;
+    std::vector<float> gam(N);
+    int rc = sb_download_field_f32(b, SB_GAMMA, gam.data(), N);
+    if (rc != SB_OK) return rc;
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    // Solver::write_concentration_image (kernel/solver.cu:500-538)
+    std::vector<float> img(N);
+    for (size_t c = 0; c < N; ++c) img[c] = (float)(((double)gam[c] - 0.9) / 0.2);
+    if (!write_exr_gray3(path, b->g.nP, b->g.nT, img.data()))
+        return fail(SB_ERR_IO, std::string("cannot write ") + path);
+    return SB_OK;
+}
+
 int sb_run(sb_bubble* b, const char* out_dir, int frames) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     const sb_params& p = b->params;
     if (frames <= 0) frames = p.frames;
     std::string dir = out_dir ? out_dir : "";
     if (!dir.empty() && dir.back() != '/') dir.push_back('/');
-    auto frame_path = [&](int i) {
+    auto frame_path = [&](const char* kind, int i) {
         char name[32];
-        std::snprintf(name, sizeof(name), "frame%04d.exr", i);
+        std::snprintf(name, sizeof(name), "%s%04d.exr", kind, i);
         return dir + name;
     };
-    int broken = 0, rc = SB_OK;
-    if (out_dir) {
-        rc = sb_write_thickness_exr(b, frame_path(0).c_str(), &broken);
-        if (rc != SB_OK) return rc;
-    }
+    // frame i: thickness (WRITE_THICKNESS_DATA), and velocity and surfactant
+    // when asked (WRITE_VELOCITY_DATA / WRITE_CONCENTRATION_DATA,
+    // kernel/bubble.cu:2643-2651, 2686-2694)
+    int broken = 0;
+    auto write_frame = [&](int i) {
+        int r = sb_write_thickness_exr(b, frame_path("frame", i).c_str(), &broken);
+        if (r == SB_OK && p.write_velocity_frames)
+            r = sb_write_velocity_exr(b, frame_path("vel", i).c_str());
+        if (r == SB_OK && p.write_concentration_frames)
+            r = sb_write_concentration_exr(b, frame_path("con", i).c_str());
+        return r;
+    };
+    int rc = SB_OK;
+    if (out_dir && (rc = write_frame(0)) != SB_OK) return rc;
     // Bubble::run frame loop (kernel/bubble.cu:2656-2696); U = 1
     const double dt_ = p.dt, DT = p.DT;
     double T = 0.0;
@@ -1020,10 +1078,7 @@ int sb_run(sb_bubble* b, const char* out_dir, int frames) {
         if ((rc = sb_get_stats(b, &st)) != SB_OK) return rc;
         if (!st.solver_converged) return fail(SB_ERR_NOT_CONVERGED, "implicit solve did not converge");
         T = i * DT;
-        if (out_dir) {
-            rc = sb_write_thickness_exr(b, frame_path(i).c_str(), &broken);
-            if (rc != SB_OK) return rc;
-        }
+        if (out_dir && (rc = write_frame(i)) != SB_OK) return rc;
     }
     if (broken) return fail(SB_ERR_BROKEN, "film is broken");
     return SB_OK;
@@ -1097,6 +1152,7 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     SbStepPlan& P = B->plan;
     P.solver = bubbles[0]->solver;
     P.storage = bubbles[0]->storage;
+    P.viscous = bubbles[0] ? bubbles[0]->ph.viscous : 0;
     for (int k = 0; k < n; ++k) {
         sb_bubble* b = bubbles[k];
         if (!b || b->device != B->device) {
@@ -1112,6 +1168,10 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
         if (b->storage != P.storage) {
             delete B;
             return fail(SB_ERR_INVALID, "batch members must share one field storage");
+        }
+        if (b->ph.viscous != P.viscous) {
+            delete B;
+            return fail(SB_ERR_INVALID, "batch members must share the viscous switch");
         }
         B->m.push_back(b);
         if (b->g.nP > P.maxNP) P.maxNP = b->g.nP;

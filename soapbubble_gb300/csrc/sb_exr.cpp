@@ -66,6 +66,11 @@ void attr(std::vector<unsigned char>& v, const char* name, const char* type, uin
 }  // namespace
 
 bool write_exr_gray3(const char* path, int width, int height, const float* img) {
+    return write_exr_bgr(path, width, height, img, img, img);
+}
+
+bool write_exr_bgr(const char* path, int width, int height, const float* b, const float* g,
+                   const float* r) {
     std::vector<unsigned char> h;
     h.push_back(0x76); h.push_back(0x2f); h.push_back(0x31); h.push_back(0x01);
     put_u32(h, 2u);  // version 2, single-part scanline
@@ -98,7 +103,7 @@ bool write_exr_gray3(const char* path, int width, int height, const float* img) 
     const uint64_t chunk = 8 + (uint64_t)width * 3 * 2;
     const uint64_t first = h.size() + 8ull * (uint64_t)height;
     for (int y = 0; y < height; ++y) put_u64(h, first + chunk * (uint64_t)y);
-    std::vector<unsigned short> row((size_t)width);
+    const float* planes[3] = {b, g, r};  // channel order B, G, R
     std::FILE* fp = std::fopen(path, "wb");
     if (!fp) return false;
     bool ok = std::fwrite(h.data(), 1, h.size(), fp) == h.size();
@@ -107,11 +112,11 @@ bool write_exr_gray3(const char* path, int width, int height, const float* img) 
         blk.clear();
         put_u32(blk, (uint32_t)y);
         put_u32(blk, (uint32_t)(width * 3 * 2));
-        for (int x = 0; x < width; ++x) row[x] = float_to_half(img[(size_t)y * width + x]);
         for (int c = 0; c < 3; ++c)
             for (int x = 0; x < width; ++x) {
-                blk.push_back((unsigned char)(row[x] & 0xff));
-                blk.push_back((unsigned char)(row[x] >> 8));
+                const unsigned short v = float_to_half(planes[c][(size_t)y * width + x]);
+                blk.push_back((unsigned char)(v & 0xff));
+                blk.push_back((unsigned char)(v >> 8));
             }
         ok = std::fwrite(blk.data(), 1, blk.size(), fp) == blk.size();
     }

@@ -11,6 +11,11 @@ namespace sb {
 // layout the reference writes through tinyexr (kernel/solver.cu:338-385).
 bool write_exr_gray3(const char* path, int width, int height, const float* img);
 
+// As write_exr_gray3 with three planes for the channels B, G and R (the
+// velocity frames of Solver::write_velocity_image, kernel/solver.cu:388-497).
+bool write_exr_bgr(const char* path, int width, int height, const float* b, const float* g,
+                   const float* r);
+
 // IEEE 754 binary32 -> binary16, round to nearest even.
 unsigned short float_to_half(float f);
 

@@ -177,6 +177,7 @@ struct SbStepPlan {
     int maxNP;                   // widest grid of the set
     SolverConfig solver;
     int storage;                 // SB_STORE_FP32 or SB_STORE_BF16 (the same for every bubble)
+    int viscous;                 // 1: viscous forces on (the same for every bubble)
     const SbBubbleDesc* one;     // host copy of the descriptor of a set of one bubble, else null
 };
 

@@ -11,7 +11,8 @@
 //   k_assemble     concentrationLinearSystemKernel (1301-1473)
 //   k_post         divergenceKernel_fromGamma, applyforcevel{theta,phi},
 //                  applyforceThickness, substractPitched (1276-1295, 1819-1935,
-//                  2041-2078)
+//                  2041-2078); the VISCOUS forces (1218-1269, 1512-1816,
+//                  1940-2038) in k_assemble and k_post
 //   k_accum        accumulateChangesCentered x2 (2081-2114),
 //                  estimateDistortionKernel + maxAbs (1131-1168, 1019-1043) and
 //                  the error of correctCentered1 (2180-2216)
@@ -182,6 +183,149 @@ __device__ __forceinline__ bool is_broken(float gamma, float eta, float gmax) {
     return gamma > gmax - kEps || eta == 0.0f;
 }
 
+// VISCOUS variant (include/header.cuh:98, off in the reference's build): the
+// film's viscous stress forces fv on the u_theta faces (gravity included) and
+// fu on the u_phi faces, from the advected velocities and thickness.  They
+// enter the system's right-hand side in place of the gravity term and the
+// velocity update.  k_assemble and k_post evaluate them where they need them
+// instead of storing them: the same function on the same inputs gives both
+// kernels the same values, and out-of-line calls keep the default path's
+// register allocation free of them.
+
+// div u at cell (i, j) (divergenceKernel, bubble.cu:1218-1269).
+__device__ __forceinline__ float vel_div(const SbGrid& g, const SbFields& f, int i, int j) {
+    const int nP = g.nP, c = i * nP + j;
+    const float uW = f.uph_adv[c], uE = f.uph_adv[i * nP + ((j + 1) & g.maskP)];
+    const float vN = i != 0 ? f.uth_adv[c - nP] : 0.0f;
+    const float vS = i != g.nT - 1 ? f.uth_adv[c] : 0.0f;
+    const float factor = (1.0f / g.sin_c[i]) * g.invh;
+    return factor * (vS * g.sin_e[i + 1] - vN * g.sin_e[i]) + g.invh * (uE - uW);
+}
+
+// helper_math.h's clamp(f, a, b) = fmaxf(a, fminf(f, b)).
+__device__ __forceinline__ float clamp_force(float v) { return fmaxf(-0.1f, fminf(v, 0.1f)); }
+
+// fv at u_theta face (i, j), i < nT - 1 (computeforcevelthetaKernel,
+// bubble.cu:1512-1643).
+__device__ __noinline__ float viscous_fv(const SbGrid& g, const SbPhys& ph, const SbFields& f,
+                                         int i, int j) {
+    const int nP = g.nP, mP = g.maskP;
+    const int jW = (j - 1) & mP, jE = (j + 1) & mP, jO = (j + nP / 2) & mP;
+    const int rN = i * nP, rS = rN + nP;
+    const float* __restrict__ u = f.uph_adv;
+    const float* __restrict__ v = f.uth_adv;
+    const float* __restrict__ e = f.eta_adv;
+    const float ih = g.invh;
+    const float etaN = e[rN + j], etaS = e[rS + j];
+    const float invEta = 2.0f / (etaN + etaS);
+    if (isinf(invEta)) return __int_as_float(0x7fffffff);
+    const float u0 = u[rN + j], u1 = u[rN + jE], u2 = u[rS + j], u3 = u[rS + jE];
+    const float divN = vel_div(g, f, i, j), divS = vel_div(g, f, i + 1, j);
+    const float div = 0.5f * (divN + divS);
+    const float uPhi = 0.25f * (u0 + u1 + u2 + u3);
+    const float pDpx = 0.25f * ih * (e[rN + jE] + e[rS + jE] - e[rN + jW] - e[rS + jW]);
+    const float pDpy = ih * (etaS - etaN);
+    const float v1 = v[rN + j], v3 = v[rN + jW], v4 = v[rN + jE];
+    const float vPole = 0.5f * (v1 - v[rN + jO]);  // across the pole
+    const float v0 = i != 0 ? v[rN - nP + j] : vPole;
+    const float v2 = i != g.nT - 2 ? v[rS + j] : vPole;
+    const float pvpy = 0.5f * ih * (v2 - v0);
+    const float pvpyN = ih * (v1 - v0), pvpyS = ih * (v2 - v1);
+    const float pvpx = 0.5f * ih * (v4 - v3);
+    const float pupy = 0.5f * ih * (u2 + u3 - u0 - u1);
+    const float pupx = 0.5f * ih * (u1 + u3 - u0 - u2);
+    const float pupxy = ih * ih * (u0 + u3 - u1 - u2);
+    const float pvpxx = ih * ih * (v3 + v4 - 2.0f * v1);
+    const float sinT = g.sin_e[i + 1], cosT = g.cos_e[i + 1];
+    const float cscT = 1.0f / sinT, cotT = cosT * cscT;
+    const float s11N = 2.0f * (pvpyN + divN), s11S = 2.0f * (pvpyS + divS);
+    const float s22 = -2.0f * (pvpy - 2.0f * div);
+    const float s12 = cscT * pvpx + pupy - uPhi * cotT;
+    // d/dtheta (sin theta sigma11) across the face's half-cells
+    const float psspy = ih * (s11S * g.sin_c[i + 1] - s11N * g.sin_c[i]);
+    const float pspx = cscT * pvpxx + pupxy - cotT * pupx;
+    const float re = ph.re;
+    const float f2 = re * cscT * invEta * pDpx * s12;
+    const float f4 = re * invEta * pDpy * 2.0f * (div + pvpy);
+    const float f5 = re * cscT * (psspy + pspx - cosT * s22);
+    const float f7 = ph.gs * sinT;
+    if (sinT < 0.1f) return f7;
+    return clamp_force(f2 + f5 + f4) + f7;
+}
+
+// fu at u_phi face (i, j) (computeforcevelphiKernel_viscous,
+// bubble.cu:1647-1816).
+__device__ __noinline__ float viscous_fu(const SbGrid& g, const SbPhys& ph, const SbFields& f,
+                                         int i, int j) {
+    const int nP = g.nP, mP = g.maskP, nT = g.nT;
+    const int jW = (j - 1) & mP, jO = (j + nP / 2) & mP, jWO = (jW + nP / 2) & mP;
+    const int r = i * nP;
+    const float* __restrict__ u = f.uph_adv;
+    const float* __restrict__ v = f.uth_adv;
+    const float* __restrict__ e = f.eta_adv;
+    const float ih = g.invh;
+    const float etaW = e[r + jW], etaE = e[r + j];
+    const float invEta = 2.0f / (etaW + etaE);
+    if (isinf(invEta)) return __int_as_float(0x7fffffff);
+    float v0, v1, v2, v3;
+    if (i != 0) {
+        v0 = v[r - nP + jW];
+        v1 = v[r - nP + j];
+    } else {
+        v0 = 0.5f * (v[jW] - v[jWO]);
+        v1 = 0.5f * (v[j] - v[jO]);
+    }
+    if (i != nT - 1) {
+        v2 = v[r + jW];
+        v3 = v[r + j];
+    } else {
+        v2 = 0.5f * (v[r - nP + jW] - v[r - nP + jWO]);
+        v3 = 0.5f * (v[r - nP + j] - v[r - nP + jO]);
+    }
+    const float divW = vel_div(g, f, i, jW), divE = vel_div(g, f, i, j);
+    const float div = 0.5f * (divW + divE);
+    const float pvpx = 0.5f * ih * (v1 + v3 - v0 - v2);
+    const float pvpyW = ih * (v2 - v0), pvpyE = ih * (v3 - v1);
+    const float pvpy = 0.5f * ih * (v2 + v3 - v0 - v1);
+    const float u1 = u[r + j];
+    float u3, u4, pupyN = 0.0f, pupyS = 0.0f;
+    if (i != 0) {
+        u3 = u[r - nP + j];
+        pupyN = ih * (u1 - u3);
+    } else {
+        u3 = -u[r + jO];
+    }
+    if (i != nT - 1) {
+        u4 = u[r + nP + j];
+        pupyS = ih * (u4 - u1);
+    } else {
+        u4 = -u[r + jO];
+    }
+    const float pupy = 0.5f * ih * (u4 - u3);
+    const float sinT = g.sin_c[i], cosT = g.cos_c[i];
+    const float cscT = 1.0f / sinT, cotT = cosT * cscT;
+    const float s12 = cscT * pvpx + pupy - u1 * cotT;
+    const float pDpx = ih * (etaE - etaW);
+    const float d0 = i != 0 ? e[r - nP + jW] : e[r + jWO];
+    const float d2 = i != 0 ? e[r - nP + j] : e[r + jO];
+    const float d1 = i != nT - 1 ? e[r + nP + jW] : e[r + jWO];
+    const float d3 = i != nT - 1 ? e[r + nP + j] : e[r + jO];
+    const float pDpy = 0.25f * ih * (d1 + d3 - d0 - d2);
+    float uN = 0.5f * (u3 + u1), uS = 0.5f * (u1 + u4);
+    if (i == 0) uN = 0.5f * (u1 - u3);
+    if (i == nT - 1) uS = 0.5f * (u1 - u4);
+    const float psspy = ih * (ih * (v0 + v3 - v1 - v2) + g.sin_e[i + 1] * pupyS -
+                              g.sin_e[i] * pupyN - g.cos_e[i + 1] * uS + g.cos_e[i] * uN);
+    const float s22W = 2.0f * (2.0f * divW - pvpyW), s22E = 2.0f * (2.0f * divE - pvpyE);
+    const float pspx = ih * (s22E - s22W);
+    const float re = ph.re;
+    const float f2 = re * invEta * pDpy * s12;
+    const float f4 = re * invEta * cscT * pDpx * 2.0f * (2.0f * div - pvpy);
+    const float f5 = re * cscT * (psspy + pspx + cosT * s12);
+    if (sinT < 0.1f) return 0.0f;
+    return clamp_force(f2 + f4 + f5);
+}
+
 // Implicit surfactant system (paper eq. 26), assembled for the increment
 // dx = gamma_new - gamma_adv so that FP32 keeps its precision:
 //   (A dx)_c = dmass_c dx_c + sum_n w_cn (dx_c - dx_n)
@@ -195,6 +339,7 @@ __device__ __forceinline__ bool is_broken(float gamma, float eta, float gmax) {
 // of its couplings moves into the neighbours' dmass, which keeps A
 // symmetric positive definite with the same solution as the reference's
 // identity row.
+template <bool VISC>
 __device__ __forceinline__ void assemble_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
     (void)ph;
@@ -269,9 +414,20 @@ __device__ __forceinline__ void assemble_cell(const SbGrid& g, const SbPhys& ph,
                              uAirW / (etaLeft / Cr * invDt + 1.0f) +
                              vAirS * sinS / (etaDown / Cr * invDt + 1.0f) -
                              vAirN * sinN / (etaUp / Cr * invDt + 1.0f));
-    sinThetaDiv += ph.gs * g.invh *
-                   (sinS * sinS * etaDown / (invDt * etaDown + Cr) -
-                    sinN * sinN * etaUp / (invDt * etaUp + Cr));
+    if (VISC) {
+        // bubble.cu:1460-1466: the viscous forces, gravity inside fv
+        const float fuW = viscous_fu(g, ph, f, i, j), fuE = viscous_fu(g, ph, f, i, jE);
+        const float fvN = i != 0 ? viscous_fv(g, ph, f, i - 1, j) : 0.0f;
+        const float fvS = i != nT - 1 ? viscous_fv(g, ph, f, i, j) : 0.0f;
+        sinThetaDiv += g.invh * (sinS * fvS * etaDown / (invDt * etaDown + Cr) -
+                                 sinN * fvN * etaUp / (invDt * etaUp + Cr) +
+                                 fuE * etaRight / (invDt * etaRight + Cr) -
+                                 fuW * etaLeft / (invDt * etaLeft + Cr));
+    } else {
+        sinThetaDiv += ph.gs * g.invh *
+                       (sinS * sinS * etaDown / (invDt * etaDown + Cr) -
+                        sinN * sinN * etaUp / (invDt * etaUp + Cr));
+    }
 
     // neighbour gamma (a broken neighbour holds gmax) and broken flags
     const float gEr = f.gam_adv[iE], gWr = f.gam_adv[iW];
@@ -320,7 +476,7 @@ __device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, floa
     return (ca ? gmax : xa) - (cb ? gmax : xb);
 }
 
-template <class T>
+template <class T, bool VISC>
 __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
     (void)cur;
@@ -365,8 +521,18 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
             const float cscT = 1.0f / g.sin_c[i];
             const float pGpx = g.invh * gnew_diff(f, idx, w, gmax) * cscT;
             const float f1 = -M * invEta * pGpx;
-            const float f2 = Cr * invEta * f.uair[idx];
-            f.uph[idx] = (u1 * invDt + f1 + f2) / (invDt + Cr * invEta);
+            if (VISC) {
+                // applyforcevelphiKernel_viscous (bubble.cu:1987-2038): the
+                // mirrored wind mix and fu
+                const float uAir = 0.5f * (f.uair[idx] * f.step->mixA +
+                                           f.uair[i * nP + (nP - j)] * f.step->mixB);
+                const float f6 = Cr * invEta * uAir;
+                f.uph[idx] = (u1 * invDt + f1 + f6 + viscous_fu(g, ph, f, i, j)) /
+                             (invDt + Cr * invEta);
+            } else {
+                const float f2 = Cr * invEta * f.uair[idx];
+                f.uph[idx] = (u1 * invDt + f1 + f2) / (invDt + Cr * invEta);
+            }
         }
     }
     // u_theta face between (i, j) and (i+1, j)
@@ -380,9 +546,18 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
         } else {
             const float pGpy = g.invh * gnew_diff(f, s, idx, gmax);
             const float f1 = -M * invEta * pGpy;
-            const float f2 = Cr * invEta * f.vair[idx];
-            const float f3v = ph.gs * g.sin_e[i + 1];
-            f.uth[idx] = (v1 * invDt + f1 + f2 + f3v) / (invDt + Cr * invEta);
+            if (VISC) {
+                // applyforcevelthetaKernel_viscous (bubble.cu:1940-1983)
+                const float vAir = 0.5f * (f.vair[idx] * f.step->mixA -
+                                           f.vair[i * nP + (nP - j)] * f.step->mixB);
+                const float f6 = Cr * invEta * vAir;
+                f.uth[idx] = (v1 * invDt + f1 + f6 + viscous_fv(g, ph, f, i, j)) /
+                             (invDt + Cr * invEta);
+            } else {
+                const float f2 = Cr * invEta * f.vair[idx];
+                const float f3v = ph.gs * g.sin_e[i + 1];
+                f.uth[idx] = (v1 * invDt + f1 + f2 + f3v) / (invDt + Cr * invEta);
+            }
         }
     }
 }
@@ -465,12 +640,12 @@ __device__ __forceinline__ const SbBubbleDesc& stage_tile_desc(SbBubbleDesc* con
 // Kernels whose cells touch the stored thickness / surfactant fields are
 // instantiated per storage type T (float or __nv_bfloat16); a plan launches
 // the instantiation of its bubbles' storage.
-#define SB_CELL_KERNEL_BODY(call)                                                      \
+#define SB_CELL_KERNEL_BODY(...)                                                       \
     __shared__ __align__(16) SbBubbleDesc s_d;                                         \
     const int2 t = tiles[blockIdx.x];                                                  \
     const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);                         \
     const int idx = t.y + threadIdx.x;                                                 \
-    if (idx < d.g.N) call(d.g, d.ph, d.f, d.cur, idx);
+    if (idx < d.g.N) __VA_ARGS__(d.g, d.ph, d.f, d.cur, idx);
 
 #define SB_CELL_KERNEL(name)                                                           \
     __global__ void __launch_bounds__(256) k_##name(SbBubbleDesc* const* __restrict__ descs, \
@@ -488,8 +663,19 @@ __device__ __forceinline__ const SbBubbleDesc& stage_tile_desc(SbBubbleDesc* con
 SB_CELL_KERNEL_T(advect_maps)
 SB_CELL_KERNEL(velocity)
 SB_CELL_KERNEL_T(bimocq)
-SB_CELL_KERNEL(assemble)
-SB_CELL_KERNEL_T(post)
+// k_assemble / k_post: the instantiations with VISC = true evaluate the
+// viscous forces (every bubble of a plan has the same switch).
+template <bool VISC>
+__global__ void __launch_bounds__(256) k_assemble(SbBubbleDesc* const* __restrict__ descs,
+                                                  const int2* __restrict__ tiles) {
+    SB_CELL_KERNEL_BODY(assemble_cell<VISC>)
+}
+
+template <class T, bool VISC>
+__global__ void __launch_bounds__(256) k_post(SbBubbleDesc* const* __restrict__ descs,
+                                              const int2* __restrict__ tiles) {
+    SB_CELL_KERNEL_BODY(post_cell<T, VISC>)
+}
 
 template <class T>
 __global__ void __launch_bounds__(256) k_accum(SbBubbleDesc* const* __restrict__ descs,
@@ -703,13 +889,21 @@ cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s) {
             if (bf) k_bimocq<__nv_bfloat16><<<n, block, 0, s>>>(d, t);
             else k_bimocq<float><<<n, block, 0, s>>>(d, t);
             break;
-        case STAGE_ASSEMBLE: k_assemble<<<n, block, 0, s>>>(d, t); break;
+        case STAGE_ASSEMBLE:
+            if (P.viscous) k_assemble<true><<<n, block, 0, s>>>(d, t);
+            else k_assemble<false><<<n, block, 0, s>>>(d, t);
+            break;
         case STAGE_SOLVE:
             return P.one ? launch_solve_one(P.one->g, P.one->f, P.set, P.solver, s)
                          : launch_solve(P.set, P.maxNP, P.solver, s);
         case STAGE_POST:
-            if (bf) k_post<__nv_bfloat16><<<n, block, 0, s>>>(d, t);
-            else k_post<float><<<n, block, 0, s>>>(d, t);
+            if (P.viscous) {
+                if (bf) k_post<__nv_bfloat16, true><<<n, block, 0, s>>>(d, t);
+                else k_post<float, true><<<n, block, 0, s>>>(d, t);
+            } else {
+                if (bf) k_post<__nv_bfloat16, false><<<n, block, 0, s>>>(d, t);
+                else k_post<float, false><<<n, block, 0, s>>>(d, t);
+            }
             break;
         case STAGE_ACCUM:
             if (bf) k_accum<__nv_bfloat16><<<n, block, 0, s>>>(d, t);

@@ -39,6 +39,8 @@ struct SbPhys {
     float base_eta, base_gam;  // BF16 storage: offsets of the eta and gamma fields (else 0)
     int plain_adv;    // 1: thickness advected like gamma, no characteristic maps (BIMOCQ off)
     int single_step;  // 1: velocity traced in one step (RUNGE_KUTTA off)
+    int viscous;      // 1: viscous stress forces in the system and the velocity update
+    float re;         // nu / (U r), the film's inverse Reynolds number
 };
 
 // Per-step diagnostics written by the kernels.

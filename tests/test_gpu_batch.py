@@ -164,3 +164,33 @@ def test_batch_rejects_mixed_solver_settings(gpulib):
             GpuBatch([a, b])
     finally:
         _close([a, b])
+
+
+def test_viscous_batch_matches_members_stepped_alone(gpulib):
+    from soapbubble_gb300.bubble import GpuBatch
+    a, b = _twins(SMALL[:3], viscous=1, radius=0.05, solver_tol=1e-6)
+    try:
+        with GpuBatch(a) as batch:
+            for t, dt in _schedule(10, 0.005):
+                batch.step(1, t, dt)
+                for g in b:
+                    g.step(1, t, dt)
+            batch.synchronize()
+        for ga, gb in zip(a, b):
+            for name in FIELDS:
+                np.testing.assert_array_equal(ga.download(name), gb.download(name),
+                                              err_msg=f"nT={ga.nTheta} {name}")
+    finally:
+        _close(a + b)
+
+
+def test_batch_rejects_mixed_viscous_switch(gpulib):
+    from soapbubble_gb300._lib import SoapBubbleError
+    from soapbubble_gb300.bubble import GpuBatch
+    a = _member(16, 1, viscous=0)
+    b = _member(16, 2, viscous=1)
+    try:
+        with pytest.raises(SoapBubbleError, match="viscous"):
+            GpuBatch([a, b])
+    finally:
+        _close([a, b])

@@ -223,3 +223,32 @@ def test_switch_variants_match_oracle(oracle, gpulib, sw):
             assert gb.stats().reinits == 0
     finally:
         gb.close()
+
+
+# The VISCOUS variant (viscous stress forces in the system and the velocity
+# update) against the oracle built with the same switch, at the reference's
+# config radius (0.05 m: re = 2.5e-3, most forces at their clamp) and at 1 m.
+@pytest.mark.parametrize("radius", [0.05, 1.0], ids=["r0.05", "r1"])
+def test_viscous_variant_matches_oracle(oracle, gpulib, radius):
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    nT, dt, seed = 64, 0.005, 4322
+    f = synth.make_fields("c0", nT, seed)
+    op = oracle.default_params(nT, radius=radius, dt_s=dt)
+    op.t = 0.5
+    op.viscous = 1
+    ob = oracle.OracleBubble(op, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    for _ in range(5):
+        ob.step()
+    gb = GpuBubble(make_params(nT, dt, radius=radius, solver_tol=1e-10, solver_max_iter=2000,
+                               viscous=1))
+    try:
+        P.sync_state(gb, ob)
+        for k in range(3):
+            gb.step(1, 0.5, dt)
+            ob.step()
+            err = P.compare(gb, ob, list(PHYS))
+            for name in PHYS:
+                assert err[name] <= TOL_FIELD, (k, name, err[name])
+    finally:
+        gb.close()

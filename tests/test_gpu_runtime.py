@@ -55,6 +55,47 @@ def test_frame_loop_writes_reference_frames(gpulib, tmp_path):
         assert gb.stats().steps == 12
 
 
+def _velocity_image(uth, uph):
+    """Solver::write_velocity_image (kernel/solver.cu:388-497) in numpy."""
+    uth, uph = uth.astype(np.float64), uph.astype(np.float64)
+    nT, nP = uph.shape
+    opp = (np.arange(nP) + nP // 2) % nP
+    u = 0.5 * (uph + np.roll(uph, -1, axis=1))
+    vN = np.vstack([0.75 * uth[:1] - 0.25 * uth[:1, opp], uth])
+    vS = np.vstack([uth, 0.75 * uth[-1:] - 0.25 * uth[-1:, opp]])
+    v = 0.5 * (vN + vS)
+    return (u / 2 + 0.5).astype(np.float32), (v / 2 + 0.5).astype(np.float32)
+
+
+def test_velocity_and_concentration_frames(gpulib, tmp_path):
+    """vel%04d.exr (R = u/2 + 0.5, G = v/2 + 0.5, B = 0.5) and con%04d.exr
+    ((gamma - 0.9) / 0.2 in all channels) beside the thickness frames when
+    the params ask for them (WRITE_VELOCITY_DATA, WRITE_CONCENTRATION_DATA)."""
+    from soapbubble_gb300.exr import read_exr
+    gb = _bubble(32, dt=0.005, DT=0.01, frames=3, write_velocity_frames=1,
+                 write_concentration_frames=1)
+    with gb:
+        gb.run(str(tmp_path) + "/", frames=3)
+        names = sorted(os.listdir(tmp_path))
+        assert names == sorted([f"{k}{i:04d}.exr" for k in ("frame", "vel", "con")
+                                for i in range(3)])
+        R, G = _velocity_image(gb.download("u_theta"), gb.download("u_phi"))
+        vel = read_exr(str(tmp_path / "vel0002.exr"))
+        np.testing.assert_array_equal(vel["R"], R.astype(np.float16).astype(np.float32))
+        np.testing.assert_array_equal(vel["G"], G.astype(np.float16).astype(np.float32))
+        assert np.all(vel["B"] == 0.5)
+        assert np.abs(vel["R"] - 0.5).max() > 1e-3  # the wind moved the film
+        con = read_exr(str(tmp_path / "con0002.exr"))
+        gam = gb.download("gamma").astype(np.float32).astype(np.float64)
+        expect = ((gam - 0.9) / 0.2).astype(np.float32).astype(np.float16).astype(np.float32)
+        for c in "BGR":
+            np.testing.assert_array_equal(con[c], expect)
+        # the writers also work on their own
+        gb.write_velocity_exr(str(tmp_path / "v.exr"))
+        gb.write_concentration_exr(str(tmp_path / "c.exr"))
+        np.testing.assert_array_equal(read_exr(str(tmp_path / "v.exr"))["G"], vel["G"])
+
+
 def test_stats_and_mass_bookkeeping(gpulib):
     gb = _bubble(64)
     with gb:

@@ -226,3 +226,73 @@ def test_forced_reinit_resets_maps(oracle):
     np.testing.assert_array_equal(b.a["eta_init"], b.a["eta"])
     assert np.all(b.a["eta_delta"] == 0)
     assert b.stats.reinit == 1
+
+
+# VISCOUS variant (include/header.cuh:98): the viscous stress forces vanish
+# for a rigid rotation and for a fluid at rest (leaving gravity inside fv),
+# and with no flow and no wind the variant's step equals the default step.
+
+def _viscous_params(oracle, radius=0.05):
+    p = oracle.default_params(nT, radius=radius, dt_s=0.005)
+    p.viscous = 1
+    return p
+
+
+def test_viscous_forces_vanish_for_rigid_rotation(oracle):
+    p = _viscous_params(oracle)
+    assert p.re == pytest.approx(1.25e-4 / 0.05)
+    h = np.pi / nT
+    theta_c = (np.arange(nT) + 0.5) * h
+    uph = np.repeat((0.7 * np.sin(theta_c))[:, None], nP, 1)  # u_phi = Omega sin(theta)
+    uth = np.zeros((nT - 1, nP))
+    eta = rng(5).uniform(0.5, 1.0, (nT, nP))
+    div, fv, fu = oracle.viscous_forces(p, uth, uph, eta)
+    assert np.all(div == 0.0)
+    # the stress sigma12 = u_theta_phi / sin + u_phi_theta - u_phi cot vanishes up
+    # to the O(h^2) truncation of the centred differences
+    assert np.max(np.abs(fu)) < 10 * p.re * h * h
+    grav = p.gs * np.sin(np.arange(1, nT) * h)[:, None]
+    sin_f = np.sin(np.arange(1, nT) * h)[:, None] * np.ones((1, nP))
+    far = sin_f >= 0.1
+    assert np.max(np.abs(fv - grav)[far]) < 10 * p.re * h * h
+    np.testing.assert_array_equal(fv[~far], np.broadcast_to(grav, fv.shape)[~far])
+
+
+def test_viscous_forces_at_rest_are_gravity(oracle):
+    p = _viscous_params(oracle)
+    h = np.pi / nT
+    z = np.zeros((nT, nP))
+    div, fv, fu = oracle.viscous_forces(p, np.zeros((nT - 1, nP)), z, rng(6).uniform(0.5, 1, (nT, nP)))
+    assert not div.any() and not fu.any()
+    np.testing.assert_allclose(fv, np.broadcast_to(p.gs * np.sin(np.arange(1, nT) * h)[:, None],
+                                                   fv.shape), rtol=0, atol=1e-15)
+
+
+def test_viscous_forces_are_clamped(oracle):
+    p = _viscous_params(oracle)
+    r = rng(7)
+    div, fv, fu = oracle.viscous_forces(p, 0.5 * r.standard_normal((nT - 1, nP)),
+                                        0.5 * r.standard_normal((nT, nP)), r.uniform(0.5, 1, (nT, nP)))
+    h = np.pi / nT
+    assert np.max(np.abs(fu)) <= 0.1 and np.max(np.abs(fu)) == pytest.approx(0.1)
+    grav = p.gs * np.sin(np.arange(1, nT) * h)[:, None]
+    assert np.max(np.abs(fv - grav)) <= 0.1 + 1e-15
+    # the rows within sin(theta) < 0.1 of the poles carry no viscous force
+    sin_c = np.sin((np.arange(nT) + 0.5) * h)
+    assert not fu[sin_c < 0.1].any()
+
+
+def test_viscous_step_at_rest_equals_default_step(oracle):
+    from soapbubble_gb300 import synth
+    f = synth.make_fields("c0", nT, 3)
+    z, zv = np.zeros((nT, nP)), np.zeros((nT - 1, nP))
+    out = []
+    for visc in (0, 1):
+        p = _viscous_params(oracle)
+        p.viscous, p.t = visc, 0.0  # corridor factor 3 - |t - 3| = 0: no wind
+        b = oracle.OracleBubble(p, f.eta, f.gamma, zv, z, z, zv)
+        b.step()
+        out.append({k: b.a[k].copy() for k in ("eta", "gamma", "uth", "uph")})
+    assert np.max(np.abs(out[1]["uth"])) > 1e-3  # gravity moved the film
+    for k in out[0]:
+        np.testing.assert_allclose(out[1][k], out[0][k], rtol=0, atol=1e-12, err_msg=k)
