@@ -374,6 +374,19 @@ def run_ours(args):
             from soapbubble_gb300 import storage as stor
             storage = stor.compare(steps=args.storage_steps, device=local, peak_gbs=peak)
 
+    ensemble_sharded = None
+    if world > 1 and args.ensemble_steps > 0:
+        # the ensemble's bubbles partitioned over the ranks (no data exchange)
+        from soapbubble_gb300 import shard
+        from soapbubble_gb300 import synth as syn
+        r = shard.run_ensemble_shard(syn.ensemble(0), args.ensemble_steps, syn.ENSEMBLE["dt"],
+                                     shard.Ranks(), device=local)
+        ensemble_sharded = {
+            "value": r["value"], "unit": UNIT, "ranks": world, "steps": args.ensemble_steps,
+            "seconds_max": r["seconds_max"], "cells_x_steps": r["units"],
+            "scaling": "strong (the 64-bubble ensemble split by cells over the ranks)",
+            "path": "per rank: its members as one batched set, CUDA graph per step"}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -402,6 +415,7 @@ def run_ours(args):
             "ensemble": ensemble,
             "serving": serving,
             "storage_c2": storage,
+            "ensemble_sharded": ensemble_sharded,
         }
         print(json.dumps(line), flush=True)
     if gb is not None:
