@@ -12,12 +12,22 @@ import pytest
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 
 
+def switches(meta):
+    """radius and the plain_advection / single_step_velocity / viscous
+    switches of a fixture (fixtures without them: radius 1, all off)."""
+    if len(meta) < 11:
+        return 1.0, 0, 0, 0
+    return float(meta[7]), int(meta[8]), int(meta[9]), int(meta[10])
+
+
 def load_case(oracle, path):
     z = np.load(path)
     nT, dt, t, strict, force = z["meta"][:5]
+    radius, plain, single, viscous = switches(z["meta"])
     nT = int(nT)
-    p = oracle.default_params(nT, dt_s=float(dt))
+    p = oracle.default_params(nT, radius=radius, dt_s=float(dt))
     p.t, p.strict, p.force_reinit, p.nthreads = float(t), int(strict), int(force), 1
+    p.plain_advection, p.single_step_velocity, p.viscous = plain, single, viscous
     a = {k[3:]: z[k].astype(np.float64) for k in z.files if k.startswith("in_")}
     ob = oracle.OracleBubble(p, a["eta"], a["gamma"], a["uth"], a["uph"], a["uair_init"],
                              a["vair_init"])

@@ -157,9 +157,13 @@ def test_step_matches_golden(gpulib, path):
     from soapbubble_gb300.bubble import GpuBubble, make_params
     z = np.load(path)
     nT, dt, t, strict, force = z["meta"][:5]
+    meta = z["meta"]
+    radius, plain, single, visc = ((float(meta[7]), int(meta[8]), int(meta[9]), int(meta[10]))
+                                   if len(meta) >= 11 else (1.0, 0, 0, 0))
     nT = int(nT)
-    gb = GpuBubble(make_params(nT, float(dt), solver_tol=1e-10, solver_max_iter=2000,
-                               force_reinit={-1: 0, 0: 1, 1: 2}[int(force)]))
+    gb = GpuBubble(make_params(nT, float(dt), radius=radius, solver_tol=1e-10, solver_max_iter=2000,
+                               force_reinit={-1: 0, 0: 1, 1: 2}[int(force)], plain_advection=plain,
+                               single_step_velocity=single, viscous=visc))
     with gb:
         for gname, oname in P.FIELD_MAP.items():
             gb.upload(gname, z["in_" + oname].astype(np.float64))
