@@ -56,16 +56,18 @@ ALG_BYTES_PER_CELL = {
     "k_reinit": 0,        # no traffic unless re-initialising (about 1 step in 10)
 }
 # The implicit solve, per cell.  Fixed: set-up (r0, rhs, dmass, cE, cS ->
-# x (float-float), r, q, z1 = 40), the first Neumann phase (16), the final
-# true-residual check (x, r0, dmass, cE, cS -> r = 28) and the result
-# (x, gamma_adv -> dx, gamma = 20).  Per CG iteration: Neumann phase (z1, cS,
-# r -> z = 16), q = A p (z, p, dmass, cE, cS -> p, q = 28), update and
-# preconditioner (p, r, q, x -> x, r, z1 = 36).
-PCG_BYTES_FIXED, PCG_BYTES_PER_ITER = 104, 80
+# x (float-float), r, q, z or z1 = 40), the final true-residual check (x, r0,
+# dmass, cE, cS -> r = 28) and the result (x, gamma_adv -> dx, gamma = 20).
+# Per CG iteration: q = A p (z, p, dmass, cE, cS -> p, q = 28) and the update
+# with the line solve (p, r, q, x -> x, r, z or z1 = 36).  With the Neumann
+# term, one more phase per iteration and one at the start (z1, cS, r -> z =
+# 16).  Keyed by the preconditioner a solve used (1: line, 2: Neumann).
+PCG_BYTES = {1: (88, 64), 2: (104, 80)}
 ROOFLINE_NOTES = {
     "k_solve": "latency-bound, not HBM-bound: the solve's vectors and factors stay in L2 and in "
                "shared memory across its iterations (DRAM traffic per launch is their first touch "
-               "and does not grow with the iteration count); three grid barriers per CG iteration",
+               "and does not grow with the iteration count); two grid barriers per CG iteration with the "
+               "line blocks alone, three with the Neumann term",
 }
 
 
@@ -180,7 +182,9 @@ def workload_config(extra=None):
          "nTheta": NTHETA, "nPhi": 2 * NTHETA, "cells": NTHETA * 2 * NTHETA, "dt": DT,
          "steps_per_frame": STEPS_PER_FRAME,
          "solver": "mixed-precision PCG (float-float iterate and scalars, exact dot-product sums, "
-                   "float-float true-residual refinement), phi-line preconditioner",
+                   "float-float true-residual refinement); preconditioner: exact phi-line blocks, "
+                   "plus their two-term Neumann series when the previous solve needed many "
+                   "iterations",
          "solver_tol": 1e-6, "seed": SEED,
          "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); "
                f"state {state_mb():.0f} MB per bubble"}
@@ -284,7 +288,7 @@ def run_ours(args):
     # are the live input of the roofline
     kr = args.steps
     stage_ms = np.zeros(nst)
-    iters = []
+    iters, solve_bytes = [], []
     tw = GpuBubble(make_params(NTHETA, DT, solver_tol=1e-6, solver_mode=0, device=local))
     tw.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
     for k in range(args.warmup):
@@ -292,7 +296,10 @@ def run_ours(args):
     tstream = tw.stream()
     for k in range(kr):
         tw.step_timed(1, t_of(k0 + k), DT, stage_ms)
-        iters.append(tw.stats().solver_iters)
+        st_k = tw.stats()
+        iters.append(st_k.solver_iters)
+        fixed, per_it = PCG_BYTES[st_k.solver_precond_used]
+        solve_bytes.append(fixed + per_it * st_k.solver_iters)
         flush.memset_async(k & 0xff, tstream)
     tw.synchronize()
     tw.close()
@@ -300,7 +307,7 @@ def run_ours(args):
     dom = names[k_dom]
     mean_iters = float(np.mean(iters)) if iters else 0.0
     alg = dict(ALG_BYTES_PER_CELL)
-    alg["k_solve"] = PCG_BYTES_FIXED + PCG_BYTES_PER_ITER * mean_iters
+    alg["k_solve"] = float(np.mean(solve_bytes)) if solve_bytes else 0.0
     per_launch_bytes = alg[dom] * N
     avg_launch_s = stage_ms[k_dom] / 1e3 / kr
     achieved = per_launch_bytes / avg_launch_s / 1e9
@@ -411,6 +418,7 @@ def run_ours(args):
             "stage_share": stage_share, "stage_us_per_step": stage_us,
             "stage_steps": kr, "step_path": "CUDA graph per step (value); kernel-by-kernel with events (stages)",
             "solver_iters_mean": mean_iters, "solver_rel_resid_last": st.solver_rel_resid,
+            "solver_alg_bytes_per_cell": alg["k_solve"],
             "reinits": int(final.reinits), "result_finite": finite,
             "ensemble": ensemble,
             "serving": serving,

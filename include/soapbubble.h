@@ -83,6 +83,9 @@ typedef struct {
                                        kernel/bubble.cu:2646-2648, 2689-2691) */
     int write_concentration_frames; /* sb_run also writes con%04d.exr (WRITE_CONCENTRATION_DATA,
                                        kernel/bubble.cu:2649-2651, 2692-2694) */
+    int solver_precond;       /* preconditioner of the implicit solve: 0 chooses per solve
+                                 from the previous solve's iterations, 1 the exact phi-line
+                                 blocks B alone, 2 B^-1 + B^-1 C B^-1 (C: the theta couplings) */
 } sb_params;
 
 enum { SB_STORE_FP32 = 0, SB_STORE_BF16 = 1 };
@@ -101,6 +104,8 @@ typedef struct {
     double mass_eta;          /* sum eta sin(theta) (after sb_update_mass) */
     double mass_gamma;        /* sum gamma sin(theta) */
     long long launches;       /* CUDA kernels launched by this handle */
+    int solver_precond_used;  /* preconditioner of the last solve: 1 phi-line blocks,
+                                 2 with the Neumann term */
 } sb_stats;
 
 typedef struct sb_bubble sb_bubble;

@@ -33,6 +33,7 @@ class SbParams(C.Structure):
         ("nu_scale", C.c_double), ("storage", C.c_int), ("plain_advection", C.c_int),
         ("single_step_velocity", C.c_int), ("viscous", C.c_int),
         ("write_velocity_frames", C.c_int), ("write_concentration_frames", C.c_int),
+        ("solver_precond", C.c_int),
     ]
 
 
@@ -42,6 +43,7 @@ class SbStats(C.Structure):
         ("solver_rel_resid", C.c_double), ("solver_converged", C.c_int),
         ("broken_cells", C.c_int), ("steps", C.c_longlong), ("reinits", C.c_longlong),
         ("mass_eta", C.c_double), ("mass_gamma", C.c_double), ("launches", C.c_longlong),
+        ("solver_precond_used", C.c_int),
     ]
 
 

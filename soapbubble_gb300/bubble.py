@@ -35,7 +35,8 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
                 gs_scale: float = 0.0, M_scale: float = 0.0, nu_scale: float = 0.0,
                 device: int = 0, storage: int = 0, plain_advection: int = 0,
                 single_step_velocity: int = 0, viscous: int = 0,
-                write_velocity_frames: int = 0, write_concentration_frames: int = 0) -> SbParams:
+                write_velocity_frames: int = 0, write_concentration_frames: int = 0,
+                solver_precond: int = 0) -> SbParams:
     p = default_params()
     p.nTheta, p.dt, p.radius, p.H, p.Gamma_m, p.T = nTheta, dt, radius, H, Gamma_m, T
     p.blendCoeff = blendCoeff
@@ -50,6 +51,7 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
     p.viscous = viscous                            # 1: VISCOUS on
     p.write_velocity_frames = write_velocity_frames
     p.write_concentration_frames = write_concentration_frames
+    p.solver_precond = solver_precond  # 0 auto, 1 phi-line blocks, 2 with the Neumann term
     return p
 
 

@@ -205,6 +205,8 @@ int validate(const sb_params* p) {
     if (!(p->dt > 0)) return fail(SB_ERR_INVALID, "timePerStep must be positive");
     if (p->storage != SB_STORE_FP32 && p->storage != SB_STORE_BF16)
         return fail(SB_ERR_INVALID, "storage must be SB_STORE_FP32 or SB_STORE_BF16");
+    if (p->solver_precond < 0 || p->solver_precond > 2)
+        return fail(SB_ERR_INVALID, "solver_precond must be 0 (auto), 1 or 2");
     return SB_OK;
 }
 
@@ -421,7 +423,8 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     b->solver.mode = p->solver_mode == 1 ? 0 : 1;
     b->solver.tol = p->solver_tol > 0 ? p->solver_tol : 1e-6;
     b->solver.max_iter = p->solver_max_iter > 0 ? p->solver_max_iter : 1000;
-    b->solver.precond = 1;
+    b->solver.precond = p->solver_precond == 1 ? kPrecLine
+                        : p->solver_precond == 2 ? kPrecNeumann : kPrecAuto;
     b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
     b->storage = p->storage;
     b->ph.plain_adv = p->plain_advection ? 1 : 0;
@@ -948,6 +951,7 @@ int sb_get_stats(sb_bubble* b, sb_stats* out) {
     out->launches = b->launches;
     out->mass_eta = st.mass_eta;
     out->mass_gamma = st.mass_gamma;
+    out->solver_precond_used = st.solver_neumann ? 2 : 1;
     if (st.wait_faults)
         return fail(SB_ERR_CUDA, "a bounded wait for a shared-memory copy in the implicit solve gave up");
     return SB_OK;

@@ -86,11 +86,16 @@ struct SbBubbleDesc {
     int pad;
 };
 
+// Preconditioner of the implicit solve: the exact phi-line blocks B alone,
+// with the Neumann term B^-1 C B^-1 added (C: the theta couplings), or
+// chosen per solve from the previous solve's iteration count.
+enum { kPrecLine = 1, kPrecNeumann = 2, kPrecAuto = 3 };
+
 struct SolverConfig {
     int mode;       // 0: plain FP32, 1: mixed precision (FP64 dots + refinement)
     int max_iter;
     double tol;     // relative residual ||b - A x|| / ||b||
-    int precond;    // 0: Jacobi, 1: exact phi-line (periodic tridiagonal per row)
+    int precond;    // kPrecLine, kPrecNeumann or kPrecAuto (sb_solver.cu)
     int blob;       // bytes of a block's shared-memory factor blob (set at launch)
     float tol2f;    // target r.r / |b|^2 of the iterate (set at launch)
 };
@@ -130,6 +135,8 @@ struct SbSolveRec {
     int fresh;  // the next r.z starts a new search direction
     int it;
     int conv;
+    int neu;    // 1: the preconditioner adds the Neumann term (chosen at set-up)
+    int pad;
 };
 
 // Words of a system's exact dot-product accumulators: three buffers (used

@@ -66,13 +66,47 @@ constexpr int kRowChunk = 16;         // rows a block counts at a time (sets)
 //   K_UPDATE   x += alpha p, r -= alpha q, z1 = B^-1 r
 //   K_CHECK    r = r0 - A x of the float-float iterate (mixed mode); |r|^2
 //   K_RESTART  z1 = B^-1 r from the refined iterate's residual
-enum { K_SETUP = 0, K_NEUMANN = 1, K_Q = 2, K_UPDATE = 3, K_CHECK = 4, K_RESTART = 5 };
+// and, with the line preconditioner alone (z = B^-1 r, no Neumann phase):
+//   K_SETUP_L    as K_SETUP with z = B^-1 r; r.z, r.r, |b|^2
+//   K_UPDATE_L   x += alpha p, r -= alpha q, z = B^-1 r; r.z, r.r
+//   K_RESTART_L  z = B^-1 r from the refined iterate's residual; r.z, r.r
+enum {
+    K_SETUP = 0, K_NEUMANN = 1, K_Q = 2, K_UPDATE = 3, K_CHECK = 4, K_RESTART = 5,
+    K_SETUP_L = 6, K_UPDATE_L = 7, K_RESTART_L = 8
+};
 
 // Dot-product values a phase kind produces (bit v: accumulator value v):
-// the set-up |b|^2 (value 2), the Neumann phase r.z and r.r (0, 1), q = A p
-// and the refinement check one value each.
+// r.z (0), r.r (1) and the set-up |b|^2 (2); q = A p and the refinement
+// check one value each.
 __host__ __device__ inline int kind_values(int kind) {
-    return kind == K_SETUP ? 4 : kind == K_NEUMANN ? 3 : (kind == K_Q || kind == K_CHECK) ? 1 : 0;
+    switch (kind) {
+        case K_SETUP: return 4;
+        case K_SETUP_L: return 7;
+        case K_NEUMANN: case K_UPDATE_L: case K_RESTART_L: return 3;
+        case K_Q: case K_CHECK: return 1;
+        default: return 0;
+    }
+}
+
+// The line preconditioner alone costs two phases per CG iteration, with the
+// Neumann term three (and one more at the start); the term pays where it
+// removes more than about a third of the iterations, which happens where the
+// theta couplings are strong (thin or ruptured films: c1 late in the run,
+// 44 -> 24 iterations) and shows as many iterations, and not on smooth thick
+// films (c1 early, c2: 2 iterations either way).  Auto mode turns the term
+// on after a solve that needed kNeumannOn or more iterations with the line
+// preconditioner alone (break-even near 6) and off after one that needed at
+// most kNeumannOff with it.
+constexpr int kNeumannOn = 7;
+constexpr int kNeumannOff = 2;
+
+__device__ __forceinline__ int first_kind(const SbDevStats* st, const SolverConfig& cfg) {
+    bool neu;
+    if (cfg.precond == kPrecNeumann) neu = true;
+    else if (cfg.precond == kPrecLine) neu = false;
+    else if (st->solver_neumann) neu = st->solver_iters > kNeumannOff;
+    else neu = st->solver_iters >= kNeumannOn;
+    return neu ? K_SETUP : K_SETUP_L;
 }
 
 // ---------------------------------------------------------------------------
@@ -790,6 +824,7 @@ __device__ __forceinline__ SbSolveRec load_rec(const SbSolveRec* p) {
     r.fresh = __ldcg(&p->fresh);
     r.it = __ldcg(&p->it);
     r.conv = __ldcg(&p->conv);
+    r.neu = __ldcg(&p->neu);
     return r;
 }
 
@@ -800,6 +835,7 @@ __device__ __forceinline__ void write_stats(SbDevStats* st, const SbSolveRec& rc
     st->solver_rel_resid = sqrt(ff_to_d(to_ff(rc.rr)) / bb);
     st->solver_b_norm = sqrt(bb);
     st->solver_converged = rc.conv;
+    st->solver_neumann = rc.neu;
 }
 
 // The loop head of CG after r.z and r.r are known: iteration limit, NaN,
@@ -820,6 +856,22 @@ __device__ __forceinline__ bool loop_head(SbSolveRec& rc, const SolverConfig& cf
     return false;
 }
 
+// After a phase that formed r.z (A) and r.r (B): the next search direction's
+// beta (none after a start or restart), then the loop head.
+template <bool MIXED>
+__device__ __forceinline__ bool after_rz(SbSolveRec& rc, ff A, ff B, const SolverConfig& cfg) {
+    if (rc.fresh) {
+        rc.beta = 0.0f;  // a new search direction (start or restart)
+        rc.fresh = 0;
+    } else {
+        rc.beta = ff_to_f(ff_div(A, to_ff(rc.rz)));
+        ++rc.it;
+    }
+    rc.rz = to_f2(A);
+    rc.rr = to_f2(B);
+    return loop_head<MIXED>(rc, cfg);
+}
+
 // Advances a system's scalars past a phase of kind rc.kind with its exact
 // sums (A, B, C: the values kind_values names) and sets the next kind;
 // returns true when the system is finished.  Every path that advances a
@@ -829,7 +881,8 @@ template <bool MIXED>
 __device__ __forceinline__ bool transition(SbSolveRec& rc, ff A, ff B, ff C,
                                            const SolverConfig& cfg) {
     switch (rc.kind) {
-        case K_SETUP: {
+        case K_SETUP:
+        case K_SETUP_L: {
             const ff bb = C.hi > 0.0f ? C : ff{1.0f, 0.0f};
             rc.bb = to_f2(bb);
             // tol2f = tol^2 (plain) or (0.8 tol)^2 (mixed: the float-float
@@ -841,24 +894,23 @@ __device__ __forceinline__ bool transition(SbSolveRec& rc, ff A, ff B, ff C,
             rc.it = 0;
             rc.conv = 0;
             rc.fresh = 1;
-            rc.kind = K_NEUMANN;
-            return false;
-        }
-        case K_NEUMANN:
-            if (rc.fresh) {
-                rc.beta = 0.0f;  // a new search direction (start or restart)
-                rc.fresh = 0;
-            } else {
-                rc.beta = ff_to_f(ff_div(A, to_ff(rc.rz)));
-                ++rc.it;
+            rc.neu = rc.kind == K_SETUP ? 1 : 0;
+            if (rc.neu) {
+                rc.kind = K_NEUMANN;
+                return false;
             }
-            rc.rz = to_f2(A);
-            rc.rr = to_f2(B);
-            return loop_head<MIXED>(rc, cfg);
+            return after_rz<MIXED>(rc, A, B, cfg);  // the set-up formed z = B^-1 r
+        }
+        case K_RESTART_L:
+            rc.fresh = 1;
+            return after_rz<MIXED>(rc, A, B, cfg);
+        case K_NEUMANN:
+        case K_UPDATE_L:
+            return after_rz<MIXED>(rc, A, B, cfg);
         case K_Q:
             if (!(A.hi > 0.0f)) return true;  // breakdown: keep the current iterate
             rc.alpha = to_f2(ff_div(to_ff(rc.rz), A));
-            rc.kind = K_UPDATE;
+            rc.kind = rc.neu ? K_UPDATE : K_UPDATE_L;
             return false;
         case K_UPDATE:
             rc.kind = K_NEUMANN;
@@ -869,7 +921,7 @@ __device__ __forceinline__ bool transition(SbSolveRec& rc, ff A, ff B, ff C,
                 rc.conv = 1;
                 return true;
             }
-            rc.kind = K_RESTART;
+            rc.kind = rc.neu ? K_RESTART : K_RESTART_L;
             return false;
         default:  // K_RESTART
             rc.fresh = 1;
@@ -906,7 +958,7 @@ template <bool MIXED>
 __device__ __forceinline__ void advance(const SbSolveSet& S, int b, int p, const ff* sums,
                                         const SolverConfig& cfg) {
     SbSolveRec rc = load_rec(S.rec + (p & 1) * S.nb + b);
-    if (p == 0) rc.kind = K_SETUP;
+    if (p == 0) rc.kind = first_kind(S.descs[b]->f.stats, cfg);
     if (transition<MIXED>(rc, sums[0], sums[1], sums[2], cfg)) {
         write_stats(S.descs[b]->f.stats, rc);
         S.done_at[b] = p + 1;
@@ -995,6 +1047,25 @@ __device__ __forceinline__ void store_z1(const SbGrid& g, const SbFields& f, int
     }
 }
 
+// Stores the preconditioner's result D as this thread's columns of row i
+// of z and adds the columns' r.z and r.r terms (column order).
+template <bool MIXED, int PER>
+__device__ __forceinline__ void store_z_dots(const SbGrid& g, const SbFields& f, int i,
+                                             const Stage& St, const float (&rv)[PER], ff& a,
+                                             ff& b2) {
+    const int row = i * g.nP;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int j = col_of(k);
+        if (j < g.nP) {
+            const float z = St.work[j];
+            f.z[row + j] = z;
+            a = acc<MIXED>(a, rv[k], z);
+            b2 = acc<MIXED>(b2, rv[k], rv[k]);
+        }
+    }
+}
+
 // w = C z1 on row i: the theta couplings (weights cS of the faces north and
 // south of each cell) applied to the neighbouring rows of z1; z1 and r of
 // the row itself are returned in zo and ro (loaded with the rest, before
@@ -1045,9 +1116,9 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
     float rv[PER];
     switch (kind) {
         case K_SETUP:
+        case K_SETUP_L:
             row_init<MIXED, PER>(g, f, i, rv, c2);
             precondition_row<PER, true>(g, f, i, St, rv);
-            store_z1<PER>(g, f, i, St);
             break;
         case K_NEUMANN: {
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
@@ -1073,22 +1144,25 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
             a = row_spmv<MIXED, PER>(g, f, i, beta, pB, pA);
             break;
         case K_UPDATE:
+        case K_UPDATE_L:
             // the row's factors travel while the update runs
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
             row_update<MIXED, PER>(g, f, i, alpha, pA, rv);
             precondition_row<PER, false>(g, f, i, St, rv);
-            store_z1<PER>(g, f, i, St);
             break;
         case K_CHECK:
             if (MIXED) a = row_true_residual<PER>(g, f, i);
             break;
-        default:  // K_RESTART
+        default:  // K_RESTART, K_RESTART_L
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
             row_load_r<PER>(g, f, i, rv);
             precondition_row<PER, false>(g, f, i, St, rv);
-            store_z1<PER>(g, f, i, St);
             break;
     }
+    // the line-preconditioner kinds (_L, the last three) store z = B^-1 r and
+    // its dot products where the Neumann kinds store z1 = B^-1 r
+    if (kind >= K_SETUP_L) store_z_dots<MIXED, PER>(g, f, i, St, rv, a, b2);
+    else if (kind == K_SETUP || kind == K_UPDATE || kind == K_RESTART) store_z1<PER>(g, f, i, St);
     // this thread's shares of the values the kind produces, for reduce_row
     // (after D: the other threads may still read their D entries)
     const int vals = kind_values(kind);
@@ -1143,7 +1217,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             // grid reads the same record), staged with the descriptor
             if (threadIdx.x == 0) {
                 SbSolveRec rc;
-                rc.kind = K_SETUP;
+                rc.kind = p == 0 ? first_kind(S.descs[b]->f.stats, cfg) : K_SETUP;
                 rc.it = 0;
                 rc.beta = 0.0f;
                 rc.alpha = make_float2(0.0f, 0.0f);
@@ -1223,7 +1297,7 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     __shared__ int s_done;
     __shared__ unsigned long long s_w[kAccBuf];
     __shared__ ff s_sums[3];
-    if (threadIdx.x == 0) s_rc.kind = K_SETUP;
+    if (threadIdx.x == 0) s_rc.kind = first_kind(f.stats, cfg);
     Stage St;
     stage_init(St, &bar, sm, cfg.blob);  // (its barrier publishes s_rc.kind)
     const int G = gridDim.x, nT = g.nT;

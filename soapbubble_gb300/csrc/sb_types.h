@@ -57,7 +57,7 @@ struct SbDevStats {
     double mass_gamma;
     long long reinit_total;        // re-initialisations since creation
     int wait_faults;               // bounded waits that gave up (copy never landed)
-    int pad;
+    int solver_neumann;            // 1: the last solve used the Neumann term
 };
 
 }  // namespace sb

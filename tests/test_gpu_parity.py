@@ -256,3 +256,46 @@ def test_viscous_variant_matches_oracle(oracle, gpulib, radius):
                 assert err[name] <= TOL_FIELD, (k, name, err[name])
     finally:
         gb.close()
+
+
+# The preconditioner settings of the implicit solve (the phi-line blocks
+# alone, with the Neumann term, chosen per solve) reach the same solution.
+@pytest.mark.parametrize("precond", [0, 1, 2], ids=["auto", "line", "neumann"])
+def test_preconditioner_settings_match_oracle(oracle, gpulib, precond):
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    nT, dt, seed = 64, 0.005, 4323
+    f = synth.make_fields("c0", nT, seed)
+    op = oracle.default_params(nT, dt_s=dt)
+    op.t = 0.5
+    ob = oracle.OracleBubble(op, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    for _ in range(5):
+        ob.step()
+    gb = GpuBubble(make_params(nT, dt, solver_tol=1e-10, solver_max_iter=2000,
+                               solver_precond=precond))
+    try:
+        P.sync_state(gb, ob)
+        used = []
+        for k in range(3):
+            prev = gb.stats()
+            gb.step(1, 0.5, dt)
+            ob.step()
+            st = gb.stats()
+            assert st.solver_converged == 1
+            used.append(st.solver_precond_used)
+            if precond == 0 and k > 0:
+                # the term comes on after a solve of 7 or more iterations
+                # without it and goes off after one of 2 or fewer with it
+                if prev.solver_precond_used == 1:
+                    assert used[-1] == (2 if prev.solver_iters >= 7 else 1)
+                else:
+                    assert used[-1] == (1 if prev.solver_iters <= 2 else 2)
+            err = P.compare(gb, ob, list(PHYS))
+            for name in PHYS:
+                assert err[name] <= TOL_FIELD, (k, name, err[name])
+        if precond:
+            assert used == [precond] * 3
+        else:
+            assert used[0] == 1  # a new bubble starts with the line blocks alone
+    finally:
+        gb.close()
