@@ -325,11 +325,18 @@ def run_ours(args):
 
     # end to end through the C ABI with pinned host buffers: a second twin
     # steps the same timed steps (same trajectory, same work per step), each
-    # step uploading its wind forcing and reading the thickness back
+    # step uploading its wind forcing and copying the thickness back, which
+    # the host reads.  The copies go through the C ABI's staged I/O (the
+    # handle's copy stream), so step k+1's forcing and step k-1's thickness
+    # move while step k computes; the host reads step k-1's thickness (two
+    # host buffers) while step k runs.  The L2 flush between steps stays in
+    # the compute stream and its device time (CUDA events) is taken out of
+    # the host-clock total.
     e2e_steps = args.steps
     h_u = cudart.PinnedArray((N,))
     h_v = cudart.PinnedArray((Nv,))
-    h_eta = cudart.PinnedArray((N,))
+    h_etas = [cudart.PinnedArray((N,)), cudart.PinnedArray((N,))]
+    h_eta = h_etas[0]
     h_u.array[:] = f.uair_init.ravel().astype(np.float32)
     h_v.array[:] = f.vair_init.ravel().astype(np.float32)
     te = GpuBubble(make_params(NTHETA, DT, solver_tol=1e-6, solver_mode=0, device=local))
@@ -339,17 +346,29 @@ def run_ours(args):
     estream = te.stream()
     barrier(dist)
     te.synchronize()
-    e2e_s = 0.0
+    fl_ev = [(cudart.Event(), cudart.Event()) for _ in range(e2e_steps)]
+    readback = 0.0
+    t0 = time.perf_counter()
+    te.stage_upload_f32("uair_init", h_u.array)
+    te.stage_upload_f32("vair_init", h_v.array)
     for k in range(e2e_steps):
-        t0 = time.perf_counter()
-        te.upload_f32("uair_init", h_u.array)
-        te.upload_f32("vair_init", h_v.array)
-        te.step(1, t_of(k0 + k), DT)
-        te.download_f32("eta", h_eta.array)
-        te.synchronize()
-        e2e_s += time.perf_counter() - t0
+        te.step(1, t_of(k0 + k), DT)  # takes the staged forcing of step k
+        if k + 1 < e2e_steps:
+            te.stage_upload_f32("uair_init", h_u.array)
+            te.stage_upload_f32("vair_init", h_v.array)
+        te.wait_staged()  # step k-1's thickness (and step k+1's forcing) landed
+        if k > 0:  # the host reads step k-1's thickness while step k runs
+            readback += float(h_etas[(k - 1) & 1].array[::4096].sum())
+        te.stage_download_f32("eta", h_etas[k & 1].array)
+        fl_ev[k][0].record(estream)
         flush.memset_async(k & 0xff, estream)
-        te.synchronize()
+        fl_ev[k][1].record(estream)
+    te.wait_staged()
+    readback += float(h_etas[(e2e_steps - 1) & 1].array[::4096].sum())
+    te.synchronize()
+    flush_s = sum(a.elapsed_ms(b) for a, b in fl_ev) / 1e3
+    e2e_s = time.perf_counter() - t0 - flush_s
+    h_eta = h_etas[(e2e_steps - 1) & 1]
     e2e_s_max = max_over_ranks(e2e_s, dist)
     e2e_value = world * N * e2e_steps / e2e_s_max
     finite = bool(np.isfinite(h_eta.array).all())
@@ -367,7 +386,7 @@ def run_ours(args):
 
     ensemble = serving = storage = None
     if rank == 0 and world == 1:
-        h_u.free(); h_v.free(); h_eta.free(); flush.free()
+        h_u.free(); h_v.free(); [h.free() for h in h_etas]; flush.free()
         gb.close()
         gb = None
         from soapbubble_gb300 import ensemble as ens, serve
@@ -412,7 +431,10 @@ def run_ours(args):
                     "same_steps_as_value": same,
                     "h2d_bytes_per_step": 4 * (N + Nv), "d2h_bytes_per_step": 4 * N,
                     "inputs": "uair_init + vair_init (wind forcing) from pinned host memory",
-                    "result": "eta (thickness) to pinned host memory, read every step"},
+                    "result": "eta (thickness) to pinned host memory, read by the host every step",
+                    "overlap": "staged I/O on the handle's copy stream: step k+1's forcing and "
+                               "step k-1's thickness move while step k computes; L2 flush "
+                               "device time excluded"},
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),
             "stage_share": stage_share, "stage_us_per_step": stage_us,
@@ -427,7 +449,7 @@ def run_ours(args):
         }
         print(json.dumps(line), flush=True)
     if gb is not None:
-        h_u.free(); h_v.free(); h_eta.free(); flush.free()
+        h_u.free(); h_v.free(); [h.free() for h in h_etas]; flush.free()
         gb.close()
     if dist is not None:
         dist.destroy_process_group()

@@ -211,6 +211,26 @@ int sb_download_field_f32(sb_bubble* b, sb_field which, float* dst, size_t n);
  * last solve missed its tolerance. */
 int sb_synchronize(sb_bubble* b);
 
+/* Staged I/O beside the steps (no counterpart in the reference, whose frame
+ * loop copies synchronously).  Copies run on the handle's own copy stream
+ * through per-field FP32 device buffers, so they overlap the kernels queued
+ * on the compute stream:
+ *   sb_stage_upload_f32 queues the host -> buffer copy of src (n =
+ *     sb_field_size elements) now; the handle's next sb_step or
+ *     sb_step_timed waits for it and moves it into the field (a device copy,
+ *     or a conversion for BF16 storage) before its first kernel.  One staged
+ *     upload per field until a step takes it (SB_ERR_INVALID otherwise);
+ *   sb_stage_download_f32 copies the field, as it stands after the queued
+ *     steps, into the buffer on the compute stream and then to dst on the
+ *     copy stream;
+ *   sb_wait_staged returns when every staged copy queued so far has landed.
+ * Host buffers must be page-locked for the copies to overlap and stay valid
+ * until sb_wait_staged (downloads) or the taking step (uploads) returns.
+ * Fields: every field of sb_upload_field_f32 (the maps are not staged). */
+int sb_stage_upload_f32(sb_bubble* b, sb_field which, const float* src, size_t n);
+int sb_stage_download_f32(sb_bubble* b, sb_field which, float* dst, size_t n);
+int sb_wait_staged(sb_bubble* b);
+
 /* Statistics of the last step (synchronises). */
 int sb_get_stats(sb_bubble* b, sb_stats* out);
 

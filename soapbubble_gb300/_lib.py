@@ -117,6 +117,10 @@ def lib() -> C.CDLL:
     L.sb_init_thickness_from_exr.argtypes = [H, C.c_char_p]
     L.sb_init_airflow_from_exr.argtypes = [H, C.c_char_p]
     L.sb_exr_load_resized.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, dp]
+    fp = C.POINTER(C.c_float)
+    L.sb_stage_upload_f32.argtypes = [H, C.c_int, fp, C.c_size_t]
+    L.sb_stage_download_f32.argtypes = [H, C.c_int, fp, C.c_size_t]
+    L.sb_wait_staged.argtypes = [H]
     L.sb_write_velocity_exr.argtypes = [H, C.c_char_p]
     L.sb_write_concentration_exr.argtypes = [H, C.c_char_p]
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
@@ -126,7 +130,8 @@ def lib() -> C.CDLL:
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
                  "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
                  "sb_init_thickness_from_exr", "sb_init_airflow_from_exr", "sb_exr_load_resized",
-                 "sb_write_velocity_exr", "sb_write_concentration_exr"):
+                 "sb_write_velocity_exr", "sb_write_concentration_exr", "sb_stage_upload_f32",
+                 "sb_stage_download_f32", "sb_wait_staged"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -146,4 +151,5 @@ EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",
            "sb_batch_step_timed", "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
            "sb_batch_stream", "sb_init_thickness_from_exr", "sb_init_airflow_from_exr",
-           "sb_exr_load_resized", "sb_write_velocity_exr", "sb_write_concentration_exr"]
+           "sb_exr_load_resized", "sb_write_velocity_exr", "sb_write_concentration_exr",
+           "sb_stage_upload_f32", "sb_stage_download_f32", "sb_wait_staged"]

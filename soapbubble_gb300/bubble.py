@@ -156,6 +156,24 @@ class GpuBubble:
                                           out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
               "sb_download_field_f32")
 
+    def stage_upload_f32(self, name: str, a: np.ndarray) -> None:
+        """Host -> device copy on the copy stream, taken by the next step."""
+        assert a.dtype == np.float32 and a.flags.c_contiguous
+        check(lib().sb_stage_upload_f32(self.h, _lib.FIELD_ID[name],
+                                        a.ctypes.data_as(C.POINTER(C.c_float)), a.size),
+              "sb_stage_upload_f32")
+
+    def stage_download_f32(self, name: str, out: np.ndarray) -> None:
+        """The field after the queued steps to `out`, on the copy stream;
+        wait_staged() before reading `out`."""
+        assert out.dtype == np.float32 and out.flags.c_contiguous
+        check(lib().sb_stage_download_f32(self.h, _lib.FIELD_ID[name],
+                                          out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
+              "sb_stage_download_f32")
+
+    def wait_staged(self) -> None:
+        check(lib().sb_wait_staged(self.h), "sb_wait_staged")
+
     def synchronize(self) -> None:
         check(lib().sb_synchronize(self.h), "sb_synchronize")
 

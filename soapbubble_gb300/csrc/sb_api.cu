@@ -85,6 +85,13 @@ struct sb_bubble {
     SbStepPlan plan{};                 // this bubble as a set of one
     SbBubbleDesc desc{};               // host copy of the bubble's descriptor
     cudaGraphExec_t graph = nullptr;   // one captured step
+    // staged I/O (sb_stage_upload_f32 / sb_stage_download_f32): a copy
+    // stream, per field and direction an FP32 device buffer (made on first
+    // use), and the events that order the buffers between the two streams
+    cudaStream_t copy_stream = nullptr;
+    float* stage_buf[2][SB_FIELD_COUNT] = {};      // [0] uploads, [1] downloads
+    cudaEvent_t stage_ev[4][SB_FIELD_COUNT] = {};  // kUpLanded, kUpTaken, kDnReady, kDnDone
+    bool up_pending[SB_FIELD_COUNT] = {};
 };
 
 static_assert(SB_STORE_FP32 == kStoreF32 && SB_STORE_BF16 == kStoreBF16, "storage codes");
@@ -599,6 +606,16 @@ int sb_destroy(sb_bubble* b) {
     if (!b) return SB_OK;
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->copy_stream) {
+        cudaStreamSynchronize(b->copy_stream);
+        cudaStreamDestroy(b->copy_stream);
+    }
+    for (auto& row : b->stage_buf)
+        for (float* p : row)
+            if (p) cudaFree(p);
+    for (auto& row : b->stage_ev)
+        for (cudaEvent_t e : row)
+            if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : b->ev)
         if (e) cudaEventDestroy(e);
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -842,12 +859,113 @@ void bubble_advance(sb_bubble* b, int n) {
 
 extern "C" {
 
+namespace {
+
+enum { kUpLanded = 0, kUpTaken = 1, kDnReady = 2, kDnDone = 3 };
+
+// The copy stream, the buffer of `which` for direction dir (0 up, 1 down)
+// and the field's events, made on first use.
+int stage_prepare(sb_bubble* b, sb_field which, int dir) {
+    if (!b->copy_stream) SB_CHECK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+    if (!b->stage_ev[0][which])
+        for (int k = 0; k < 4; ++k)
+            SB_CHECK(cudaEventCreateWithFlags(&b->stage_ev[k][which], cudaEventDisableTiming));
+    if (!b->stage_buf[dir][which]) {
+        const size_t n = sb_field_size(b, which);
+        if (cudaMalloc(&b->stage_buf[dir][which], n * sizeof(float)) != cudaSuccess)
+            return fail(SB_ERR_OOM, "staging buffer allocation failed");
+    }
+    return SB_OK;
+}
+
+// Moves the staged uploads that have not been taken yet into their fields,
+// on stream s, after their host copies have landed.
+int take_staged_uploads(sb_bubble* b, cudaStream_t s) {
+    for (int w = 0; w < SB_FIELD_COUNT; ++w) {
+        if (!b->up_pending[w]) continue;
+        const sb_field which = (sb_field)w;
+        const size_t n = sb_field_size(b, which);
+        const float* src = b->stage_buf[0][w];
+        SB_CHECK(cudaStreamWaitEvent(s, b->stage_ev[kUpLanded][w], 0));
+        SbScalar* sp = sptr(b, which);
+        if (sp && b->storage != kStoreF32) {
+            SB_CHECK(launch_store(sp, src, (int)n, base_of(b, sp), b->storage, s));
+            b->launches += 1;
+        } else {
+            float* dst = sp ? reinterpret_cast<float*>(sp) : fptr(b, which);
+            SB_CHECK(cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        }
+        SB_CHECK(cudaEventRecord(b->stage_ev[kUpTaken][w], s));
+        b->up_pending[w] = false;
+    }
+    return SB_OK;
+}
+
+bool stageable(sb_bubble* b, sb_field which) {
+    return which >= 0 && which < SB_FIELD_COUNT && (sptr(b, which) || fptr(b, which));
+}
+
+}  // namespace
+
+int sb_stage_upload_f32(sb_bubble* b, sb_field which, const float* src, size_t n) {
+    if (!b || !src) return fail(SB_ERR_INVALID, "null argument");
+    if (!stageable(b, which)) return fail(SB_ERR_INVALID, "maps cannot be staged");
+    if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
+    if (b->up_pending[which])
+        return fail(SB_ERR_INVALID, "the field's previous staged upload has not been taken by a step");
+    SB_CHECK(cudaSetDevice(b->device));
+    int rc = stage_prepare(b, which, 0);
+    if (rc != SB_OK) return rc;
+    // the buffer is free once the step that took the previous upload has copied it
+    SB_CHECK(cudaStreamWaitEvent(b->copy_stream, b->stage_ev[kUpTaken][which], 0));
+    SB_CHECK(cudaMemcpyAsync(b->stage_buf[0][which], src, n * sizeof(float),
+                             cudaMemcpyHostToDevice, b->copy_stream));
+    SB_CHECK(cudaEventRecord(b->stage_ev[kUpLanded][which], b->copy_stream));
+    b->up_pending[which] = true;
+    return SB_OK;
+}
+
+int sb_stage_download_f32(sb_bubble* b, sb_field which, float* dst, size_t n) {
+    if (!b || !dst) return fail(SB_ERR_INVALID, "null argument");
+    if (!stageable(b, which)) return fail(SB_ERR_INVALID, "maps cannot be staged");
+    if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
+    SB_CHECK(cudaSetDevice(b->device));
+    int rc = stage_prepare(b, which, 1);
+    if (rc != SB_OK) return rc;
+    float* buf = b->stage_buf[1][which];
+    // snapshot of the field after the queued steps (the buffer is free once
+    // the previous staged download of the field has left it)
+    SB_CHECK(cudaStreamWaitEvent(b->stream, b->stage_ev[kDnDone][which], 0));
+    SbScalar* sp = sptr(b, which);
+    if (sp && b->storage != kStoreF32) {
+        SB_CHECK(launch_load(buf, sp, (int)n, base_of(b, sp), b->storage, b->stream));
+        b->launches += 1;
+    } else {
+        const float* src = sp ? reinterpret_cast<const float*>(sp) : fptr(b, which);
+        SB_CHECK(cudaMemcpyAsync(buf, src, n * sizeof(float), cudaMemcpyDeviceToDevice, b->stream));
+    }
+    SB_CHECK(cudaEventRecord(b->stage_ev[kDnReady][which], b->stream));
+    SB_CHECK(cudaStreamWaitEvent(b->copy_stream, b->stage_ev[kDnReady][which], 0));
+    SB_CHECK(cudaMemcpyAsync(dst, buf, n * sizeof(float), cudaMemcpyDeviceToHost, b->copy_stream));
+    SB_CHECK(cudaEventRecord(b->stage_ev[kDnDone][which], b->copy_stream));
+    return SB_OK;
+}
+
+int sb_wait_staged(sb_bubble* b) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    if (!b->copy_stream) return SB_OK;
+    SB_CHECK(cudaSetDevice(b->device));
+    SB_CHECK(cudaStreamSynchronize(b->copy_stream));
+    return SB_OK;
+}
+
 int sb_step(sb_bubble* b, int n_steps, double t_frame, double dt) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     if (n_steps < 0 || !(dt > 0)) return fail(SB_ERR_INVALID, "bad step count or dt");
     SB_CHECK(cudaSetDevice(b->device));
     int rc = set_step_params(b, t_frame, dt);
     if (rc != SB_OK) return rc;
+    if ((rc = take_staged_uploads(b, b->stream)) != SB_OK) return rc;
     if (n_steps > 0 && !b->graph && (rc = capture_plan(b->plan, b->stream, &b->graph)) != SB_OK)
         return rc;
     for (int s = 0; s < n_steps; ++s) SB_CHECK(cudaGraphLaunch(b->graph, b->stream));
@@ -861,6 +979,7 @@ int sb_step_timed(sb_bubble* b, int n_steps, double t_frame, double dt, double* 
     SB_CHECK(cudaSetDevice(b->device));
     int rc = set_step_params(b, t_frame, dt);
     if (rc != SB_OK) return rc;
+    if ((rc = take_staged_uploads(b, b->stream)) != SB_OK) return rc;
     for (int s = 0; s < n_steps; ++s) {
         if ((rc = timed_plan_step(b->plan, b->stream, b->ev, stage_ms)) != SB_OK) return rc;
         bubble_advance(b, 1);
