@@ -156,7 +156,7 @@ struct ArenaPlan {
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
     size_t div, d_eta, d_gam, err_eta, err_gam;
     size_t dmass, cE, cS, rhs, r0, x, dx, r, z, z1, p, q, xff, pcr, pcr_levels, step, stats;
-    size_t self, self_list, roff, done_at, cnt, rec, acc;  // the bubble's solve set
+    size_t self, self_list, roff, done_at, cnt, rec, acc, bar;  // the bubble's solve set
     size_t tiles[3];                                           // its cell tiles
 };
 
@@ -198,6 +198,7 @@ ArenaPlan plan_arena(const SbGrid& g, int storage) {
     a.cnt = a.L.take(4);
     a.rec = a.L.take(2 * sizeof(SbSolveRec));
     a.acc = a.L.take(sizeof(unsigned long long) * kSolveAccWords);
+    a.bar = a.L.take(sizeof(unsigned) * kGridBarWords);
     a.step = a.L.take(sizeof(SbStepParams));
     a.stats = a.L.take(sizeof(SbDevStats) + 64);
     return a;
@@ -491,6 +492,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.cnt = (int*)(A + a.cnt);
     f.rec = (SbSolveRec*)(A + a.rec);
     f.acc = (unsigned long long*)(A + a.acc);
+    f.bar = (unsigned*)(A + a.bar);
 
     // trigonometric tables in FP64, stored FP32
     std::vector<float> tab(4 * g.nT + 2);
@@ -577,6 +579,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
         S.done_at = f.done_at;
         S.cnt = f.cnt;
         S.acc = f.acc;
+        S.bar = f.bar;
         P.maxNP = g.nP;
         P.solver = b->solver;
         P.storage = b->storage;
@@ -1332,7 +1335,8 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     const size_t o_roff = L.take(sizeof(int) * (n + 1)),
                  o_rec = L.take(sizeof(SbSolveRec) * 2 * n), o_done = L.take(sizeof(int) * n),
                  o_cnt = L.take(sizeof(int) * n),
-                 o_acc = L.take(sizeof(unsigned long long) * kSolveAccWords * n);
+                 o_acc = L.take(sizeof(unsigned long long) * kSolveAccWords * n),
+                 o_bar = L.take(sizeof(unsigned) * kGridBarWords);
     e = cudaMalloc((void**)&B->arena, L.bytes);
     if (e == cudaSuccess) e = cudaMemset(B->arena, 0, L.bytes);
     if (e != cudaSuccess) {
@@ -1362,6 +1366,7 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     S.done_at = (int*)(A + o_done);
     S.cnt = (int*)(A + o_cnt);
     S.acc = (unsigned long long*)(A + o_acc);
+    S.bar = (unsigned*)(A + o_bar);
     // members may have work queued on their own streams
     for (sb_bubble* b : B->m) e = e == cudaSuccess ? cudaStreamSynchronize(b->stream) : e;
     if (e == cudaSuccess)

@@ -72,6 +72,7 @@ struct SbFields {
     int *roff, *done_at, *cnt;
     SbSolveRec* rec;
     unsigned long long* acc;
+    unsigned* bar;                                 // grid barrier words of its cooperative launches
     SbStepParams* step;                            // device copy of step scalars
     SbDevStats* stats;
 };
@@ -141,7 +142,8 @@ struct SbSolveRec {
 
 // Words of a system's exact dot-product accumulators: three buffers (used
 // in rotation by phase) of three values of 10 fixed-point chunks and a flag.
-constexpr int kSolveAccWords = 3 * 3 * 11;
+constexpr int kSolveAccWords = 3 * 3 * 16;  // 3 buffers x 3 values x one 128-byte line
+constexpr int kGridBarWords = 32;           // grid barrier word on its own 128-byte line (sb_sync.cuh)
 
 // A set of implicit systems solved by one cooperative launch: the system of
 // one bubble, or the systems of every bubble of a batch (at most 1024, with
@@ -155,6 +157,8 @@ struct SbSolveSet {
     int* done_at;               // [nb] first phase in which the system is finished
     int* cnt;                   // [nb] rows completed in the current phase (0 between launches)
     unsigned long long* acc;    // [nb][kSolveAccWords] exact dot-product accumulators (0 between launches)
+    unsigned* bar;              // [kGridBarWords] grid barrier of the cooperative launches
+                                // (sb_sync.cuh; zeroed at creation)
 };
 
 // Implicit surfactant solve (sb_solver.cu).  prepare_solve sets the kernel

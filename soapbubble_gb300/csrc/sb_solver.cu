@@ -40,15 +40,13 @@
 // products are summed in float-float within a row and exactly across rows.
 // (Rounding the products, as plain mode does, costs the mixed mode about a
 // fifth more iterations on ruptured films.)
-#include <cooperative_groups.h>
 
 #include <algorithm>
 #include <climits>
 
 #include "sb_ff.cuh"
 #include "sb_internal.h"
-
-namespace cg = cooperative_groups;
+#include "sb_sync.cuh"
 
 namespace sb {
 
@@ -673,8 +671,10 @@ __device__ __forceinline__ void row_final(const SbGrid& g, const SbFields& f, in
 // again before phase p + 3.
 constexpr int kAccChunks = 10;             // chunks 0..8 take additions, chunk 9 carries
 constexpr int kAccWords = kAccChunks + 1;  // per value
-constexpr int kAccBuf = 3 * kAccWords;     // per buffer (three values)
+constexpr int kAccSlot = 16;               // words per value in memory: one 128-byte line
+constexpr int kAccBuf = 3 * kAccSlot;      // per buffer (three values)
 static_assert(3 * kAccBuf == kSolveAccWords, "accumulator words per system");
+static_assert(kAccWords <= kAccSlot, "a value fits its line");
 
 __device__ __forceinline__ unsigned long long* acc_buf(const SbSolveSet& S, int b, int p) {
     return S.acc + (size_t)b * kSolveAccWords + (size_t)(p % 3) * kAccBuf;
@@ -704,8 +704,8 @@ __device__ __forceinline__ void acc_add(unsigned long long* a, float v) {
 
 // x.hi + x.lo into value v of buffer a.
 __device__ __forceinline__ void acc_add_ff(unsigned long long* a, int v, ff x) {
-    acc_add(a + v * kAccWords, x.hi);
-    acc_add(a + v * kAccWords, x.lo);
+    acc_add(a + v * kAccSlot, x.hi);
+    acc_add(a + v * kAccSlot, x.lo);
 }
 
 // Carries: chunks 0..8 into [0, 2^32), the sign in chunk 9.
@@ -935,18 +935,25 @@ __device__ __forceinline__ bool transition(SbSolveRec& rc, ff A, ff B, ff C,
 // every block of the grid would queue on the same few lines), threads 0..2
 // convert one value each; the sums land in out[0..2] (shared memory) for
 // every thread after the call.
+// Only the values of bit mask vals are read (each value is one line, so a
+// phase that produced one value costs every block one line request, where
+// all blocks of the grid read the same lines at once).
 // Warp 0 only (the sums are in out[] for warp 0 afterwards).
 __device__ __forceinline__ void acc_sums_warp0(const unsigned long long* ab,
-                                               unsigned long long* s_w, ff* out) {
-    for (int k = threadIdx.x; k < kAccBuf; k += 32) s_w[k] = __ldcg(ab + k);
+                                               unsigned long long* s_w, ff* out, int vals) {
+    const int lane = threadIdx.x;
+    for (int l = lane; l < 3 * kAccWords; l += 32) {  // 33 words: lane 0 takes two
+        const int v = l / kAccWords, w = l - v * kAccWords;
+        if ((vals >> v) & 1) s_w[l] = __ldcg(ab + v * kAccSlot + w);
+    }
     __syncwarp();
-    if (threadIdx.x < 3) out[threadIdx.x] = acc_ff(s_w + threadIdx.x * kAccWords);
+    if (lane < 3 && ((vals >> lane) & 1)) out[lane] = acc_ff(s_w + lane * kAccWords);
     __syncwarp();
 }
 
 __device__ __forceinline__ void acc_sums(const unsigned long long* ab, unsigned long long* s_w,
-                                         ff* out) {
-    if (threadIdx.x < 32) acc_sums_warp0(ab, s_w, out);
+                                         ff* out, int vals) {
+    if (threadIdx.x < 32) acc_sums_warp0(ab, s_w, out, vals);
     __syncthreads();
 }
 
@@ -1190,11 +1197,12 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     __shared__ __align__(16) SbBubbleDesc s_d;
     __shared__ unsigned s_pre[kMaxSystems + 1];
     __shared__ int s_last;
-    __shared__ unsigned long long s_w[kAccBuf];
+    __shared__ unsigned long long s_w[3 * kAccWords];
     __shared__ ff s_sums[3];
     __shared__ SbSolveRec s_rc;
     int staged = -1;  // system whose descriptor is in s_d
-    cg::grid_group grid = cg::this_grid();
+    int* const faults = &S.descs[0]->f.stats->wait_faults;
+    if (*faults) return;  // a wait gave up earlier: the barrier word is not trusted any more
     Stage St;
     stage_init(St, &bar, sm, cfg.blob);
     const unsigned G = gridDim.x;
@@ -1254,12 +1262,15 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             }
             if (last) {
                 __threadfence();
-                if (vals) acc_sums(acc_buf(S, b, p), s_w, s_sums);
+                if (vals) acc_sums(acc_buf(S, b, p), s_w, s_sums, vals);
                 if (threadIdx.x == 0) advance<MIXED>(S, b, p, s_sums, cfg);
             }
             __syncthreads();  // s_d and s_last are reused
         }
-        grid.sync();
+        if (!grid_barrier(S.bar, G, faults)) {
+            stage_wait(St, S.descs[0]->f.stats);  // no copy may land after the block left
+            return;
+        }
     }
     // the increment and the new gamma of every system, same split with all
     // systems counted
@@ -1292,11 +1303,11 @@ __global__ void __launch_bounds__(kSolveBlock, 4)
 k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     extern __shared__ __align__(16) float sm[];
     __shared__ __align__(8) uint64_t bar;
-    cg::grid_group grid = cg::this_grid();
     __shared__ SbSolveRec s_rc;  // the system's scalars (the same in every block)
     __shared__ int s_done;
-    __shared__ unsigned long long s_w[kAccBuf];
+    __shared__ unsigned long long s_w[3 * kAccWords];
     __shared__ ff s_sums[3];
+    if (f.stats->wait_faults) return;  // a wait gave up earlier: the barrier word is not trusted
     if (threadIdx.x == 0) s_rc.kind = first_kind(f.stats, cfg);
     Stage St;
     stage_init(St, &bar, sm, cfg.blob);  // (its barrier publishes s_rc.kind)
@@ -1306,7 +1317,8 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
             // warp 0 reads the sums (if the phase produced any) and advances
             // the scalars; one barrier
             if (threadIdx.x < 32) {
-                if (kind_values(s_rc.kind)) acc_sums_warp0(acc_buf(S, 0, p - 1), s_w, s_sums);
+                const int pv = kind_values(s_rc.kind);
+                if (pv) acc_sums_warp0(acc_buf(S, 0, p - 1), s_w, s_sums, pv);
                 if (threadIdx.x == 0) {
                     s_done = transition<MIXED>(s_rc, s_sums[0], s_sums[1], s_sums[2], cfg) ? 1 : 0;
                     if (s_done && blockIdx.x == 0) write_stats(f.stats, s_rc);
@@ -1326,10 +1338,13 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
             row_phase<MIXED, PER>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
             if (vals) reduce_row(S, 0, p, vals, reinterpret_cast<const ff*>(St.work + g.nP));
         }
-        grid.sync();
+        if (!grid_barrier(S.bar, G, &f.stats->wait_faults)) {
+            stage_wait(St, f.stats);  // no copy may land after the block left
+            return;
+        }
     }
     // every block has read its last sums: clear the buffers for the next solve
-    grid.sync();
+    if (!grid_barrier(S.bar, G, &f.stats->wait_faults)) return;
     if (blockIdx.x == 0) acc_zero(S.acc, kSolveAccWords, threadIdx.x, blockDim.x);
     for (int i = blockIdx.x; i < nT; i += G) row_final<MIXED, PER>(g, f, i);
 }

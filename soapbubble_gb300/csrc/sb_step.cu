@@ -19,12 +19,10 @@
 //   k_reinit       reInitializeMapping, correctCentered2 (2218-2280, 2509-2564)
 // van der Waals is identically zero in the reference (W1 = W2 = 0,
 // bubble.cu:2633-2638) and is folded out.
-#include <cooperative_groups.h>
 
 #include "sb_device.cuh"
 #include "sb_internal.h"
-
-namespace cg = cooperative_groups;
+#include "sb_sync.cuh"
 
 namespace sb {
 
@@ -763,8 +761,9 @@ __device__ __forceinline__ void reinit_commit(const SbPhys& ph, const SbFields& 
 template <class T>
 __global__ void __launch_bounds__(kBlock)
 k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict__ tiles,
-         int ntiles) {
+         int ntiles, unsigned* gbar) {
     __shared__ int any;
+    if (descs[0]->f.stats->wait_faults) return;  // the barrier word is not trusted any more
     if (threadIdx.x == 0) {
         int a = 0;
         for (int b = 0; b < nb; ++b) a |= reinit_now(descs[b]->f.stats) ? 1 : 0;
@@ -772,7 +771,6 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
     }
     __syncthreads();
     if (!any) return;
-    cg::grid_group grid = cg::this_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
         const SbBubbleDesc& d = *descs[tl.x];
@@ -785,7 +783,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
             reinit_correct<T>(d.g, d.ph, d.f, d.cur, idx);
         }
     }
-    grid.sync();
+    if (!grid_barrier(gbar, gridDim.x, &descs[0]->f.stats->wait_faults)) return;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
         const SbBubbleDesc& d = *descs[tl.x];
@@ -915,7 +913,8 @@ cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s) {
             int nb = P.nb;
             const int2* tt = P.tiles[1];
             int nt = P.ntiles[1];
-            void* args[] = {&dd, &nb, &tt, &nt};
+            unsigned* gb = P.set.bar;
+            void* args[] = {&dd, &nb, &tt, &nt, &gb};
             const void* fn = bf ? (const void*)k_reinit<__nv_bfloat16> : (const void*)k_reinit<float>;
             return cudaLaunchCooperativeKernel(fn, dim3(reinit_blocks()), dim3(kBlock), args, 0, s);
         }

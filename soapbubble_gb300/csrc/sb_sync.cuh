@@ -1,0 +1,67 @@
+// Grid-wide barrier with a bounded wait, for the cooperative kernels (the
+// implicit solve and the map re-initialisation).
+//
+// The kernels are launched cooperatively, so every block is resident and a
+// barrier completes as soon as every block reaches it.  The wait is bounded
+// all the same: a block whose wait gives up counts a fault (reported by
+// sb_get_stats as an error) and leaves the kernel, so that a bug that sends
+// blocks down different paths ends the launch with an error instead of
+// leaving the GPU waiting.
+//
+// Memory (kGridBarWords words, zeroed when the bubble or batch is made): word 0 holds
+// the arrivals in its low 31 bits and the generation in bit 31.  Every block
+// adds 1 except block 0, which adds 2^31 - (nblocks - 1); the adds of one
+// barrier sum to 2^31, so bit 31 flips exactly when the last block arrives
+// and the low bits return to zero for the next barrier.  One atomic per block
+// and a poll of the same word.  A block's writes before the barrier are
+// published by its thread 0 (block barrier, then a GPU-scope fence before
+// arriving), and the waiting side fences after seeing the flip, so every
+// write before the barrier is visible to every block after it.  The launches
+// of one bubble or batch share the word: a launch that completes leaves its
+// low bits at zero for the next.  After a wait gave up the word is no longer
+// trusted, so the cooperative kernels of a bubble with a counted fault return
+// at once (its results stop changing and sb_get_stats keeps reporting the
+// fault).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sb_internal.h"
+
+namespace sb {
+
+constexpr unsigned kGridBarPolls = 1u << 22;  // polls before a wait gives up (~1-2 s)
+constexpr unsigned kGridBarSpin = 1u << 10;   // polls before each poll also sleeps briefly
+
+__device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Returns true in every thread of the block, or false in every thread when
+// this block's wait gave up (one fault counted in *faults).
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* faults) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (nblocks - 1u) : 1u;
+        __threadfence();
+        const unsigned old = atomicAdd(bar, add);
+        unsigned polls = 0;
+        while (((ld_relaxed_gpu(bar) ^ old) & 0x80000000u) == 0u) {
+            if (++polls > kGridBarPolls) {
+                atomicAdd(faults, 1);
+                ok = 0;
+                break;
+            }
+            if (polls > kGridBarSpin) __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+}  // namespace sb
