@@ -25,7 +25,7 @@ PHYS = ("eta", "gamma", "u_theta", "u_phi")
 
 
 def new_pair(oracle, nT, recipe, dt, pre, t, seed, force=0, solver_mode=0, tol=1e-10,
-             gs_scale=1.0, nu_scale=1.0, M_scale=1.0):
+             gs_scale=1.0, nu_scale=1.0, M_scale=1.0, otol=None):
     from soapbubble_gb300 import synth
     from soapbubble_gb300.bubble import GpuBubble, make_params
     f = synth.make_fields(recipe, nT, seed)
@@ -37,6 +37,8 @@ def new_pair(oracle, nT, recipe, dt, pre, t, seed, force=0, solver_mode=0, tol=1
     op.gs *= gs_scale
     op.M *= M_scale
     op.Cr *= np.sqrt(nu_scale)
+    if otol is not None:
+        op.solver_tol = otol
     ob = oracle.OracleBubble(op, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
     for _ in range(pre):
         ob.step()
@@ -106,6 +108,36 @@ def test_step_matches_oracle(oracle, gpulib, case):
         assert gs.reinit == st.reinit
         assert gs.distortion == pytest.approx(st.distortion, rel=1e-3, abs=1e-6)
         check_errors(P.compare(gb, ob))
+
+
+# The benchmark grids themselves: c1 (512 x 1024) and c2 (1024 x 2048), one
+# step from a state the oracle stepped once (oracle solve to 1e-11).
+FULL_CASES = [(512, "c1", 0.002, 1, 0.0, 20261203), (1024, "c2", 0.001, 1, 0.0, 20261204)]
+
+
+@pytest.mark.parametrize("case", FULL_CASES, ids=lambda c: f"{c[0]}-{c[1]}")
+def test_full_size_step_matches_oracle(oracle, gpulib, case):
+    nT, recipe, dt, pre, t, seed = case
+    gb, ob = new_pair(oracle, nT, recipe, dt, pre, t, seed, otol=1e-11)
+    with gb:
+        st = ob.step()
+        gb.step(1, t, dt)
+        gs = gb.stats()
+        assert gs.solver_converged == 1
+        assert gs.reinit == st.reinit
+        assert gs.distortion == pytest.approx(st.distortion, rel=1e-3, abs=1e-6)
+        err = P.compare(gb, ob)
+        for k in PHYS + ("eta_init", "gamma_init", "eta_init_last", "gamma_init_last"):
+            assert err[k] <= TOL_FIELD, (k, err[k])
+        for k in ("fwd", "bwd", "bwdprev"):
+            assert err[k] <= TOL_MAP_CELLS, (k, err[k])
+        # the BIMOCQ change accumulators hold a step or two of small changes
+        # here (c2: dt 0.001 s), so they are measured against the field they
+        # correct rather than against their own size
+        for k, field in (("eta_delta", "eta"), ("gamma_delta", "gamma"),
+                         ("eta_delta_last", "eta"), ("gamma_delta_last", "gamma")):
+            d = np.nanmax(np.abs(gb.download(k) - ob.a[P.FIELD_MAP[k]]))
+            assert d / np.nanmax(np.abs(ob.a[P.FIELD_MAP[field]])) <= TOL_FIELD, (k, d)
 
 
 @pytest.mark.parametrize("scales", [(1.5, 0.5, 1.3), (0.5, 1.5, 0.6)])
