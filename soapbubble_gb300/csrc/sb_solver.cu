@@ -1203,6 +1203,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     int staged = -1;  // system whose descriptor is in s_d
     int* const faults = &S.descs[0]->f.stats->wait_faults;
     if (*faults) return;  // a wait gave up earlier: the barrier word is not trusted any more
+    unsigned gen = grid_barrier_gen(S.bar);
     Stage St;
     stage_init(St, &bar, sm, cfg.blob);
     const unsigned G = gridDim.x;
@@ -1267,7 +1268,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             }
             __syncthreads();  // s_d and s_last are reused
         }
-        if (!grid_barrier(S.bar, G, faults)) {
+        if (!grid_barrier(S.bar, gen, G, faults)) {
             stage_wait(St, S.descs[0]->f.stats);  // no copy may land after the block left
             return;
         }
@@ -1308,6 +1309,7 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     __shared__ unsigned long long s_w[3 * kAccWords];
     __shared__ ff s_sums[3];
     if (f.stats->wait_faults) return;  // a wait gave up earlier: the barrier word is not trusted
+    unsigned gen = grid_barrier_gen(S.bar);
     if (threadIdx.x == 0) s_rc.kind = first_kind(f.stats, cfg);
     Stage St;
     stage_init(St, &bar, sm, cfg.blob);  // (its barrier publishes s_rc.kind)
@@ -1338,13 +1340,13 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
             row_phase<MIXED, PER>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
             if (vals) reduce_row(S, 0, p, vals, reinterpret_cast<const ff*>(St.work + g.nP));
         }
-        if (!grid_barrier(S.bar, G, &f.stats->wait_faults)) {
+        if (!grid_barrier(S.bar, gen, G, &f.stats->wait_faults)) {
             stage_wait(St, f.stats);  // no copy may land after the block left
             return;
         }
     }
     // every block has read its last sums: clear the buffers for the next solve
-    if (!grid_barrier(S.bar, G, &f.stats->wait_faults)) return;
+    if (!grid_barrier(S.bar, gen, G, &f.stats->wait_faults)) return;
     if (blockIdx.x == 0) acc_zero(S.acc, kSolveAccWords, threadIdx.x, blockDim.x);
     for (int i = blockIdx.x; i < nT; i += G) row_final<MIXED, PER>(g, f, i);
 }

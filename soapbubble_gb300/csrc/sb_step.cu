@@ -771,6 +771,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
     }
     __syncthreads();
     if (!any) return;
+    unsigned gen = grid_barrier_gen(gbar);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
         const SbBubbleDesc& d = *descs[tl.x];
@@ -783,7 +784,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
             reinit_correct<T>(d.g, d.ph, d.f, d.cur, idx);
         }
     }
-    if (!grid_barrier(gbar, gridDim.x, &descs[0]->f.stats->wait_faults)) return;
+    if (!grid_barrier(gbar, gen, gridDim.x, &descs[0]->f.stats->wait_faults)) return;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
         const SbBubbleDesc& d = *descs[tl.x];
