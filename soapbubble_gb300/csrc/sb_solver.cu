@@ -542,28 +542,42 @@ __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i
     float* __restrict__ qout = f.x;
     const bool hasS = i < nT - 1, hasN = i > 0;
     ff pq = ff_zero();
+    // columns in pairs: both columns' loads are issued before either's
+    // arithmetic (two L2 round trips per row instead of four at PER = 4)
+    constexpr int G2 = PER >= 2 ? 2 : 1;
 #pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
-        const int jj = j < nP ? j : 0;  // rows shorter than the block: a valid dummy
-        const int c = row + jj;
-        const int e = row + ((jj + 1) & g.maskP);
-        const int w = row + ((jj - 1) & g.maskP);
-        const int sc = hasS ? c + nP : c, nc = hasN ? c - nP : c;
-        const float zc = z[c], pc0 = pold[c];
-        const float ze = z[e], pe = pold[e], zw = z[w], pw = pold[w];
-        const float zs = z[sc], ps = pold[sc], zn = z[nc], pn = pold[nc];
-        const float dm = dmass[c], ce = cE[c], cw = cE[w];
-        const float cs = hasS ? cS[c] : 0.0f;
-        const float cn = hasN ? cS[nc] : 0.0f;
-        if (j < nP) {
-            const float pc = zc + beta * pc0;
-            float qf = dm * pc + ce * (pc - (ze + beta * pe)) + cw * (pc - (zw + beta * pw));
-            if (hasS) qf += cs * (pc - (zs + beta * ps));
-            if (hasN) qf += cn * (pc - (zn + beta * pn));
-            pnew[c] = pc;
-            qout[c] = qf;
-            pq = acc<MIXED>(pq, pc, qf);
+    for (int k0 = 0; k0 < PER; k0 += G2) {
+        float zc[G2], pc0[G2], ze[G2], pe[G2], zw[G2], pw[G2], zs[G2], ps[G2], zn[G2], pn[G2];
+        float dm[G2], ce[G2], cw[G2], cs[G2], cn[G2];
+        int cc[G2];
+#pragma unroll
+        for (int u = 0; u < G2; ++u) {
+            const int j = col_of(k0 + u);
+            const int jj = j < nP ? j : 0;  // rows shorter than the block: a valid dummy
+            const int c = row + jj;
+            const int e = row + ((jj + 1) & g.maskP);
+            const int w = row + ((jj - 1) & g.maskP);
+            const int sc = hasS ? c + nP : c, nc = hasN ? c - nP : c;
+            cc[u] = c;
+            zc[u] = z[c]; pc0[u] = pold[c];
+            ze[u] = z[e]; pe[u] = pold[e]; zw[u] = z[w]; pw[u] = pold[w];
+            zs[u] = z[sc]; ps[u] = pold[sc]; zn[u] = z[nc]; pn[u] = pold[nc];
+            dm[u] = dmass[c]; ce[u] = cE[c]; cw[u] = cE[w];
+            cs[u] = hasS ? cS[c] : 0.0f;
+            cn[u] = hasN ? cS[nc] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < G2; ++u) {
+            if (col_of(k0 + u) < nP) {
+                const float pc = zc[u] + beta * pc0[u];
+                float qf = dm[u] * pc + ce[u] * (pc - (ze[u] + beta * pe[u])) +
+                           cw[u] * (pc - (zw[u] + beta * pw[u]));
+                if (hasS) qf += cs[u] * (pc - (zs[u] + beta * ps[u]));
+                if (hasN) qf += cn[u] * (pc - (zn[u] + beta * pn[u]));
+                pnew[cc[u]] = pc;
+                qout[cc[u]] = qf;
+                pq = acc<MIXED>(pq, pc, qf);
+            }
         }
     }
     return pq;
