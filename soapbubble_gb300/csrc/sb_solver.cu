@@ -52,8 +52,17 @@ namespace sb {
 
 namespace {
 
-constexpr int kSolveBlock = 256;
-constexpr int kWarps = kSolveBlock / 32;
+// Threads of a solve block: 256, or 512 for rows of 2048 columns (four
+// columns per thread either way).  Dot products are formed in an order that
+// does not depend on the block width: virtual thread v < 256 owns columns
+// v + 256 k; its share is the float-float sum of its even k (in order) plus
+// that of its odd k, and the row's value sums the 256 shares in a fixed
+// order.  A block of 512 threads gives each virtual thread's even and odd k
+// to threads v and v + 256, so a bubble gets the same sums whichever block
+// width a solve set uses.
+constexpr int kVThreads = 256;
+constexpr int kWarps = kVThreads / 32;
+constexpr int kMaxNP = 2048;
 constexpr int kWaitPolls = 1 << 22;   // mbarrier polls before a copy counts as lost
 constexpr int kMaxSystems = 1024;     // systems of one solve set
 constexpr int kRowChunk = 16;         // rows a block counts at a time (sets)
@@ -212,14 +221,26 @@ __device__ __forceinline__ ff acc(ff s, float a, float b) {
 }
 
 // Column of element k of this thread in a row.
-__device__ __forceinline__ int col_of(int k) { return threadIdx.x + k * kSolveBlock; }
+template <int TB>
+__device__ __forceinline__ int col_of(int k) { return threadIdx.x + k * TB; }
+
+// The two float-float accumulators of a thread's dot-product terms: element
+// k of a 256-thread block goes to k's parity; a 512-thread block's thread
+// holds one parity only (see kVThreads).
+template <int TB>
+__device__ __forceinline__ int half_of(int k) { return TB == kVThreads ? (k & 1) : 0; }
+
+template <int TB>
+__device__ __forceinline__ ff fold_halves(const ff (&h)[2]) {
+    return TB == kVThreads ? ff_add(h[0], h[1]) : h[0];
+}
 
 // y = B_i^-1 v on theta row i: the exact solve of the row's periodic
 // tridiagonal block B_i (phi couplings; the theta couplings stay on its
-// diagonal).  rv[k] holds v at column col_of(k) (this thread's elements);
+// diagonal).  rv[k] holds v at column col_of<TB>(k) (this thread's elements);
 // the result is left in the block's work array D = S.work (D[j] for
 // column j) for the caller.  PER = equations per thread
-// (nP <= PER * kSolveBlock).
+// (nP <= PER * TB).
 //
 // Row solve of n = nP equations (indices mod n) in excess form: equation j
 //   (E_j + L_j + U_j) x_j - L_j x_{j-s} - U_j x_{j+s} = D_j,  E, L, U >= 0,
@@ -247,7 +268,7 @@ __device__ __forceinline__ int col_of(int k) { return threadIdx.x + k * kSolveBl
 // records the levels of step 3 in f.pcr_levels; later applications replay
 // the right-hand-side updates with the factors (fetched by stage_fetch
 // unless the block still holds them), with the same arithmetic.
-template <int PER, bool BUILD>
+template <int PER, int TB, bool BUILD>
 __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f, int i,
                                                  Stage& S, const float (&rv)[PER]) {
     const int nP = g.nP, nT = g.nT, mask = g.maskP;
@@ -270,7 +291,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         float* const U = S.work + 3 * n;  // coupling to j + s
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
-            const int j = col_of(k);
+            const int j = col_of<TB>(k);
             if (j < n) {
                 const int c = row + j;
                 float ex = f.dmass[c];
@@ -286,7 +307,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         // step 1; an even entry is read only by its own thread: in place
 #pragma unroll
         for (int t = 0; t < H; ++t) {
-            const int m = threadIdx.x + t * kSolveBlock;
+            const int m = threadIdx.x + t * TB;
             if (m < h) {
                 const int j = 2 * m, jm = (j - 1) & mask, jp = j + 1;
                 const float bm = E[jm] + L[jm] + U[jm];
@@ -312,7 +333,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         float sE[Q], sL[Q], sU[Q], sD[Q];
 #pragma unroll
         for (int t = 0; t < Q; ++t) {
-            const int m = threadIdx.x + t * kSolveBlock;
+            const int m = threadIdx.x + t * TB;
             if (m < q) {
                 const int j = 4 * m, jm = (j - 2) & mask, jp = j + 2;
                 const float bm = E[jm] + L[jm] + U[jm];
@@ -334,7 +355,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         bool need = false;
 #pragma unroll
         for (int t = 0; t < Q; ++t) {
-            const int m = threadIdx.x + t * kSolveBlock;
+            const int m = threadIdx.x + t * TB;
             if (m < q) {
                 P[m] = sE[t];
                 P[q + m] = sL[t];
@@ -353,7 +374,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
             need = false;
 #pragma unroll
             for (int t = 0; t < Q; ++t) {
-                const int m = threadIdx.x + t * kSolveBlock;
+                const int m = threadIdx.x + t * TB;
                 if (m < q) {
                     const int mm = (m - s) & qmask, mp = (m + s) & qmask;
                     const float bm = Ei[mm] + Li[mm] + Ui[mm];
@@ -381,7 +402,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
             const float *Lf = Ef + q, *Uf = Ef + 2 * q, *Df = Ef + 3 * q;
 #pragma unroll
             for (int t = 0; t < Q; ++t) {
-                const int m = threadIdx.x + t * kSolveBlock;
+                const int m = threadIdx.x + t * TB;
                 if (m < q) {
                     const int kk = (m + q / 2) & qmask;
                     float c1, c2;
@@ -407,14 +428,14 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         const int levels = lv < 0 ? -lv : lv;
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
-            const int j = col_of(k);
+            const int j = col_of<TB>(k);
             if (j < n) D[j] = rv[k];
         }
         stage_wait(S, f.stats);
         __syncthreads();
 #pragma unroll
         for (int t = 0; t < H; ++t) {
-            const int m = threadIdx.x + t * kSolveBlock;
+            const int m = threadIdx.x + t * TB;
             if (m < h) {
                 const int j = 2 * m;
                 const float2 c = cr1[m];
@@ -426,7 +447,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         float* Po = Pi + q;
 #pragma unroll
         for (int t = 0; t < Q; ++t) {
-            const int m = threadIdx.x + t * kSolveBlock;
+            const int m = threadIdx.x + t * TB;
             if (m < q) {
                 const int j = 4 * m;
                 const float2 c = cr2[m];
@@ -437,7 +458,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         for (int l = 0, s = 1; l < levels; ++l, s <<= 1) {
 #pragma unroll
             for (int t = 0; t < Q; ++t) {
-                const int m = threadIdx.x + t * kSolveBlock;
+                const int m = threadIdx.x + t * TB;
                 if (m < q) {
                     const float2 c = pcr[l * q + m];
                     Po[m] = Pi[m] + c.x * Pi[(m - s) & qmask] + c.y * Pi[(m + s) & qmask];
@@ -450,7 +471,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         }
 #pragma unroll
         for (int t = 0; t < Q; ++t) {
-            const int m = threadIdx.x + t * kSolveBlock;
+            const int m = threadIdx.x + t * TB;
             if (m < q) {
                 const float2 c = fin[m];
                 D[4 * m] = c.x * Pi[m] + c.y * Pi[(m + q / 2) & qmask];
@@ -461,7 +482,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
     // step 4 (both paths)
 #pragma unroll
     for (int t = 0; t < Q; ++t) {
-        const int m = threadIdx.x + t * kSolveBlock;
+        const int m = threadIdx.x + t * TB;
         if (m < q) {
             const int j = 4 * m + 2;
             D[j] = g2[m] * D[j] + g2[q + m] * D[j - 2] + g2[2 * q + m] * D[(j + 2) & mask];
@@ -470,7 +491,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
     __syncthreads();
 #pragma unroll
     for (int t = 0; t < H; ++t) {
-        const int m = threadIdx.x + t * kSolveBlock;
+        const int m = threadIdx.x + t * TB;
         if (m < h) {
             const int j = 2 * m + 1;
             D[j] = g1[m] * D[j] + g1[h + m] * D[j - 1] + g1[2 * h + m] * D[(j + 1) & mask];
@@ -482,7 +503,7 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
         // later phases; the blob is the block's resident copy
         float* const dst = f.pcr + (size_t)i * (B.bytes / 4);
         const float4* src = reinterpret_cast<const float4*>(S.blob);
-        for (int k = threadIdx.x; k < B.bytes / 16; k += kSolveBlock)
+        for (int k = threadIdx.x; k < B.bytes / 16; k += TB)
             reinterpret_cast<float4*>(dst)[k] = src[k];
         S.resident = dst;
         // generic writes of both copies before later bulk copies from the
@@ -499,19 +520,20 @@ __device__ __forceinline__ const float* row_blob(const SbGrid& g, const SbFields
 }
 
 // ---------------------------------------------------------------------------
-// Row bodies.  Every thread handles the columns col_of(0 .. PER-1) of a theta
+// Row bodies.  Every thread handles the columns col_of<TB>(0 .. PER-1) of a theta
 // row, one column after the other (measured faster than issuing all loads
 // of a thread's columns first, which costs registers).  Dot-product terms
 // are accumulated in column order.
 
 // dx = 0, r = r0, p_old = 0; rv = r; adds |rhs|^2 to bb.
-template <bool MIXED, int PER>
+template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int i,
                                          float (&rv)[PER], ff& bb) {
     const int nP = g.nP, row = i * nP;
+    ff h[2] = {ff_zero(), ff_zero()};
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         rv[k] = 0.0f;
         if (j < nP) {
             const int c = row + j;
@@ -521,9 +543,10 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
             else f.dx[c] = 0.0f;
             f.r[c] = rv[k];
             f.q[c] = 0.0f;
-            bb = ff_add_prod(bb, rhs, rhs);
+            h[half_of<TB>(k)] = ff_add_prod(h[half_of<TB>(k)], rhs, rhs);
         }
     }
+    bb = fold_halves<TB>(h);
 }
 
 // p_new = z + beta p_old on the row and, on the fly, on the neighbours it
@@ -531,7 +554,7 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
 // is kept in f.x.  Returns the row's p.q.  Every load of a column is issued
 // before its arithmetic, through restrict-qualified pointers so that the
 // compiler may also start the next column's loads early.
-template <bool MIXED, int PER>
+template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i, float beta,
                                        const float* __restrict__ pold, float* __restrict__ pnew) {
     const int nP = g.nP, nT = g.nT, row = i * nP;
@@ -541,7 +564,7 @@ __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i
     const float* __restrict__ cS = f.cS;
     float* __restrict__ qout = f.x;
     const bool hasS = i < nT - 1, hasN = i > 0;
-    ff pq = ff_zero();
+    ff pq[2] = {ff_zero(), ff_zero()};
     // columns in pairs: both columns' loads are issued before either's
     // arithmetic (two L2 round trips per row instead of four at PER = 4)
     constexpr int G2 = PER >= 2 ? 2 : 1;
@@ -552,7 +575,7 @@ __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i
         int cc[G2];
 #pragma unroll
         for (int u = 0; u < G2; ++u) {
-            const int j = col_of(k0 + u);
+            const int j = col_of<TB>(k0 + u);
             const int jj = j < nP ? j : 0;  // rows shorter than the block: a valid dummy
             const int c = row + jj;
             const int e = row + ((jj + 1) & g.maskP);
@@ -568,7 +591,7 @@ __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i
         }
 #pragma unroll
         for (int u = 0; u < G2; ++u) {
-            if (col_of(k0 + u) < nP) {
+            if (col_of<TB>(k0 + u) < nP) {
                 const float pc = zc[u] + beta * pc0[u];
                 float qf = dm[u] * pc + ce[u] * (pc - (ze[u] + beta * pe[u])) +
                            cw[u] * (pc - (zw[u] + beta * pw[u]));
@@ -576,37 +599,38 @@ __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i
                 if (hasN) qf += cn[u] * (pc - (zn[u] + beta * pn[u]));
                 pnew[cc[u]] = pc;
                 qout[cc[u]] = qf;
-                pq = acc<MIXED>(pq, pc, qf);
+                pq[half_of<TB>(k0 + u)] = acc<MIXED>(pq[half_of<TB>(k0 + u)], pc, qf);
             }
         }
     }
-    return pq;
+    return fold_halves<TB>(pq);
 }
 
 // True residual r = r0 - A x of the float-float iterate (mixed mode),
 // carried in float-float; stores it (rounded) in f.r and returns the row's
 // |r|^2.
-template <int PER>
+template <int PER, int TB>
 __device__ __forceinline__ ff row_true_residual(const SbGrid& g, const SbFields& f, int i) {
     const int nP = g.nP, row = i * nP;
-    ff a = ff_zero();
+    ff a[2] = {ff_zero(), ff_zero()};
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         if (j < nP) {
             const int c = row + j;
             const ff r = ff_add_f(ff_neg(apply_A_ff(g, f, f.xff, c, i, j)), f.r0[c]);
             f.r[c] = ff_to_f(r);
             // r^2 = hi^2 + 2 hi lo (+ lo^2, below the float-float precision)
-            a = ff_add_f(ff_add_prod(a, r.hi, r.hi), __fmul_rn(2.0f, __fmul_rn(r.hi, r.lo)));
+            ff& ah = a[half_of<TB>(k)];
+            ah = ff_add_f(ff_add_prod(ah, r.hi, r.hi), __fmul_rn(2.0f, __fmul_rn(r.hi, r.lo)));
         }
     }
-    return a;
+    return fold_halves<TB>(a);
 }
 
 // x += alpha p_new, r -= alpha q; rv = the new r.  Every load of the
 // thread's columns is issued before any arithmetic.
-template <bool MIXED, int PER>
+template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, int i, ff alpha,
                                            const float* __restrict__ pnew, float (&rv)[PER]) {
     const int nP = g.nP, row = i * nP;
@@ -616,7 +640,7 @@ __device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, i
     float2 xc[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         const int c = row + (j < nP ? j : 0);
         pc[k] = pnew[c];
         rc[k] = f.r[c];
@@ -626,7 +650,7 @@ __device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, i
     }
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         rv[k] = 0.0f;
         if (j < nP) {
             const int c = row + j;
@@ -643,24 +667,24 @@ __device__ __forceinline__ void row_update(const SbGrid& g, const SbFields& f, i
 }
 
 // rv = r (restart from the refined iterate's residual).
-template <int PER>
+template <int PER, int TB>
 __device__ __forceinline__ void row_load_r(const SbGrid& g, const SbFields& f, int i,
                                            float (&rv)[PER]) {
     const int nP = g.nP, row = i * nP;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         rv[k] = j < nP ? f.r[row + j] : 0.0f;
     }
 }
 
 // The increment and the new gamma: dx, x = gamma_adv + dx.
-template <bool MIXED, int PER>
+template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_final(const SbGrid& g, const SbFields& f, int i) {
     const int nP = g.nP, row = i * nP;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         if (j < nP) {
             const int c = row + j;
             const float dx = MIXED ? ff_to_f(ld_ff(f.xff, c)) : f.dx[c];
@@ -790,12 +814,25 @@ __device__ __forceinline__ void acc_zero(unsigned long long* a, int n, int tid, 
 // over the block in a fixed order (each lane 8 threads' shares, then the
 // lanes by shuffle tree) and adds the row's partial into the phase's exact
 // accumulator.
+template <int TB>
 __device__ __forceinline__ void reduce_row(const SbSolveSet& S, int b, int p, int vals,
-                                           const ff* tpart) {
+                                           ff* tpart) {
     __syncthreads();
+    if (TB != kVThreads) {
+        // a 512-thread block: virtual thread v's share is its even half
+        // (thread v) plus its odd half (thread v + 256)
+        if (threadIdx.x < kVThreads) {
+#pragma unroll
+            for (int v = 0; v < 3; ++v)
+                if ((vals >> v) & 1)
+                    tpart[v * TB + threadIdx.x] =
+                        ff_add(tpart[v * TB + threadIdx.x], tpart[v * TB + kVThreads + threadIdx.x]);
+        }
+        __syncthreads();
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp < 3 && ((vals >> warp) & 1)) {
-        const ff* t = tpart + warp * kSolveBlock;
+        const ff* t = tpart + warp * TB;
         ff x = ff_zero();
 #pragma unroll
         for (int k = 0; k < kWarps; ++k) x = ff_add(x, t[lane + 32 * k]);
@@ -1001,13 +1038,14 @@ __device__ __forceinline__ unsigned row_weight(int nT) { return 2u * (unsigned)n
 // p (every system in phase 0 and in the final pass, p < 0); s_pre[nb] is the
 // total.  Every block computes the same table: a system's done_at only
 // moves during phase p from INT_MAX to p + 1, which reads as active in p.
+template <int TB>
 __device__ __forceinline__ unsigned active_prefix(const SbSolveSet& S, int p, unsigned* s_pre) {
-    __shared__ unsigned wsum[kSolveBlock / 32];
+    __shared__ unsigned wsum[TB / 32];
     __shared__ unsigned carry;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (int base = 0; base < S.nb; base += kSolveBlock) {
+    for (int base = 0; base < S.nb; base += TB) {
         const int b = base + threadIdx.x;
         unsigned v = 0;
         if (b < S.nb) {
@@ -1026,7 +1064,7 @@ __device__ __forceinline__ unsigned active_prefix(const SbSolveSet& S, int p, un
         for (int k = 0; k < w; ++k) before += wsum[k];
         if (b < S.nb) s_pre[b] = before + incl - v;
         __syncthreads();
-        if (threadIdx.x == kSolveBlock - 1) carry = before + incl;
+        if (threadIdx.x == TB - 1) carry = before + incl;
         __syncthreads();
     }
     const unsigned total = carry;
@@ -1057,41 +1095,45 @@ __device__ __forceinline__ void stage_desc(const SbSolveSet& S, int b, SbBubbleD
 
 // Stores the preconditioner's result D (in the block's work array) as this
 // thread's columns of row i of z1.
-template <int PER>
+template <int PER, int TB>
 __device__ __forceinline__ void store_z1(const SbGrid& g, const SbFields& f, int i,
                                          const Stage& St) {
     const int row = i * g.nP;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         if (j < g.nP) f.z1[row + j] = St.work[j];
     }
 }
 
 // Stores the preconditioner's result D as this thread's columns of row i
 // of z and adds the columns' r.z and r.r terms (column order).
-template <bool MIXED, int PER>
+template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void store_z_dots(const SbGrid& g, const SbFields& f, int i,
                                              const Stage& St, const float (&rv)[PER], ff& a,
                                              ff& b2) {
     const int row = i * g.nP;
+    ff ha[2] = {ff_zero(), ff_zero()}, hb[2] = {ff_zero(), ff_zero()};
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         if (j < g.nP) {
             const float z = St.work[j];
             f.z[row + j] = z;
-            a = acc<MIXED>(a, rv[k], z);
-            b2 = acc<MIXED>(b2, rv[k], rv[k]);
+            const int hk = half_of<TB>(k);
+            ha[hk] = acc<MIXED>(ha[hk], rv[k], z);
+            hb[hk] = acc<MIXED>(hb[hk], rv[k], rv[k]);
         }
     }
+    a = fold_halves<TB>(ha);
+    b2 = fold_halves<TB>(hb);
 }
 
 // w = C z1 on row i: the theta couplings (weights cS of the faces north and
 // south of each cell) applied to the neighbouring rows of z1; z1 and r of
 // the row itself are returned in zo and ro (loaded with the rest, before
 // the row solve that w feeds).
-template <int PER>
+template <int PER, int TB>
 __device__ __forceinline__ void row_theta_coupling(const SbGrid& g, const SbFields& f, int i,
                                                    float (&w)[PER], float (&zo)[PER],
                                                    float (&ro)[PER]) {
@@ -1101,7 +1143,7 @@ __device__ __forceinline__ void row_theta_coupling(const SbGrid& g, const SbFiel
     const float* __restrict__ r = f.r;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int j = col_of(k);
+        const int j = col_of<TB>(k);
         w[k] = 0.0f;
         zo[k] = 0.0f;
         ro[k] = 0.0f;
@@ -1127,7 +1169,7 @@ __device__ __forceinline__ void row_theta_coupling(const SbGrid& g, const SbFiel
 // of one more phase per iteration.  Each thread's shares of the row's dot
 // products go to the block's work arrays (after the preconditioner's D)
 // for reduce_row.
-template <bool MIXED, int PER>
+template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
                                           const SolverConfig& cfg, int i, int kind,
                                           float beta, ff alpha, float* pA, const float* pB,
@@ -1138,59 +1180,63 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
     switch (kind) {
         case K_SETUP:
         case K_SETUP_L:
-            row_init<MIXED, PER>(g, f, i, rv, c2);
-            precondition_row<PER, true>(g, f, i, St, rv);
+            row_init<MIXED, PER, TB>(g, f, i, rv, c2);
+            precondition_row<PER, TB, true>(g, f, i, St, rv);
             break;
         case K_NEUMANN: {
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
             float z1v[PER], r0v[PER];
-            row_theta_coupling<PER>(g, f, i, rv, z1v, r0v);
-            precondition_row<PER, false>(g, f, i, St, rv);
+            row_theta_coupling<PER, TB>(g, f, i, rv, z1v, r0v);
+            precondition_row<PER, TB, false>(g, f, i, St, rv);
             const int row = i * g.nP;
+            ff ha[2] = {ff_zero(), ff_zero()}, hb[2] = {ff_zero(), ff_zero()};
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
-                const int j = col_of(k);
+                const int j = col_of<TB>(k);
                 if (j < g.nP) {
                     const int c = row + j;
                     const float z = z1v[k] + St.work[j];
                     const float r = r0v[k];
                     f.z[c] = z;
-                    a = acc<MIXED>(a, r, z);
-                    b2 = acc<MIXED>(b2, r, r);
+                    const int hk = half_of<TB>(k);
+                    ha[hk] = acc<MIXED>(ha[hk], r, z);
+                    hb[hk] = acc<MIXED>(hb[hk], r, r);
                 }
             }
+            a = fold_halves<TB>(ha);
+            b2 = fold_halves<TB>(hb);
             break;
         }
         case K_Q:
-            a = row_spmv<MIXED, PER>(g, f, i, beta, pB, pA);
+            a = row_spmv<MIXED, PER, TB>(g, f, i, beta, pB, pA);
             break;
         case K_UPDATE:
         case K_UPDATE_L:
             // the row's factors travel while the update runs
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
-            row_update<MIXED, PER>(g, f, i, alpha, pA, rv);
-            precondition_row<PER, false>(g, f, i, St, rv);
+            row_update<MIXED, PER, TB>(g, f, i, alpha, pA, rv);
+            precondition_row<PER, TB, false>(g, f, i, St, rv);
             break;
         case K_CHECK:
-            if (MIXED) a = row_true_residual<PER>(g, f, i);
+            if (MIXED) a = row_true_residual<PER, TB>(g, f, i);
             break;
         default:  // K_RESTART, K_RESTART_L
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
-            row_load_r<PER>(g, f, i, rv);
-            precondition_row<PER, false>(g, f, i, St, rv);
+            row_load_r<PER, TB>(g, f, i, rv);
+            precondition_row<PER, TB, false>(g, f, i, St, rv);
             break;
     }
     // the line-preconditioner kinds (_L, the last three) store z = B^-1 r and
     // its dot products where the Neumann kinds store z1 = B^-1 r
-    if (kind >= K_SETUP_L) store_z_dots<MIXED, PER>(g, f, i, St, rv, a, b2);
-    else if (kind == K_SETUP || kind == K_UPDATE || kind == K_RESTART) store_z1<PER>(g, f, i, St);
+    if (kind >= K_SETUP_L) store_z_dots<MIXED, PER, TB>(g, f, i, St, rv, a, b2);
+    else if (kind == K_SETUP || kind == K_UPDATE || kind == K_RESTART) store_z1<PER, TB>(g, f, i, St);
     // this thread's shares of the values the kind produces, for reduce_row
     // (after D: the other threads may still read their D entries)
     const int vals = kind_values(kind);
     ff* tpart = reinterpret_cast<ff*>(St.work + g.nP);
     if (vals & 1) tpart[threadIdx.x] = a;
-    if (vals & 2) tpart[kSolveBlock + threadIdx.x] = b2;
-    if (vals & 4) tpart[2 * kSolveBlock + threadIdx.x] = c2;
+    if (vals & 2) tpart[TB + threadIdx.x] = b2;
+    if (vals & 4) tpart[2 * TB + threadIdx.x] = c2;
 }
 
 // The solve of a set of systems: each system runs the phase kinds of its
@@ -1203,8 +1249,8 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
 // partials into the system's exact accumulator and counts the rows; the
 // block that completes a system reads the sums and advances it.  The loop
 // ends when no system is left.
-template <bool MIXED, int PER>
-__global__ void __launch_bounds__(kSolveBlock, 4)
+template <bool MIXED, int PER, int TB>
+__global__ void __launch_bounds__(TB, 1024 / TB)
 k_solve(SbSolveSet S, SolverConfig cfg) {
     extern __shared__ __align__(16) float sm[];
     __shared__ __align__(8) uint64_t bar;
@@ -1223,7 +1269,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     const unsigned G = gridDim.x;
 
     for (int p = 0;; ++p) {
-        const unsigned W = active_prefix(S, p, s_pre);
+        const unsigned W = active_prefix<TB>(S, p, s_pre);
         if (W == 0) break;  // same in every block
         const unsigned lo = (unsigned)(((unsigned long long)W * blockIdx.x) / G);
         const unsigned hi = (unsigned)(((unsigned long long)W * (blockIdx.x + 1)) / G);
@@ -1269,8 +1315,8 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
             bool last = false;
             for (int i = i0; i < i1; ++i) {
                 const int k = (i - i0) % kRowChunk;
-                row_phase<MIXED, PER>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
-                if (vals) reduce_row(S, b, p, vals, reinterpret_cast<const ff*>(St.work + g.nP));
+                row_phase<MIXED, PER, TB>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
+                if (vals) reduce_row<TB>(S, b, p, vals, reinterpret_cast<ff*>(St.work + g.nP));
                 // count every kRowChunk rows and at the end; the block that
                 // completes the system advances it
                 if (k == kRowChunk - 1 || i == i1 - 1) last = count_rows(S, b, nT, k + 1, &s_last);
@@ -1289,7 +1335,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
     }
     // the increment and the new gamma of every system, same split with all
     // systems counted
-    const unsigned W = active_prefix(S, -1, s_pre);
+    const unsigned W = active_prefix<TB>(S, -1, s_pre);
     const unsigned lo = (unsigned)(((unsigned long long)W * blockIdx.x) / G);
     const unsigned hi = (unsigned)(((unsigned long long)W * (blockIdx.x + 1)) / G);
     for (int b = first_system_after(s_pre, S.nb, lo); b < S.nb && s_pre[b] < hi; ++b) {
@@ -1300,7 +1346,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
         const int i1 = min(nT, (int)((hi - w0 + wr - 1) / wr));
         if (i0 >= i1) continue;
         stage_desc(S, b, &s_d);
-        for (int i = i0; i < i1; ++i) row_final<MIXED, PER>(s_d.g, s_d.f, i);
+        for (int i = i0; i < i1; ++i) row_final<MIXED, PER, TB>(s_d.g, s_d.f, i);
         __syncthreads();
     }
 }
@@ -1313,8 +1359,8 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
 // result, are bit-identical to solving the same system inside a set (this
 // file is compiled without multiply-add contraction, so both kernels round
 // the same operations the same way).
-template <bool MIXED, int PER>
-__global__ void __launch_bounds__(kSolveBlock, 4)
+template <bool MIXED, int PER, int TB>
+__global__ void __launch_bounds__(TB, 1024 / TB)
 k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     extern __shared__ __align__(16) float sm[];
     __shared__ __align__(8) uint64_t bar;
@@ -1351,8 +1397,8 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
         float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
         float* pB = (it & 1) ? f.p : f.q;  // p_old
         for (int i = blockIdx.x; i < nT; i += G) {
-            row_phase<MIXED, PER>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
-            if (vals) reduce_row(S, 0, p, vals, reinterpret_cast<const ff*>(St.work + g.nP));
+            row_phase<MIXED, PER, TB>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
+            if (vals) reduce_row<TB>(S, 0, p, vals, reinterpret_cast<ff*>(St.work + g.nP));
         }
         if (!grid_barrier(S.bar, gen, G, &f.stats->wait_faults)) {
             stage_wait(St, f.stats);  // no copy may land after the block left
@@ -1362,26 +1408,26 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     // every block has read its last sums: clear the buffers for the next solve
     if (!grid_barrier(S.bar, gen, G, &f.stats->wait_faults)) return;
     if (blockIdx.x == 0) acc_zero(S.acc, kSolveAccWords, threadIdx.x, blockDim.x);
-    for (int i = blockIdx.x; i < nT; i += G) row_final<MIXED, PER>(g, f, i);
+    for (int i = blockIdx.x; i < nT; i += G) row_final<MIXED, PER, TB>(g, f, i);
 }
 
 template <bool MIXED>
 const void* solve_one_kernel(int per) {
     switch (per) {
-        case 1: return (const void*)k_solve_one<MIXED, 1>;
-        case 2: return (const void*)k_solve_one<MIXED, 2>;
-        case 4: return (const void*)k_solve_one<MIXED, 4>;
-        default: return (const void*)k_solve_one<MIXED, 8>;
+        case 1: return (const void*)k_solve_one<MIXED, 1, 256>;
+        case 2: return (const void*)k_solve_one<MIXED, 2, 256>;
+        case 4: return (const void*)k_solve_one<MIXED, 4, 256>;
+        default: return (const void*)k_solve_one<MIXED, 4, 512>;  // rows of 2048 columns
     }
 }
 
 template <bool MIXED>
 const void* solve_kernel(int per) {
     switch (per) {
-        case 1: return (const void*)k_solve<MIXED, 1>;
-        case 2: return (const void*)k_solve<MIXED, 2>;
-        case 4: return (const void*)k_solve<MIXED, 4>;
-        default: return (const void*)k_solve<MIXED, 8>;
+        case 1: return (const void*)k_solve<MIXED, 1, 256>;
+        case 2: return (const void*)k_solve<MIXED, 2, 256>;
+        case 4: return (const void*)k_solve<MIXED, 4, 256>;
+        default: return (const void*)k_solve<MIXED, 4, 512>;  // rows of 2048 columns
     }
 }
 
@@ -1390,21 +1436,26 @@ float tol2_factor(const SolverConfig& cfg) {
     return (float)((cfg.mode == 1 ? 0.64 : 1.0) * cfg.tol * cfg.tol);
 }
 
+// Kernel variant of rows of up to nP columns: 1, 2, 4 columns per thread
+// of 256-thread blocks, or 8 for 2048 columns (512-thread blocks, four
+// columns per thread).
 int per_of(int nP) {
-    int per = (nP + kSolveBlock - 1) / kSolveBlock;
+    int per = (nP + kVThreads - 1) / kVThreads;
     return per <= 1 ? 1 : per <= 2 ? 2 : per <= 4 ? 4 : 8;
 }
+
+int threads_of(int per) { return per == 8 ? 512 : kVThreads; }
 
 // Dynamic shared memory of one solve block for rows of up to nP columns:
 // the factor blob of one row and the work arrays: the four nP-float arrays
 // of the preconditioner build (the replay needs 1.5 nP floats), which also
 // hold the result D (nP floats) followed by the threads' dot-product shares
-// (3 x 256 float-float).  For
+// (3 x threads float-float).  For
 // nP = 1024 that is 47 KB, so four 256-thread blocks share an SM next to
 // their static shared memory.
 size_t solve_smem(int nP) {
-    const size_t work =
-        std::max<size_t>(16 * (size_t)nP, 4 * (size_t)nP + 3 * kSolveBlock * sizeof(ff));
+    const size_t tb = (size_t)threads_of(per_of(nP));
+    const size_t work = std::max<size_t>(16 * (size_t)nP, 4 * (size_t)nP + 3 * tb * sizeof(ff));
     return (size_t)factor_blob(nP).bytes + work;
 }
 
@@ -1417,7 +1468,7 @@ const void* kernel_for(int per, int mode, bool one) {
 // serve rows of up to PER * 256 columns; smaller rows need less).
 size_t variant_smem(int per) {
     size_t m = 0;
-    for (int nP = 16; nP <= per * kSolveBlock; nP *= 2)
+    for (int nP = 16; nP <= per * kVThreads; nP *= 2)
         if (per_of(nP) == per) m = std::max(m, solve_smem(nP));
     return m;
 }
@@ -1438,7 +1489,7 @@ int max_blocks(int per, int mode, bool one) {
     int sms = 0, occ = 0;
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolveBlock, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads_of(per), smem);
     c = sms * (occ > 0 ? occ : 1);
     return c;
 }
@@ -1446,7 +1497,7 @@ int max_blocks(int per, int mode, bool one) {
 }  // namespace
 
 cudaError_t prepare_solve(int maxNP, const SolverConfig& cfg, int* blocks) {
-    if (maxNP > 8 * kSolveBlock) return cudaErrorInvalidValue;
+    if (maxNP > kMaxNP) return cudaErrorInvalidValue;
     const int b = max_blocks(per_of(maxNP), cfg.mode, false);
     max_blocks(per_of(maxNP), cfg.mode, true);
     if (blocks) *blocks = b;
@@ -1455,7 +1506,7 @@ cudaError_t prepare_solve(int maxNP, const SolverConfig& cfg, int* blocks) {
 
 cudaError_t launch_solve_one(const SbGrid& g, const SbFields& f, const SbSolveSet& set,
                              const SolverConfig& cfg, cudaStream_t s) {
-    if (g.nP > 8 * kSolveBlock || set.nb != 1) return cudaErrorInvalidValue;
+    if (g.nP > kMaxNP || set.nb != 1) return cudaErrorInvalidValue;
     const int per = per_of(g.nP);
     const int G = std::min(g.nT, max_blocks(per, cfg.mode, true));
     SbGrid gg = g;
@@ -1465,13 +1516,13 @@ cudaError_t launch_solve_one(const SbGrid& g, const SbFields& f, const SbSolveSe
     cc.blob = factor_blob(g.nP).bytes;
     cc.tol2f = tol2_factor(cfg);
     void* args[] = {&gg, &ff, &ss, &cc};
-    return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, true), dim3(G), dim3(kSolveBlock),
+    return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, true), dim3(G), dim3(threads_of(per)),
                                        args, solve_smem(g.nP), s);
 }
 
 cudaError_t launch_solve(const SbSolveSet& set, int maxNP, const SolverConfig& cfg,
                          cudaStream_t s) {
-    if (maxNP > 8 * kSolveBlock || set.R <= 0) return cudaErrorInvalidValue;
+    if (maxNP > kMaxNP || set.R <= 0) return cudaErrorInvalidValue;
     const int per = per_of(maxNP);
     const int G = std::min(set.R, max_blocks(per, cfg.mode, false));
     SbSolveSet ss = set;
@@ -1479,7 +1530,7 @@ cudaError_t launch_solve(const SbSolveSet& set, int maxNP, const SolverConfig& c
     cc.blob = factor_blob(maxNP).bytes;
     cc.tol2f = tol2_factor(cfg);
     void* args[] = {&ss, &cc};
-    return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, false), dim3(G), dim3(kSolveBlock),
+    return cudaLaunchCooperativeKernel(kernel_for(per, cfg.mode, false), dim3(G), dim3(threads_of(per)),
                                        args, solve_smem(maxNP), s);
 }
 

@@ -194,3 +194,28 @@ def test_batch_rejects_mixed_viscous_switch(gpulib):
             GpuBatch([a, b])
     finally:
         _close([a, b])
+
+
+def test_wide_rows_batch_matches_members_stepped_alone(gpulib):
+    """A set whose widest rows have 2048 columns runs the solve with
+    512-thread blocks; its smaller members still match themselves stepped
+    alone (256-thread blocks) bit for bit: the dot products are formed in an
+    order that does not depend on the block width."""
+    from soapbubble_gb300.bubble import GpuBatch
+    specs = [(1024, 21, "c2", 0.001, (1.0, 1.0, 1.0)), (64, 22, "c0", 0.001, (1.2, 0.8, 1.1)),
+             (256, 23, "c1", 0.001, (0.9, 1.1, 1.0)), (512, 24, "c1", 0.001, (1.0, 1.0, 1.0))]
+    a, b = _twins(specs, solver_tol=1e-6)
+    try:
+        with GpuBatch(a) as batch:
+            for t, dt in _schedule(4, 0.001):
+                batch.step(1, t, dt)
+                for g in b:
+                    g.step(1, t, dt)
+            batch.synchronize()
+        for ga, gb in zip(a, b):
+            for name in ("eta", "gamma", "u_theta", "u_phi", "eta_delta", "fwd_t"):
+                np.testing.assert_array_equal(ga.download(name), gb.download(name),
+                                              err_msg=f"nT={ga.nTheta} {name}")
+            assert ga.stats().solver_iters == gb.stats().solver_iters
+    finally:
+        _close(a + b)
