@@ -150,6 +150,7 @@ class Server:
         id to its fields.  Returns the results in request order."""
         pending = list(requests)
         waiting: List[Request] = []
+        ready: List[Active] = []  # made while the GPU ran a frame, not yet in the set
         active: List[Active] = []
         results: Dict[int, Result] = {}
         batch: Optional[GpuBatch] = None
@@ -162,26 +163,37 @@ class Server:
         def now():
             return time.perf_counter() - t_start
 
+        def make_ready(in_use: bool) -> None:
+            """Creates and fills the bubbles of waiting requests, first come
+            first served, while they fit the budget (the first always does
+            when nothing else is resident)."""
+            while pending and pending[0].arrival <= now():
+                waiting.append(pending.pop(0))
+            while waiting:
+                req = waiting[0]
+                need = bytes_required(params_of(req, device=self.device))
+                if self.resident_bytes + need > self.budget and (in_use or ready):
+                    break
+                waiting.pop(0)
+                f = payloads[req.rid]
+                g = GpuBubble(params_of(req, device=self.device))
+                g.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+                ready.append(Active(req, g, 0, np.empty(g.nTheta * g.nPhi, dtype=np.float32)))
+                self.resident_bytes += need
+
         try:
-            while pending or waiting or active:
-                tnow = now()
-                while pending and pending[0].arrival <= tnow:
-                    waiting.append(pending.pop(0))
-                # admission at frame boundaries, first come first served
+            while pending or waiting or ready or active:
+                # admission at frame boundaries, first come first served: the
+                # bubbles made during the last frame join, then any other
+                # waiting request that fits
                 if g_step % STEPS_PER_FRAME == 0:
-                    while waiting:
-                        req = waiting[0]
-                        need = bytes_required(params_of(req, device=self.device))
-                        if self.resident_bytes + need > self.budget and active:
-                            break
-                        waiting.pop(0)
-                        f = payloads[req.rid]
-                        g = GpuBubble(params_of(req, device=self.device))
-                        g.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
-                        active.append(Active(req, g, 0, np.empty(g.nTheta * g.nPhi,
-                                                                 dtype=np.float32)))
-                        self.resident_bytes += need
-                        admitted_at[req.rid] = now()
+                    make_ready(bool(active))
+                    for a in ready:
+                        admitted_at[a.req.rid] = now()
+                        a.bubble.synchronize()  # its fields are in place
+                    if ready:
+                        active.extend(ready)
+                        ready.clear()
                         changed = True
                 if not active:
                     g_step = 0  # idle: the frame grid restarts with the next admission
@@ -203,6 +215,9 @@ class Server:
                 for a in active:
                     a.done += n
                     cell_steps += n * a.bubble.nTheta * a.bubble.nPhi
+                if g_step % STEPS_PER_FRAME == 0:
+                    # the next admission's bubbles are made while the GPU runs
+                    make_ready(True)
                 batch.synchronize()
                 finished = []
                 for a in active:
@@ -232,7 +247,7 @@ class Server:
         finally:
             if batch is not None:
                 batch.close()
-            for a in active:
+            for a in active + ready:
                 a.bubble.close()
         self.wall = now()
         self.cell_steps = cell_steps
