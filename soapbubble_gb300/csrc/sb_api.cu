@@ -9,7 +9,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/soapbubble.h"
@@ -146,6 +150,38 @@ double corridor(double radius, double gTheta, double gPhi, bool phiComponent) {
     const double s = 0.5 * std::sin(beta) / 1.0 * radius * (1. - ss);
     if (phiComponent) return s * (pw[0] * -sP + pw[1] * cP);
     return s * (pw[0] * cT * cP + pw[1] * cT * sP - pw[2] * sT);
+}
+
+// The corridor factors of every face of a grid (u_phi faces, then u_theta
+// faces).  They depend on the grid and the radius only, and computing them
+// in FP64 costs about 0.2 s at 512 x 1024, so they are made once per
+// (nTheta, radius) and shared by later bubbles (a serving loop creates many
+// bubbles of few sizes); at most 16 grids are kept.
+struct Corridor {
+    std::vector<float> u, v;
+};
+
+std::shared_ptr<const Corridor> corridor_factors(int nT, double radius) {
+    static std::mutex mu;
+    static std::map<std::pair<int, double>, std::shared_ptr<const Corridor>> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(nT, radius);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    const int nP = 2 * nT;
+    const double h = kPi / nT;
+    auto c = std::make_shared<Corridor>();
+    c->u.resize((size_t)nT * nP);
+    c->v.resize((size_t)(nT - 1) * nP);
+    for (int i = 0; i < nT; ++i)
+        for (int j = 0; j < nP; ++j) {
+            c->u[(size_t)i * nP + j] = (float)corridor(radius, (i + 0.5) * h, (j - 0.5) * h, true);
+            if (i < nT - 1)
+                c->v[(size_t)i * nP + j] = (float)corridor(radius, (i + 1.0) * h, j * h, false);
+        }
+    if (cache.size() >= 16) cache.clear();
+    cache.emplace(key, c);
+    return c;
 }
 
 struct ArenaPlan {
@@ -522,18 +558,9 @@ int sb_create(const sb_params* p, sb_bubble** out) {
 
     // static corridor factors
     {
-        std::vector<float> cu((size_t)g.N), cv((size_t)g.Nv);
-        for (int i = 0; i < g.nT; ++i)
-            for (int j = 0; j < g.nP; ++j) {
-                double v = corridor(p->radius, (i + 0.5) * h, (j - 0.5) * h, true);
-                cu[(size_t)i * g.nP + j] = (float)v;
-                if (i < g.nT - 1) {
-                    double w = corridor(p->radius, (i + 1.0) * h, j * h, false);
-                    cv[(size_t)i * g.nP + j] = (float)w;
-                }
-            }
-        e = cudaMemcpy(f.corr_u, cu.data(), cu.size() * 4, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(f.corr_v, cv.data(), cv.size() * 4, cudaMemcpyHostToDevice);
+        const std::shared_ptr<const Corridor> c = corridor_factors(g.nT, p->radius);
+        e = cudaMemcpy(f.corr_u, c->u.data(), c->u.size() * 4, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(f.corr_v, c->v.data(), c->v.size() * 4, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) { int r = cuda_fail(e, "corridor"); sb_destroy(b); return r; }
     }
     // Solver::Solver initial state: eta = 0.5, gamma = 1, u = 0, no wind
