@@ -1,6 +1,6 @@
 """GPU parity: one CUDA step against the FP64 oracle on identical inputs.
 
-Tolerance (the benchmark spec): the thickness, surfactant and both velocity
+Tolerance: the thickness, surfactant and both velocity
 components match the FP64 oracle to <= 1e-5 normwise relative error
 (max |gpu - oracle| / max |oracle|) per step.  The BIMOCQ accumulators
 (delta buffers) are small differences of O(1) fields and are checked at
