@@ -190,7 +190,7 @@ struct ArenaPlan {
     size_t bim[8];
     size_t fwd[2], bwd[2], bwdprev;
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
-    size_t div, d_eta, d_gam, err_eta, err_gam;
+    size_t d_eta, d_gam, err_eta, err_gam;
     size_t dmass, cE, cS, rhs, r0, x, dx, r, z, z1, p, q, xff, pcr, pcr_levels, step, stats;
     size_t self, self_list, roff, done_at, cnt, rec, acc, bar;  // the bubble's solve set
     size_t tiles[3];                                           // its cell tiles
@@ -216,7 +216,7 @@ ArenaPlan plan_arena(const SbGrid& g, int storage) {
     a.uair_init = a.L.take(N * F); a.vair_init = a.L.take(Nv * F);
     a.corr_u = a.L.take(N * F); a.corr_v = a.L.take(Nv * F);
     a.uair = a.L.take((N + 1) * F); a.vair = a.L.take((Nv + 1) * F);
-    a.div = a.L.take(N * F); a.d_eta = a.L.take(N * F); a.d_gam = a.L.take(N * F);
+    a.d_eta = a.L.take(N * F); a.d_gam = a.L.take(N * F);
     a.err_eta = a.L.take(N * F); a.err_gam = a.L.take(N * F);
     a.dmass = a.L.take(N * F); a.cE = a.L.take(N * F); a.cS = a.L.take(N * F);
     a.rhs = a.L.take(N * F); a.r0 = a.L.take(N * F); a.x = a.L.take(N * F); a.dx = a.L.take(N * F);
@@ -510,7 +510,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.uair_init = F32(a.uair_init); f.vair_init = F32(a.vair_init);
     f.corr_u = F32(a.corr_u); f.corr_v = F32(a.corr_v);
     f.uair = F32(a.uair); f.vair = F32(a.vair);
-    f.div = F32(a.div); f.d_eta = F32(a.d_eta); f.d_gam = F32(a.d_gam);
+    f.d_eta = F32(a.d_eta); f.d_gam = F32(a.d_gam);
     f.err_eta = F32(a.err_eta); f.err_gam = F32(a.err_gam);
     f.dmass = F32(a.dmass); f.cE = F32(a.cE); f.cS = F32(a.cS); f.rhs = F32(a.rhs); f.r0 = F32(a.r0);
     f.x = F32(a.x); f.dx = F32(a.dx); f.r = F32(a.r); f.z = F32(a.z); f.z1 = F32(a.z1);

@@ -56,7 +56,7 @@ struct SbFields {
     float2 *fwd[2], *bwd[2], *bwdprev;             // map offsets (ping-pong)
     float *uair_init, *vair_init, *corr_u, *corr_v;
     float *uair, *vair;                            // N+1, Nv+1 (last element 0)
-    float *div, *d_eta, *d_gam, *err_eta, *err_gam;
+    float *d_eta, *d_gam, *err_eta, *err_gam;  // per-step increments, re-initialisation errors
     // implicit system for the increment dx = gamma_new - gamma_adv:
     // (A dx)_c = dmass_c dx_c + sum_n w_cn (dx_c - dx_n), weights w > 0 to
     // the east (cE) and south (cS) neighbours; r = b - A gamma_adv formed
