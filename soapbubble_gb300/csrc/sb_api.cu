@@ -308,8 +308,7 @@ int write_step_params(sb_bubble* b, double t, double dt_s, cudaStream_t stream) 
     s->mixA = (float)(t / 12.0);
     s->mixB = (float)(1.0 - t / 12.0);
     s->evapDt = (float)((double)b->ph.evap * dtn);
-    s->gsdt = 0.f;
-    s->pad = 0.f;
+    s->pad[0] = s->pad[1] = 0.f;
     SB_CHECK(cudaMemcpyAsync(b->f.step, s, sizeof(SbStepParams), cudaMemcpyHostToDevice, stream));
     b->last_dt = dt_s;
     b->last_t = t;

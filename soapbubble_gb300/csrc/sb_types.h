@@ -25,8 +25,7 @@ struct SbStepParams {
     float mixA;     // t / 12 (mirrored wind mix, kernel/bubble.cu:1360-1392)
     float mixB;     // 1 - t / 12
     float evapDt;   // evaporationRate * dt
-    float gsdt;     // unused scratch
-    float pad;
+    float pad[2];   // the struct stays 32 bytes
 };
 
 // Storage of the thickness and surfactant fields (the values of
