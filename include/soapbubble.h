@@ -231,7 +231,12 @@ int sb_stage_upload_f32(sb_bubble* b, sb_field which, const float* src, size_t n
 int sb_stage_download_f32(sb_bubble* b, sb_field which, float* dst, size_t n);
 int sb_wait_staged(sb_bubble* b);
 
-/* Statistics of the last step (synchronises). */
+/* Statistics of the last step (synchronises).  Returns SB_ERR_CUDA (stats
+ * still filled) once a bounded wait inside a kernel has given up (a grid
+ * barrier of the implicit solve or the re-initialisation, or a
+ * shared-memory copy): the step kernels never wait without a limit, and
+ * after such a fault the bubble's cooperative kernels return at once, so
+ * its fields stop changing. */
 int sb_get_stats(sb_bubble* b, sb_stats* out);
 
 /* Computes the mass integrals into the stats (synchronises). */
