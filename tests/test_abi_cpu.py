@@ -67,3 +67,22 @@ def test_config_reader(tmp_path):
     c = read_config(str(cfg))
     assert c["nTheta"] == 256 and c["frames"] == 500 and c["thicknessImage"] == ""
     assert c["outputDir"] == "../out/test" and c["blendCoeff"] == 0.5 and c["device"] == 0
+
+
+@pytest.mark.parametrize("field,value,msg", [
+    ("nTheta", 100, "power of two"), ("nTheta", 2048, "power of two"),
+    ("radius", -1.0, "positive"), ("dt", 0.0, "timePerStep"),
+    ("storage", 5, "storage"), ("solver_precond", 3, "solver_precond")])
+def test_invalid_params_are_rejected_before_any_device_work(gpulib, field, value, msg):
+    """sb_create validates its parameters first: a bad configuration is an
+    SB_ERR_INVALID with a message, on any machine."""
+    import ctypes as C
+    from soapbubble_gb300._lib import SB_ERR_INVALID
+    from soapbubble_gb300.bubble import make_params
+    p = make_params(64, 0.005)
+    setattr(p, field, value)
+    h = C.c_void_p()
+    L = gpulib.lib()
+    assert L.sb_create(C.byref(p), C.byref(h)) == SB_ERR_INVALID
+    assert not h.value
+    assert msg in L.sb_last_error().decode()
