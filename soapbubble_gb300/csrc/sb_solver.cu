@@ -16,13 +16,14 @@
 // distributed or in which order blocks add: a bubble solved alone and
 // inside a batch gives bit-identical results.
 //
-// Preconditioner: a two-term Neumann series M^-1 = B^-1 + B^-1 C B^-1 of the
-// splitting A = B - C, B the exact solve of each theta row's periodic
+// Preconditioner: B^-1, the exact solve of each theta row's periodic
 // tridiagonal block (phi couplings; the theta couplings stay on its
-// diagonal), C the theta couplings.  Near the poles the phi couplings carry
-// 1/sin(theta) and dominate the diagonal by 1e4-1e5, which is what makes
-// point Jacobi slow there; where the film has ruptured the theta couplings
-// matter too, and the second term halves the iterations.  The row solve is
+// diagonal), or the two-term Neumann series M^-1 = B^-1 + B^-1 C B^-1 of
+// the splitting A = B - C, C the theta couplings, chosen per solve (see
+// first_kind).  Near the poles the phi couplings carry 1/sin(theta) and
+// dominate the diagonal by 1e4-1e5, which is what makes point Jacobi slow
+// there; where the film has ruptured the theta couplings matter too, and
+// the second term halves the iterations.  The row solve is
 // cyclic / parallel cyclic reduction in shared memory, written in "excess"
 // form: each equation keeps (excess e, |lower|, |upper|, rhs) with
 // diagonal = e + |lower| + |upper|, and every update adds positive terms,
@@ -30,8 +31,11 @@
 // off-diagonal sum by a factor 1 + 1e-5 (the Grassmann-Taksar-Heyman idea
 // applied to cyclic reduction).
 //
-// Phases of one CG iteration (each ends at a grid barrier): q = A p; the
-// update of x and r with z1 = B^-1 r; z = z1 + B^-1 C z1 with r.z and r.r.
+// Phases of one CG iteration (each ends at a grid barrier, sb_sync.cuh):
+// q = A p; the update of x and r with z = B^-1 r and r.z, r.r (B^-1 alone),
+// or with z1 = B^-1 r followed by a phase forming z = z1 + B^-1 C z1 with
+// r.z and r.r (Neumann term).  Rows of up to 1024 columns run in 256-thread
+// blocks, rows of 2048 columns in 512-thread blocks (see kVThreads).
 //
 // Modes: plain FP32 (FP32 iterate, float products), or mixed precision
 // (FP32 SpMV and preconditioner, float-float iterate, exact products in the
