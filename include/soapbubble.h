@@ -265,7 +265,10 @@ int sb_write_exr_gray(const char* path, int width, int height, const float* img)
 /* Replaces Bubble::run (kernel/bubble.cu:2607-2704): the frame loop with
  * full steps, a fractional last step per frame, and frame%04d.exr output
  * (plus vel%04d.exr / con%04d.exr when the params ask for them) into
- * out_dir (NULL: no output).  frames <= 0 uses p->frames. */
+ * out_dir (NULL: no output).  frames <= 0 uses p->frames.  The stop on a
+ * broken film (SB_ERR_BROKEN: no cell of positive thickness) is decided
+ * while a thickness frame is written, as in the reference, so a run
+ * without output does not stop on it. */
 int sb_run(sb_bubble* b, const char* out_dir, int frames);
 
 /* No counterpart in the reference.  The two mass integrals of
