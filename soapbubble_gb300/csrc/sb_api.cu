@@ -1299,15 +1299,17 @@ extern "C" {
 int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     if (!out || !bubbles || n <= 0) return fail(SB_ERR_INVALID, "bad batch arguments");
     *out = nullptr;
+    for (int k = 0; k < n; ++k)
+        if (!bubbles[k]) return fail(SB_ERR_INVALID, "batch members must be valid bubbles on one device");
     sb_batch* B = new sb_batch();
     B->device = bubbles[0]->device;
     SbStepPlan& P = B->plan;
     P.solver = bubbles[0]->solver;
     P.storage = bubbles[0]->storage;
-    P.viscous = bubbles[0] ? bubbles[0]->ph.viscous : 0;
+    P.viscous = bubbles[0]->ph.viscous;
     for (int k = 0; k < n; ++k) {
         sb_bubble* b = bubbles[k];
-        if (!b || b->device != B->device) {
+        if (b->device != B->device) {
             delete B;
             return fail(SB_ERR_INVALID, "batch members must be valid bubbles on one device");
         }

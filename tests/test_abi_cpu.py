@@ -87,3 +87,24 @@ def test_invalid_params_are_rejected_before_any_device_work(gpulib, field, value
     assert L.sb_create(C.byref(p), C.byref(h)) == SB_ERR_INVALID
     assert not h.value
     assert msg in L.sb_last_error().decode()
+
+
+def test_null_handles_and_members_are_rejected(gpulib):
+    """Entry points check their handles before any device work: a null
+    bubble, or a batch with a null member or no members, is an
+    SB_ERR_INVALID with a message, on any machine."""
+    import ctypes as C
+    from soapbubble_gb300._lib import SB_ERR_INVALID
+    L = gpulib.lib()
+    out = C.c_void_p()
+    for members in ([None], [None, None]):
+        arr = (C.c_void_p * len(members))(*members)
+        assert L.sb_batch_create(arr, len(members), C.byref(out)) == SB_ERR_INVALID
+        assert not out.value
+        assert "valid bubbles" in L.sb_last_error().decode()
+    arr = (C.c_void_p * 1)(None)
+    assert L.sb_batch_create(arr, 0, C.byref(out)) == SB_ERR_INVALID
+    assert L.sb_step(None, 1, 0.0, 0.005) == SB_ERR_INVALID
+    assert L.sb_run(None, None, 1) == SB_ERR_INVALID
+    assert L.sb_wait_staged(None) == SB_ERR_INVALID
+    assert L.sb_batch_step(None, 1, 0.0, 0.005) == SB_ERR_INVALID
