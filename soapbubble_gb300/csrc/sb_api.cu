@@ -416,6 +416,7 @@ int fill_const(sb_bubble* b, SbScalar* dst, size_t n, float v) {
 extern "C" {
 
 void sb_default_params(sb_params* p) {
+    if (!p) return;
     std::memset(p, 0, sizeof(*p));
     p->radius = 0.05;
     p->H = 0.000001;
