@@ -187,15 +187,16 @@ def workload_config(extra=None):
                    "iterations",
          "solver_tol": 1e-6, "seed": SEED,
          "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); "
-               f"state {state_mb():.0f} MB per bubble"}
+               "state 121 MB per bubble"}
     if extra:
         c.update(extra)
     return c
 
 
-def cpu_oracle_rate(target_s: float, nthreads: int, max_steps: int = 1000):
+def cpu_oracle_rate(target_s: float, nthreads: int, max_steps: int = 1000, warmup: int = 0):
     """FP64 oracle (CPU restatement of the reference step) on the same
-    workload: cell-steps/s over a bounded number of steps."""
+    workload: cell-steps/s over a bounded number of steps, after `warmup`
+    untimed steps."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     from soapbubble_gb300 import synth
@@ -205,17 +206,32 @@ def cpu_oracle_rate(target_s: float, nthreads: int, max_steps: int = 1000):
     p.solver_tol = 1e-6
     p.nthreads = nthreads
     ob = po.OracleBubble(p, f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+    k0 = 0
+    for k0 in range(warmup):
+        ob.p.t = (k0 // STEPS_PER_FRAME) * STEPS_PER_FRAME * DT
+        ob.step()
+    k0 = warmup
     t0 = time.perf_counter()
-    ob.step()  # first step: estimates the cost
+    ob.p.t = (k0 // STEPS_PER_FRAME) * STEPS_PER_FRAME * DT
+    ob.step()  # first timed step: estimates the cost
     first = time.perf_counter() - t0
     n = max(1, min(max_steps, int(target_s / max(first, 1e-3))))
     t0 = time.perf_counter()
     for k in range(n):
-        ob.p.t = ((k + 1) // STEPS_PER_FRAME) * STEPS_PER_FRAME * DT
+        ob.p.t = ((k0 + 1 + k) // STEPS_PER_FRAME) * STEPS_PER_FRAME * DT
         ob.step()
     el = time.perf_counter() - t0
     cells = NTHETA * 2 * NTHETA
     return cells * n / el, n, el
+
+
+def cuda_library_mapped() -> list:
+    """Files of this repository's CUDA library mapped into this process."""
+    try:
+        with open("/proc/self/maps") as fh:
+            return sorted({ln.split()[-1] for ln in fh if "libsoapbubble_gb300" in ln})
+    except OSError:
+        return []
 
 
 def run_reference(args):
@@ -224,16 +240,19 @@ def run_reference(args):
         return 0
     threads = os.cpu_count() or 1
     rate, n, el = cpu_oracle_rate(target_s=min(120.0, 20.0 + 2.0 * args.steps), nthreads=threads,
-                                  max_steps=max(1, args.steps))
+                                  max_steps=max(1, args.steps), warmup=args.warmup)
+    mapped = cuda_library_mapped()
+    if mapped:
+        raise RuntimeError(f"the reference arm must not load the CUDA library: {mapped}")
     line = {
         "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": n,
-        "requested_steps": args.steps, "warmup": 1, "ms_per_step": 1e3 * el / n,
+        "requested_steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / n,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": workload_config(), "impl": "reference",
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} steps of the 512x1024 workload after 1 warm-up step, "
-                                   f"FP64 oracle, OpenMP {threads} threads (the reference needs "
-                                   "AmgX/Boost/OpenCV and cannot be built)"},
+                         "sample": f"{n} steps of the 512x1024 workload after {args.warmup} "
+                                   f"warm-up steps, FP64 oracle, OpenMP {threads} threads (the "
+                                   "reference needs AmgX/Boost/OpenCV and cannot be built)"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -261,12 +280,12 @@ def run_ours(args):
 
     for k in range(args.warmup):
         gb.step(1, t_of(k), DT)
-    gb.synchronize()
+    gb.synchronize(require_converged=False)
     k0 = args.warmup
     launches0 = gb.stats().launches
     ev = [(cudart.Event(), cudart.Event()) for _ in range(args.steps)]
     barrier(dist)
-    gb.synchronize()
+    gb.synchronize(require_converged=False)
     # timed region: K graph-launched steps, CUDA events on the bubble's
     # stream around every step, L2 flushed between steps (outside the events)
     with ClockSampler(local) as clocks:
@@ -275,7 +294,7 @@ def run_ours(args):
             gb.step(1, t_of(k0 + k), DT)
             ev[k][1].record(stream)
             flush.memset_async(k & 0xff, stream)
-        gb.synchronize()
+        gb.synchronize(require_converged=False)
     barrier(dist)
     st = gb.stats()
     launches = st.launches - launches0
@@ -301,7 +320,7 @@ def run_ours(args):
         fixed, per_it = PCG_BYTES[st_k.solver_precond_used]
         solve_bytes.append(fixed + per_it * st_k.solver_iters)
         flush.memset_async(k & 0xff, tstream)
-    tw.synchronize()
+    tw.synchronize(require_converged=False)
     tw.close()
     k_dom = int(np.argmax(stage_ms))
     dom = names[k_dom]
@@ -345,7 +364,7 @@ def run_ours(args):
         te.step(1, t_of(k), DT)
     estream = te.stream()
     barrier(dist)
-    te.synchronize()
+    te.synchronize(require_converged=False)
     fl_ev = [(cudart.Event(), cudart.Event()) for _ in range(e2e_steps)]
     readback = 0.0
     t0 = time.perf_counter()
@@ -365,7 +384,7 @@ def run_ours(args):
         fl_ev[k][1].record(estream)
     te.wait_staged()
     readback += float(h_etas[(e2e_steps - 1) & 1].array[::4096].sum())
-    te.synchronize()
+    te.synchronize(require_converged=False)
     flush_s = sum(a.elapsed_ms(b) for a, b in fl_ev) / 1e3
     e2e_s = time.perf_counter() - t0 - flush_s
     h_eta = h_etas[(e2e_steps - 1) & 1]
@@ -419,7 +438,9 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": workload_config({"parallelism": f"replicas x{world}" if world > 1 else "single"}),
+            "config": workload_config(),
+            "parallelism": f"replicas x{world}" if world > 1 else "single",
+            "state_mb": round(state_mb(), 1),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes_per_launch": per_launch_bytes,

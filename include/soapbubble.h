@@ -106,6 +106,11 @@ typedef struct {
     long long launches;       /* CUDA kernels launched by this handle */
     int solver_precond_used;  /* preconditioner of the last solve: 1 phi-line blocks,
                                  2 with the Neumann term */
+    long long solves;         /* implicit solves since creation */
+    long long solver_nonconverged;  /* solves that missed their tolerance (iteration
+                                       limit, breakdown or NaN) since sb_reset_stats */
+    double solver_rel_resid_max;    /* largest relative residual of the solves since
+                                       sb_reset_stats (NaN once a solve met NaN) */
 } sb_stats;
 
 typedef struct sb_bubble sb_bubble;
@@ -208,8 +213,26 @@ int sb_upload_field_f32(sb_bubble* b, sb_field which, const float* src, size_t n
 int sb_download_field_f32(sb_bubble* b, sb_field which, float* dst, size_t n);
 
 /* Wait for the handle's queued work; returns SB_ERR_NOT_CONVERGED if the
- * last solve missed its tolerance. */
+ * last solve missed its tolerance (the reference's AmgX status check,
+ * kernel/bubble.cu:1498-1507). */
 int sb_synchronize(sb_bubble* b);
+
+/* Self-test of the bounded wait of the grid barrier that the cooperative
+ * kernels (implicit solve, map re-initialisation) synchronise with.  Four
+ * co-resident blocks meet at one barrier on the bubble's barrier word; block
+ * absent_block (0..3) never arrives, so the others give up after poll_limit
+ * polls (1 .. 2^22; the kernels' own limit is 2^22, about a second) and each
+ * counts a fault.  Afterwards sb_get_stats returns SB_ERR_CUDA, the bubble's
+ * cooperative kernels return at once and the bubble halts at the end of its
+ * next step, exactly as after a real give-up.  absent_block = -1: every
+ * block arrives and nothing is counted.  Synchronises.  No counterpart in
+ * the reference, whose kernels never wait on one another. */
+int sb_selftest_grid_barrier(sb_bubble* b, int absent_block, unsigned poll_limit);
+
+/* Restarts the running solver statistics of sb_stats (solver_nonconverged
+ * and solver_rel_resid_max) from zero; synchronises.  No counterpart in the
+ * reference, which prints each solve's outcome (kernel/bubble.cu:1495-1497). */
+int sb_reset_stats(sb_bubble* b);
 
 /* Staged I/O beside the steps (no counterpart in the reference, whose frame
  * loop copies synchronously).  Copies run on the handle's own copy stream
@@ -235,8 +258,9 @@ int sb_wait_staged(sb_bubble* b);
  * still filled) once a bounded wait inside a kernel has given up (a grid
  * barrier of the implicit solve or the re-initialisation, or a
  * shared-memory copy): the step kernels never wait without a limit, and
- * after such a fault the bubble's cooperative kernels return at once, so
- * its fields stop changing. */
+ * after such a fault the bubble's cooperative kernels return at once and
+ * the bubble halts at the end of that step (every kernel then leaves it
+ * untouched), so its fields stop changing. */
 int sb_get_stats(sb_bubble* b, sb_stats* out);
 
 /* Computes the mass integrals into the stats (synchronises). */
@@ -268,24 +292,32 @@ int sb_write_exr_gray(const char* path, int width, int height, const float* img)
  * out_dir (NULL: no output).  frames <= 0 uses p->frames.  The stop on a
  * broken film (SB_ERR_BROKEN: no cell of positive thickness) is decided
  * while a thickness frame is written, as in the reference, so a run
- * without output does not stop on it. */
+ * without output does not stop on it.  A solve that misses its tolerance
+ * stops the run right after its step, as the reference's AmgX failure does
+ * (kernel/bubble.cu:1500-1507, 2669): the later steps of the frame are
+ * not taken (the device skips them, with no host synchronisation per
+ * step), that frame is not written, and SB_ERR_NOT_CONVERGED is returned
+ * with sb_stats.steps counting the steps actually taken. */
 int sb_run(sb_bubble* b, const char* out_dir, int frames);
 
 /* No counterpart in the reference.  The two mass integrals of
  * sb_update_mass (sum of eta sin(theta) and gamma sin(theta)) for callers
  * that may not allocate device memory: a framework that owns all device
- * memory through its own pool, code running while another component
- * captures the device's streams, or a real-time loop that cannot afford
- * cudaMalloc's implicit synchronisation.  eta and gamma are the caller's
- * device arrays ([theta][phi], nTheta x 2 nTheta FP32); mass_out is the
- * caller's device array of 2 doubles, written asynchronously on `stream`
- * (a cudaStream_t, NULL = legacy default stream).  It allocates nothing:
- * its scratch is a 20 KiB array compiled into the library (held on every
- * GPU that loads it), so nTheta is limited to powers of two in [8, 1024]
- * and larger grids are rejected with SB_ERR_INVALID.  The first call on
- * each device looks up the array's address and should come before any
- * stream capture.  All calls share the array: calls whose kernels overlap
- * on the GPU race and must be serialised by the caller. */
+ * memory through its own pool, a plug-in whose host application forbids
+ * device allocations once it has started, or a real-time loop that cannot
+ * afford cudaMalloc's implicit synchronisation.  eta and gamma are the
+ * caller's device arrays ([theta][phi], nTheta x 2 nTheta FP32); mass_out
+ * is the caller's device array of 2 doubles, written asynchronously on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  It allocates
+ * nothing: its scratch is a 20 KiB array compiled into the library (held on
+ * every GPU that loads it), so nTheta is limited to powers of two in
+ * [8, 1024] and larger grids are rejected with SB_ERR_INVALID.  The first
+ * call in each device context (the first on a device, and the first after
+ * a cudaDeviceReset) looks up the array's address and should come before
+ * any stream capture.  All calls share the array: calls whose kernels
+ * overlap on the GPU race and must be serialised by the caller.  A CUDA
+ * error left pending by earlier work is not cleared: the call returns
+ * SB_ERR_CUDA without doing any work. */
 int sb_mass_integrals_noalloc(int nTheta, const float* eta, const float* gamma,
                               double* mass_out, void* stream);
 
@@ -320,7 +352,8 @@ const char* sb_last_error(void);
 typedef struct sb_batch sb_batch;
 
 /* Builds the batch's tables (per-member descriptors, cell tiles of 64, 128
- * and 256 cells, solve-block ranges).  Synchronises the members' streams. */
+ * and 256 cells, solve-block ranges).  Synchronises the members' streams.
+ * A bubble listed twice is rejected (SB_ERR_INVALID). */
 int sb_batch_create(sb_bubble* const* members, int n, sb_batch** out);
 int sb_batch_destroy(sb_batch* batch);
 

@@ -43,7 +43,8 @@ class SbStats(C.Structure):
         ("solver_rel_resid", C.c_double), ("solver_converged", C.c_int),
         ("broken_cells", C.c_int), ("steps", C.c_longlong), ("reinits", C.c_longlong),
         ("mass_eta", C.c_double), ("mass_gamma", C.c_double), ("launches", C.c_longlong),
-        ("solver_precond_used", C.c_int),
+        ("solver_precond_used", C.c_int), ("solves", C.c_longlong),
+        ("solver_nonconverged", C.c_longlong), ("solver_rel_resid_max", C.c_double),
     ]
 
 
@@ -89,6 +90,8 @@ def lib() -> C.CDLL:
     L.sb_upload_field_f32.argtypes = [H, C.c_int, fp, C.c_size_t]
     L.sb_download_field_f32.argtypes = [H, C.c_int, fp, C.c_size_t]
     L.sb_synchronize.argtypes = [H]
+    L.sb_reset_stats.argtypes = [H]
+    L.sb_selftest_grid_barrier.argtypes = [H, C.c_int, C.c_uint]
     L.sb_get_stats.argtypes = [H, S]
     L.sb_update_mass.argtypes = [H]
     L.sb_write_thickness_exr.argtypes = [H, C.c_char_p, C.POINTER(C.c_int)]
@@ -125,8 +128,8 @@ def lib() -> C.CDLL:
     L.sb_write_concentration_exr.argtypes = [H, C.c_char_p]
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
                  "sb_download_field", "sb_step", "sb_step_timed", "sb_autotune", "sb_upload_field_f32",
-                 "sb_download_field_f32", "sb_synchronize", "sb_get_stats",
-                 "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
+                 "sb_download_field_f32", "sb_synchronize", "sb_reset_stats",
+                 "sb_selftest_grid_barrier", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
                  "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
                  "sb_init_thickness_from_exr", "sb_init_airflow_from_exr", "sb_exr_load_resized",
@@ -146,7 +149,8 @@ def check(code: int, what: str) -> None:
 EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_upload_field", "sb_download_field", "sb_field_size", "sb_step",
            "sb_step_timed", "sb_autotune", "sb_stage_count", "sb_stage_name", "sb_upload_field_f32",
-           "sb_download_field_f32", "sb_synchronize", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
+           "sb_download_field_f32", "sb_synchronize", "sb_reset_stats", "sb_selftest_grid_barrier",
+           "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",
            "sb_run", "sb_write_exr_gray", "sb_mass_integrals_noalloc", "sb_bytes_required",
            "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",
            "sb_batch_step_timed", "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",

@@ -174,8 +174,19 @@ class GpuBubble:
     def wait_staged(self) -> None:
         check(lib().sb_wait_staged(self.h), "sb_wait_staged")
 
-    def synchronize(self) -> None:
-        check(lib().sb_synchronize(self.h), "sb_synchronize")
+    def synchronize(self, require_converged: bool = True) -> None:
+        """Waits for the queued work; raises SoapBubbleError (code
+        SB_ERR_NOT_CONVERGED) when the last solve missed its tolerance,
+        unless require_converged is False (callers that count failed
+        solves through stats() instead)."""
+        rc = lib().sb_synchronize(self.h)
+        if rc == _lib.SB_ERR_NOT_CONVERGED and not require_converged:
+            return
+        check(rc, "sb_synchronize")
+
+    def reset_stats(self) -> None:
+        """Restarts solver_nonconverged and solver_rel_resid_max."""
+        check(lib().sb_reset_stats(self.h), "sb_reset_stats")
 
     def stats(self, mass: bool = False) -> SbStats:
         if mass:

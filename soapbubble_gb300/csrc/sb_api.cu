@@ -6,6 +6,8 @@
 // exactly (sb_bytes_required) and creation is one allocation.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1077,6 +1079,38 @@ int sb_synchronize(sb_bubble* b) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     SB_CHECK(cudaSetDevice(b->device));
     SB_CHECK(cudaStreamSynchronize(b->stream));
+    // the outcome of the most recent solve (none before the first step)
+    SbDevStats st;
+    SB_CHECK(cudaMemcpy(&st, b->f.stats, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st.solves > 0 && !st.solver_converged)
+        return fail(SB_ERR_NOT_CONVERGED, "the last implicit solve missed its tolerance");
+    return SB_OK;
+}
+
+int sb_selftest_grid_barrier(sb_bubble* b, int absent_block, unsigned poll_limit) {
+    constexpr int kProbeBlocks = 4;
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    if (absent_block < -1 || absent_block >= kProbeBlocks)
+        return fail(SB_ERR_INVALID, "absent_block must be -1 or a block index below 4");
+    if (poll_limit < 1 || poll_limit > (1u << 22))
+        return fail(SB_ERR_INVALID, "poll_limit must be in [1, 2^22]");
+    SB_CHECK(cudaSetDevice(b->device));
+    SB_CHECK(launch_barrier_probe(b->f.self, kProbeBlocks, absent_block, poll_limit, b->stream));
+    b->launches += 1;
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    return SB_OK;
+}
+
+int sb_reset_stats(sb_bubble* b) {
+    if (!b) return fail(SB_ERR_INVALID, "null handle");
+    SB_CHECK(cudaSetDevice(b->device));
+    // solver_nonconverged and solver_resid_max are adjacent: one memset
+    static_assert(offsetof(SbDevStats, solver_resid_max) ==
+                      offsetof(SbDevStats, solver_nonconverged) + sizeof(long long),
+                  "reset range");
+    SB_CHECK(cudaMemsetAsync(&b->f.stats->solver_nonconverged, 0,
+                             sizeof(long long) + sizeof(double), b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
     return SB_OK;
 }
 
@@ -1095,14 +1129,17 @@ int sb_get_stats(sb_bubble* b, sb_stats* out) {
     out->solver_rel_resid = st.solver_rel_resid;
     out->solver_converged = st.solver_converged;
     out->broken_cells = st.broken_cells;
-    out->steps = b->steps;
+    out->steps = st.steps_done;
     out->reinits = st.reinit_total;
+    out->solves = st.solves;
+    out->solver_nonconverged = st.solver_nonconverged;
+    out->solver_rel_resid_max = st.solver_resid_max;
     out->launches = b->launches;
     out->mass_eta = st.mass_eta;
     out->mass_gamma = st.mass_gamma;
     out->solver_precond_used = st.solver_neumann ? 2 : 1;
     if (st.wait_faults)
-        return fail(SB_ERR_CUDA, "a bounded wait for a shared-memory copy in the implicit solve gave up");
+        return fail(SB_ERR_CUDA, "a bounded wait inside a kernel (grid barrier or shared-memory copy) gave up; the bubble halts");
     return SB_OK;
 }
 
@@ -1188,6 +1225,32 @@ int sb_write_concentration_exr(sb_bubble* b, const char* path) {
     return SB_OK;
 }
 
+namespace {
+
+// The frame loop's halt switch (SbBubbleDesc::halt_on_fail / halted) on the
+// bubble's device descriptor, in stream order.
+int set_halt_on_fail(sb_bubble* b, int on) {
+    static const int zero_on[2][2] = {{0, 0}, {0, 1}};  // (halted, halt_on_fail)
+    SB_CHECK(cudaMemcpyAsync(&b->f.self->halted, zero_on[on ? 1 : 0], 2 * sizeof(int),
+                             cudaMemcpyHostToDevice, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    return SB_OK;
+}
+
+// After a halted run: the host mirrors of the map parity and the step count
+// follow the device, whose kernels skipped the steps after the failed one.
+int resync_after_halt(sb_bubble* b) {
+    int cur = 0;
+    SbDevStats st;
+    SB_CHECK(cudaMemcpy(&cur, &b->f.self->cur, sizeof(int), cudaMemcpyDeviceToHost));
+    SB_CHECK(cudaMemcpy(&st, b->f.stats, sizeof(st), cudaMemcpyDeviceToHost));
+    b->cur = cur;
+    b->steps = st.steps_done;
+    return SB_OK;
+}
+
+}  // namespace
+
 int sb_run(sb_bubble* b, const char* out_dir, int frames) {
     if (!b) return fail(SB_ERR_INVALID, "null handle");
     const sb_params& p = b->params;
@@ -1211,8 +1274,19 @@ int sb_run(sb_bubble* b, const char* out_dir, int frames) {
             r = sb_write_concentration_exr(b, frame_path("con", i).c_str());
         return r;
     };
+    SB_CHECK(cudaSetDevice(b->device));
     int rc = SB_OK;
     if (out_dir && (rc = write_frame(0)) != SB_OK) return rc;
+    // A solve that misses its tolerance ends the run after that step, as the
+    // reference's AmgX failure sets `broken`, which the step loop tests
+    // before every step (kernel/bubble.cu:1500-1507, 2669-2682): the step's
+    // k_flip halts the bubble on the device, the kernels of the frame's
+    // remaining steps leave it untouched, and the frame's end reports it.
+    if ((rc = set_halt_on_fail(b, 1)) != SB_OK) return rc;
+    auto finish = [&](int r) {
+        const int r2 = set_halt_on_fail(b, 0);
+        return r != SB_OK ? r : r2;
+    };
     // Bubble::run frame loop (kernel/bubble.cu:2656-2696); U = 1
     const double dt_ = p.dt, DT = p.DT;
     double T = 0.0;
@@ -1223,16 +1297,21 @@ int sb_run(sb_bubble* b, const char* out_dir, int frames) {
             ++n;
             T += dt_;
         }
-        if (n > 0 && (rc = sb_step(b, n, tf, dt_)) != SB_OK) return rc;
+        if (n > 0 && (rc = sb_step(b, n, tf, dt_)) != SB_OK) return finish(rc);
         if ((T + 1e-7) < i * DT) {
-            if ((rc = sb_step(b, 1, tf, i * DT - T)) != SB_OK) return rc;
+            if ((rc = sb_step(b, 1, tf, i * DT - T)) != SB_OK) return finish(rc);
         }
         sb_stats st;
-        if ((rc = sb_get_stats(b, &st)) != SB_OK) return rc;
-        if (!st.solver_converged) return fail(SB_ERR_NOT_CONVERGED, "implicit solve did not converge");
+        if ((rc = sb_get_stats(b, &st)) != SB_OK) return finish(rc);
+        if (!st.solver_converged) {
+            if ((rc = resync_after_halt(b)) != SB_OK) return finish(rc);
+            return finish(fail(SB_ERR_NOT_CONVERGED, "implicit solve did not converge; the run "
+                                                     "stopped after that step"));
+        }
         T = i * DT;
-        if (out_dir && (rc = write_frame(i)) != SB_OK) return rc;
+        if (out_dir && (rc = write_frame(i)) != SB_OK) return finish(rc);
     }
+    if ((rc = finish(SB_OK)) != SB_OK) return rc;
     if (broken) return fail(SB_ERR_BROKEN, "film is broken");
     return SB_OK;
 }
@@ -1302,6 +1381,14 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     *out = nullptr;
     for (int k = 0; k < n; ++k)
         if (!bubbles[k]) return fail(SB_ERR_INVALID, "batch members must be valid bubbles on one device");
+    {
+        // a member listed twice would be stepped twice per launch (two sets of
+        // blocks on the same fields, its map parity flipped twice)
+        std::vector<sb_bubble*> sorted(bubbles, bubbles + n);
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+            return fail(SB_ERR_INVALID, "a bubble appears twice in the batch");
+    }
     sb_batch* B = new sb_batch();
     B->device = bubbles[0]->device;
     SbStepPlan& P = B->plan;

@@ -83,7 +83,10 @@ struct SbBubbleDesc {
     SbGrid g;
     SbPhys ph;
     SbFields f;
-    int cur;   // map parity, flipped on the device at the end of every step
+    int cur;           // map parity, flipped on the device at the end of every step
+    int halted;        // 1: the kernels leave this bubble untouched (set by k_flip)
+    int halt_on_fail;  // 1: a step whose solve missed its tolerance halts the bubble
+                       // (the frame loop of sb_run stops at that step, as Bubble::run)
     int pad;
 };
 
@@ -198,5 +201,9 @@ cudaError_t prepare_plan(const SbStepPlan& P);
 cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s);
 cudaError_t launch_plan_flip(const SbStepPlan& P, cudaStream_t s);
 cudaError_t launch_plan_step(const SbStepPlan& P, cudaStream_t s);
+// Self-test of the bounded grid barrier on a bubble's barrier word (`blocks`
+// co-resident blocks, block `absent` never arrives; sb_step.cu).
+cudaError_t launch_barrier_probe(SbBubbleDesc* d, int blocks, int absent, unsigned limit,
+                                 cudaStream_t s);
 
 }  // namespace sb

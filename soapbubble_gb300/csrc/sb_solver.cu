@@ -884,13 +884,19 @@ __device__ __forceinline__ SbSolveRec load_rec(const SbSolveRec* p) {
 }
 
 // Final statistics of a system that leaves the solve (FP64, once).
+// Written by one thread per system and solve; the counters and the worst
+// residual run until sb_reset_stats (a NaN residual sticks).
 __device__ __forceinline__ void write_stats(SbDevStats* st, const SbSolveRec& rc) {
     const double bb = ff_to_d(to_ff(rc.bb));
+    const double rel = sqrt(ff_to_d(to_ff(rc.rr)) / bb);
     st->solver_iters = rc.it;
-    st->solver_rel_resid = sqrt(ff_to_d(to_ff(rc.rr)) / bb);
+    st->solver_rel_resid = rel;
     st->solver_b_norm = sqrt(bb);
     st->solver_converged = rc.conv;
     st->solver_neumann = rc.neu;
+    st->solves += 1;
+    if (!rc.conv) st->solver_nonconverged += 1;
+    if (!(rel <= st->solver_resid_max)) st->solver_resid_max = rel;
 }
 
 // The loop head of CG after r.z and r.r are known: iteration limit, NaN,
@@ -1373,6 +1379,7 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     __shared__ unsigned long long s_w[3 * kAccWords];
     __shared__ ff s_sums[3];
     if (f.stats->wait_faults) return;  // a wait gave up earlier: the barrier word is not trusted
+    if (f.self->halted) return;        // the bubble stopped at a failed solve (sb_run)
     unsigned gen = grid_barrier_gen(S.bar);
     if (threadIdx.x == 0) s_rc.kind = first_kind(f.stats, cfg);
     Stage St;

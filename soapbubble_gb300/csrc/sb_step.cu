@@ -642,6 +642,7 @@ __device__ __forceinline__ const SbBubbleDesc& stage_tile_desc(SbBubbleDesc* con
     __shared__ __align__(16) SbBubbleDesc s_d;                                         \
     const int2 t = tiles[blockIdx.x];                                                  \
     const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);                         \
+    if (d.halted) return;                                                              \
     const int idx = t.y + threadIdx.x;                                                 \
     if (idx < d.g.N) __VA_ARGS__(d.g, d.ph, d.f, d.cur, idx);
 
@@ -689,12 +690,15 @@ __global__ void __launch_bounds__(256, 4) k_accum(SbBubbleDesc* const* __restric
     __shared__ __align__(16) SbBubbleDesc s_d;
     const int2 t = tiles[blockIdx.x];
     const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);
+    if (d.halted) return;  // the same in every thread of the block
     const int idx = t.y + threadIdx.x;
     const float dist = idx < d.g.N ? accum_cell<T>(d.g, d.ph, d.f, d.cur, idx) : 0.0f;
     block_max_distortion(dist, d.f.stats);
 }
 
-__device__ __forceinline__ bool reinit_now(const SbDevStats* st) {
+__device__ __forceinline__ bool reinit_now(const SbBubbleDesc& d) {
+    if (d.halted) return false;
+    const SbDevStats* st = d.f.stats;
     if (st->force_reinit >= 0) return st->force_reinit != 0;
     return __uint_as_float(st->distortion_bits) > 4.0f;
 }
@@ -774,7 +778,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
     if (descs[0]->f.stats->wait_faults) return;  // the barrier word is not trusted any more
     if (threadIdx.x == 0) {
         int a = 0;
-        for (int b = 0; b < nb; ++b) a |= reinit_now(descs[b]->f.stats) ? 1 : 0;
+        for (int b = 0; b < nb; ++b) a |= reinit_now(*descs[b]) ? 1 : 0;
         any = a;
     }
     __syncthreads();
@@ -783,7 +787,7 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
         const SbBubbleDesc& d = *descs[tl.x];
-        if (!reinit_now(d.f.stats)) continue;
+        if (!reinit_now(d)) continue;
         for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x) {
             if (idx == 0) {
                 d.f.stats->reinit = 1;
@@ -796,16 +800,38 @@ k_reinit(SbBubbleDesc* const* __restrict__ descs, int nb, const int2* __restrict
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tl = tiles[t];
         const SbBubbleDesc& d = *descs[tl.x];
-        if (!reinit_now(d.f.stats)) continue;
+        if (!reinit_now(d)) continue;
         for (int idx = tl.y + threadIdx.x; idx < tl.y + kBlock && idx < d.g.N; idx += blockDim.x)
             reinit_commit<T>(d.ph, d.f, d.cur, idx);
     }
 }
 
-// End of a step: every bubble's map parity flips.
+// End of a step: every bubble's map parity flips and its step count
+// advances.  A bubble whose frame loop stops at a failed solve
+// (halt_on_fail, sb_run) halts here, after the step that failed: the
+// kernels of later steps leave it untouched until the host clears the flag.
 __global__ void k_flip(SbBubbleDesc* const* descs, int nb) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nb) descs[b]->cur ^= 1;
+    if (b >= nb) return;
+    SbBubbleDesc* d = descs[b];
+    if (d->halted) return;
+    d->cur ^= 1;
+    SbDevStats* st = d->f.stats;
+    st->steps_done += 1;
+    if (d->halt_on_fail && !st->solver_converged) d->halted = 1;
+    // a bounded wait of the set's cooperative kernels gave up (counted on
+    // the set's first member): the barrier word is not trusted any more
+    if (descs[0]->f.stats->wait_faults) d->halted = 1;
+}
+
+// Self-test of the bounded grid barrier: every block but `absent` waits at
+// one barrier of the bubble's barrier word, with a poll limit; with a block
+// absent the others give up and count a fault each in the bubble's
+// statistics, and the kernel ends.  absent < 0: every block arrives.
+__global__ void k_barrier_probe(SbBubbleDesc* d, int absent, unsigned limit) {
+    if ((int)blockIdx.x == absent) return;
+    unsigned gen = grid_barrier_gen(d->f.bar);
+    grid_barrier(d->f.bar, gen, gridDim.x, &d->f.stats->wait_faults, limit);
 }
 
 __global__ void k_reset_maps(SbGrid g, SbFields f) {
@@ -930,6 +956,13 @@ cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s) {
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_barrier_probe(SbBubbleDesc* d, int blocks, int absent, unsigned limit,
+                                 cudaStream_t s) {
+    void* args[] = {&d, &absent, &limit};
+    return cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(blocks), dim3(kBlock), args,
+                                       0, s);
 }
 
 cudaError_t launch_plan_flip(const SbStepPlan& P, cudaStream_t s) {

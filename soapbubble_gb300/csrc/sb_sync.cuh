@@ -23,8 +23,9 @@
 // bubble or batch share the word: a launch that completes leaves its low
 // bits at zero for the next.  After a wait gave up the word is no longer
 // trusted, so the cooperative kernels of a bubble with a counted fault return
-// at once (its results stop changing and sb_get_stats keeps reporting the
-// fault).
+// at once, the bubble halts at the end of that step (k_flip; every member of
+// a batch whose launch counted it), and sb_get_stats keeps reporting the
+// fault.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -48,10 +49,11 @@ __device__ __forceinline__ unsigned grid_barrier_gen(const unsigned* bar) {
 }
 
 // Returns true in every thread of the block, or false in every thread when
-// this block's wait gave up (one fault counted in *faults).  gen: thread 0's
-// copy of the current generation bit, advanced by the call.
+// this block's wait gave up after `limit` polls (one fault counted in
+// *faults).  gen: thread 0's copy of the current generation bit, advanced by
+// the call.
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned& gen, unsigned nblocks,
-                                             int* faults) {
+                                             int* faults, unsigned limit = kGridBarPolls) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -60,7 +62,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned& gen, unsig
         asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(add) : "memory");
         unsigned polls = 0;
         while ((ld_acquire_gpu(bar) & kGridBarGenBit) == gen) {
-            if (++polls > kGridBarPolls) {
+            if (++polls > limit) {
                 atomicAdd(faults, 1);
                 ok = 0;
                 break;

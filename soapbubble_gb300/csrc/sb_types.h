@@ -57,6 +57,10 @@ struct SbDevStats {
     long long reinit_total;        // re-initialisations since creation
     int wait_faults;               // bounded waits that gave up (copy never landed)
     int solver_neumann;            // 1: the last solve used the Neumann term
+    long long solves;              // implicit solves since creation
+    long long solver_nonconverged; // solves that missed their tolerance since the last reset
+    double solver_resid_max;       // largest relative residual since the last reset
+    long long steps_done;          // steps completed (map parity flips) since creation
 };
 
 }  // namespace sb

@@ -33,6 +33,7 @@ def rt() -> C.CDLL:
         _rt.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), vp, vp]
         _rt.cudaEventDestroy.argtypes = [vp]
         _rt.cudaMemcpy.argtypes = [vp, vp, sz, C.c_int]
+        _rt.cudaMemGetInfo.argtypes = [C.POINTER(sz), C.POINTER(sz)]
     return _rt
 
 
@@ -43,6 +44,13 @@ def _ok(code: int, what: str) -> None:
 
 def set_device(dev: int) -> None:
     _ok(rt().cudaSetDevice(dev), "cudaSetDevice")
+
+
+def mem_get_info():
+    """(free, total) bytes of the current device."""
+    free, total = C.c_size_t(), C.c_size_t()
+    _ok(rt().cudaMemGetInfo(C.byref(free), C.byref(total)), "cudaMemGetInfo")
+    return free.value, total.value
 
 
 class DeviceBuffer:

@@ -123,7 +123,7 @@ def run_alone(req: Request, fields, device: int = 0, keep_eta: bool = True) -> R
             k += n
             if k % STEPS_PER_FRAME == 0 and k < req.steps:
                 g.download_f32("eta", buf)
-                g.synchronize()
+                g.synchronize(require_converged=False)
                 frames += 1
         eta = g.download("eta")
     finally:
@@ -190,7 +190,7 @@ class Server:
                     make_ready(bool(active))
                     for a in ready:
                         admitted_at[a.req.rid] = now()
-                        a.bubble.synchronize()  # its fields are in place
+                        a.bubble.synchronize(require_converged=False)  # its fields are in place
                     if ready:
                         active.extend(ready)
                         ready.clear()
@@ -227,7 +227,7 @@ class Server:
                         a.bubble.download_f32("eta", a.frame)   # streamed frame
                 for a in active:
                     if a.done < a.req.steps and a.done % STEPS_PER_FRAME == 0:
-                        a.bubble.synchronize()
+                        a.bubble.synchronize(require_converged=False)
                 for a in finished:
                     eta = a.bubble.download("eta")
                     r = Result(a.req.rid, a.req.nTheta, a.req.steps, a.req.arrival,

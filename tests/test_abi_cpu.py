@@ -104,6 +104,13 @@ def test_null_handles_and_members_are_rejected(gpulib):
         assert "valid bubbles" in L.sb_last_error().decode()
     arr = (C.c_void_p * 1)(None)
     assert L.sb_batch_create(arr, 0, C.byref(out)) == SB_ERR_INVALID
+    # a member listed twice is refused before any member is read (the
+    # handles here are never dereferenced)
+    fake = C.c_void_p(0x1000)
+    arr = (C.c_void_p * 3)(0x2000, fake, fake)
+    assert L.sb_batch_create(arr, 3, C.byref(out)) == SB_ERR_INVALID
+    assert not out.value
+    assert "twice" in L.sb_last_error().decode()
     assert L.sb_step(None, 1, 0.0, 0.005) == SB_ERR_INVALID
     assert L.sb_run(None, None, 1) == SB_ERR_INVALID
     assert L.sb_wait_staged(None) == SB_ERR_INVALID

@@ -2,15 +2,18 @@
 
 sb_mass_integrals_noalloc exists for callers that may not allocate device
 memory when they need the answer (a framework that owns all device memory
-through its own pool, code running during someone else's stream capture, a
-real-time loop that cannot pay for cudaMalloc's implicit synchronisation).
+through its own pool, a plug-in whose host application forbids device
+allocations once it has started, a real-time loop that cannot pay for
+cudaMalloc's implicit synchronisation).
 It computes what sb_update_mass computes, from device arrays the caller
 owns, with a fixed scratch array compiled into the library.  This test calls
 it through the C ABI twice in a row (a second, larger grid on the second
 call, so a stale scratch array would show) and compares each result with
 sb_update_mass on the same fields, at 1e-9 relative: both sum the same FP32
-fields in FP64, only the order of the sums differs.  It also checks that a
-grid larger than the scratch array is refused with SB_ERR_INVALID.
+fields in FP64, only the order of the sums differs.  Around each call the
+device's free memory (cudaMemGetInfo) must not change: the call allocates
+nothing.  It also checks that a grid larger than the scratch array is
+refused with SB_ERR_INVALID.
 
 It lives in its own file so that pytest collects it after every other test.
 """
@@ -47,9 +50,11 @@ def test_noalloc_mass_integrals_match_sb_update_mass(gpulib):
             try:
                 cudart.memcpy_htod(d_eta, eta)
                 cudart.memcpy_htod(d_gam, gam)
+                free0 = cudart.mem_get_info()[0]
                 rc = L.sb_mass_integrals_noalloc(nT, d_eta.ptr, d_gam.ptr, d_out.ptr, None)
                 assert rc == 0, L.sb_last_error().decode()
                 cudart.memcpy_dtoh(out_host, d_out)  # ordered after the kernels
+                assert cudart.mem_get_info()[0] == free0
                 np.testing.assert_allclose(out_host, ref, rtol=1e-9, atol=0)
             finally:
                 d_eta.free()
