@@ -1537,9 +1537,18 @@ void sb_oracle_reinit(const sb_oracle_params* p, sb_oracle_state* s) {
 // bodyforce still accumulates the changes through the (identity) maps
 int sb_oracle_step(const sb_oracle_params* p, sb_oracle_state* s, sb_oracle_stats* st) {
     sb_oracle_stats local{};
+    // Under VISCOUS the reference launches applyforcevelphiKernel_viscous
+    // with the u_theta launch layout (nTheta - 1 rows: the VISCOUS branch of
+    // bubble.cu:2463-2474 has no determineLayout for velPhi), so the last
+    // theta row of the output buffer is never written; after the buffer
+    // swap it holds u_phi from before the step's advection.
+    const size_t N = (size_t)p->nTheta * p->nPhi, nP = (size_t)p->nPhi;
+    std::vector<double> uph_last;
+    if (p->viscous) uph_last.assign(s->uph + (N - nP), s->uph + N);
     if (!p->plain_advection) sb_oracle_update_maps(p, s);
     sb_oracle_advection(p, s);
     int rc = sb_oracle_bodyforce(p, s, &local);
+    if (p->viscous) std::copy(uph_last.begin(), uph_last.end(), s->uph + (N - nP));
     bool re = false;
     if (!p->plain_advection) {
         sb_oracle_distortion(p, s, &local);

@@ -507,8 +507,11 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
         f.d_eta[idx] = -e;
     }
 
-    // u_phi face between (i, j-1) and (i, j)
-    {
+    // u_phi face between (i, j-1) and (i, j).  Under VISCOUS the reference
+    // launches its u_phi update with the u_theta layout (nTheta - 1 rows,
+    // kernel/bubble.cu:2463-2474), so u_phi's last theta row keeps its value
+    // from before the step: the state buffer is left as it is.
+    if (!VISC || i < g.nT - 1) {
         const int w = i * nP + ((j - 1) & g.maskP);
         const float etaW = f.eta_adv[w];
         const float invEta = 2.0f / (etaW + e);
