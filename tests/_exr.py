@@ -10,17 +10,19 @@ import struct
 import numpy as np
 
 
-def write_exr_bgr(path, b, g, r) -> None:
-    """Write three equally shaped planes as HALF channels B, G, R."""
+def write_exr_bgr(path, b, g, r, pixel_type: str = "half") -> None:
+    """Write three equally shaped planes as channels B, G, R, HALF (default)
+    or FLOAT samples."""
     h, w = b.shape
-    planes = [np.asarray(p, dtype=np.float16) for p in (b, g, r)]
+    code, dt, size = {"half": (1, "<f2", 2), "float": (2, "<f4", 4)}[pixel_type]
+    planes = [np.asarray(p, dtype=np.float32).astype(dt) for p in (b, g, r)]
     hdr = bytearray(b"\x76\x2f\x31\x01") + struct.pack("<I", 2)
 
     def attr(name, typ, data):
         hdr.extend(name.encode() + b"\0" + typ.encode() + b"\0" + struct.pack("<I", len(data)))
         hdr.extend(data)
 
-    ch = b"".join(c.encode() + b"\0" + struct.pack("<iBBBBii", 1, 0, 0, 0, 0, 1, 1)
+    ch = b"".join(c.encode() + b"\0" + struct.pack("<iBBBBii", code, 0, 0, 0, 0, 1, 1)
                   for c in ("B", "G", "R")) + b"\0"
     attr("channels", "chlist", ch)
     attr("compression", "compression", b"\0")
@@ -31,14 +33,14 @@ def write_exr_bgr(path, b, g, r) -> None:
     attr("screenWindowCenter", "v2f", struct.pack("<2f", 0.0, 0.0))
     attr("screenWindowWidth", "float", struct.pack("<f", 1.0))
     hdr.extend(b"\0")
-    line = 3 * 2 * w
+    line = 3 * size * w
     first = len(hdr) + 8 * h
     table = b"".join(struct.pack("<Q", first + (8 + line) * y) for y in range(h))
     body = bytearray()
     for y in range(h):
         body.extend(struct.pack("<iI", y, line))
         for p in planes:
-            body.extend(p[y].astype("<f2").tobytes())
+            body.extend(p[y].tobytes())
     with open(path, "wb") as f:
         f.write(bytes(hdr) + table + bytes(body))
 
