@@ -283,6 +283,7 @@ def run_ours(args):
     gb.synchronize(require_converged=False)
     k0 = args.warmup
     launches0 = gb.stats().launches
+    gb.reset_stats()  # failed solves and the worst residual of the timed steps
     ev = [(cudart.Event(), cudart.Event()) for _ in range(args.steps)]
     barrier(dist)
     gb.synchronize(require_converged=False)
@@ -395,19 +396,30 @@ def run_ours(args):
     same = bool(np.array_equal(te.download("eta"), gb.download("eta")))
     te.close()
 
-    cpu = None
+    cpu = cpu1 = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, n, el = cpu_oracle_rate(target_s=15.0, nthreads=threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} steps of the same 512x1024 workload (FP64 oracle, OpenMP "
                          f"{threads} threads, PCG to 1e-6), {el:.1f} s"}
+        rate1, n1, el1 = cpu_oracle_rate(target_s=10.0, nthreads=1, max_steps=2)
+        cpu1 = {"value": rate1, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": f"{n1} steps of the same 512x1024 workload (FP64 oracle, one thread, "
+                          f"PCG to 1e-6), {el1:.1f} s"}
 
-    ensemble = serving = storage = None
+    ensemble = serving = storage = whole = modes = None
     if rank == 0 and world == 1:
         h_u.free(); h_v.free(); [h.free() for h in h_etas]; flush.free()
         gb.close()
         gb = None
+        from soapbubble_gb300 import c1report
+        if args.whole_run_steps > 0:
+            whole = c1report.whole_run(ALG_BYTES_PER_CELL, PCG_BYTES, peak, device=local,
+                                       steps=args.whole_run_steps)
+        if args.modes_prefix > 0:
+            modes = c1report.solver_modes(prefix=args.modes_prefix, device=local,
+                                          run_steps=max(args.whole_run_steps, args.modes_prefix))
         from soapbubble_gb300 import ensemble as ens, serve
         if args.ensemble_steps > 0:
             ensemble = ens.compare(steps=args.ensemble_steps, device=local)
@@ -448,6 +460,7 @@ def run_ours(args):
                          "note": ROOFLINE_NOTES.get(dom, "")},
             "stage_roofline": stage_roofline,
             "cpu_baseline": cpu,
+            "cpu_baseline_1thread": cpu1,
             "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
                     "same_steps_as_value": same,
                     "h2d_bytes_per_step": 4 * (N + Nv), "d2h_bytes_per_step": 4 * N,
@@ -461,6 +474,12 @@ def run_ours(args):
             "stage_share": stage_share, "stage_us_per_step": stage_us,
             "stage_steps": kr, "step_path": "CUDA graph per step (value); kernel-by-kernel with events (stages)",
             "solver_iters_mean": mean_iters, "solver_rel_resid_last": st.solver_rel_resid,
+            "solver_nonconverged": int(st.solver_nonconverged),
+            "solver_rel_resid_max": float(st.solver_rel_resid_max),
+            "window": f"steps {k0}..{k0 + args.steps - 1} of the 1000-step run (the film is "
+                      "still whole; c1_whole_run covers the rupture)",
+            "c1_whole_run": whole,
+            "c1_solver_modes": modes,
             "solver_alg_bytes_per_cell": alg["k_solve"],
             "reinits": int(final.reinits), "result_finite": finite,
             "ensemble": ensemble,
@@ -493,6 +512,10 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=100)
     # c2 (1024 x 2048) with FP32 and with BF16 field storage (steps; 0 skips)
     ap.add_argument("--storage-steps", type=int, default=100)
+    # the whole c1 run, every step timed (steps; 0 skips)
+    ap.add_argument("--whole-run-steps", type=int, default=1000)
+    # plain FP32 vs mixed solve on c1: steps compared with the oracle (0 skips)
+    ap.add_argument("--modes-prefix", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -128,9 +128,10 @@ def test_texture_initialisers_match_reference_formulas(gpulib, texture_path):
         np.testing.assert_allclose(gb.download("eta"), (B - 0.5) * 0.3 + 0.5, rtol=1e-7)
         np.testing.assert_allclose(gb.download("eta_init"), gb.download("eta"), rtol=0)
         np.testing.assert_allclose(gb.download("uair_init"),
-                                   0.5 * (G + np.roll(G, 1, axis=1)) * RADIUS, rtol=0, atol=1e-9)
+                                   0.5 * (G + np.roll(G, 1, axis=1)) * RADIUS, rtol=1e-7,
+                                   atol=1e-12)  # FP32 storage
         np.testing.assert_allclose(gb.download("vair_init"), -0.5 * (R[:-1] + R[1:]) * RADIUS,
-                                   rtol=0, atol=1e-9)
+                                   rtol=1e-7, atol=1e-12)
         assert np.all(gb.download("gamma") == 1.0)  # Solver::Solver's gamma = 1
 
 
