@@ -682,7 +682,9 @@ __device__ __forceinline__ void row_load_r(const SbGrid& g, const SbFields& f, i
     }
 }
 
-// The increment and the new gamma: dx, x = gamma_adv + dx.
+// The increment and the new gamma: dx, x = gamma_adv + dx; xff keeps the
+// increment as a float-float pair in both modes (plain mode: (dx, 0)),
+// which the post-solve stage differences between neighbours.
 template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_final(const SbGrid& g, const SbFields& f, int i) {
     const int nP = g.nP, row = i * nP;
@@ -694,6 +696,7 @@ __device__ __forceinline__ void row_final(const SbGrid& g, const SbFields& f, in
             const float dx = MIXED ? ff_to_f(ld_ff(f.xff, c)) : f.dx[c];
             f.dx[c] = dx;
             f.x[c] = f.gam_adv[c] + dx;
+            if (!MIXED) f.xff[c] = make_float2(dx, 0.0f);
         }
     }
 }

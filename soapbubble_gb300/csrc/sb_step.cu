@@ -466,11 +466,18 @@ __device__ __forceinline__ bool gamma_clamped(float gm, float gmax) {
     return gm <= 0.0f || gm > gmax - kEps;
 }
 
-// Difference gamma_new(a) - gamma_new(b) of two cells.
+// Difference gamma_new(a) - gamma_new(b) of two cells.  The increments
+// are differenced as the solver's float-float pairs: next to the poles the
+// new gamma varies along phi by parts in 1e5 of the increment, and the
+// Marangoni force there (1/sin(theta) times that difference) would inherit
+// the increment's FP32 rounding (2e-4 of u_phi at the config.txt grid).
 __device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, float gmax) {
     const float xa = f.x[a], xb = f.x[b];
     const bool ca = gamma_clamped(xa, gmax), cb = gamma_clamped(xb, gmax);
-    if (!ca && !cb) return (f.gam_adv[a] - f.gam_adv[b]) + (f.dx[a] - f.dx[b]);
+    if (!ca && !cb) {
+        const float2 da = f.xff[a], db = f.xff[b];
+        return (f.gam_adv[a] - f.gam_adv[b]) + ((da.x - db.x) + (da.y - db.y));
+    }
     return (ca ? gmax : xa) - (cb ? gmax : xb);
 }
 
