@@ -597,13 +597,26 @@ __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i
         for (int u = 0; u < G2; ++u) {
             if (col_of<TB>(k0 + u) < nP) {
                 const float pc = zc[u] + beta * pc0[u];
-                float qf = dm[u] * pc + ce[u] * (pc - (ze[u] + beta * pe[u])) +
-                           cw[u] * (pc - (zw[u] + beta * pw[u]));
-                if (hasS) qf += cs[u] * (pc - (zs[u] + beta * ps[u]));
+                const float dE = pc - (ze[u] + beta * pe[u]);
+                const float dS = pc - (zs[u] + beta * ps[u]);
+                float qf = dm[u] * pc + ce[u] * dE + cw[u] * (pc - (zw[u] + beta * pw[u]));
+                if (hasS) qf += cs[u] * dS;
                 if (hasN) qf += cn[u] * (pc - (zn[u] + beta * pn[u]));
                 pnew[cc[u]] = pc;
                 qout[cc[u]] = qf;
-                pq[half_of<TB>(k0 + u)] = acc<MIXED>(pq[half_of<TB>(k0 + u)], pc, qf);
+                ff& h = pq[half_of<TB>(k0 + u)];
+                if (MIXED) {
+                    h = ff_add_prod(h, pc, qf);  // exact products: p.q as the sum of p_c q_c
+                } else {
+                    // plain FP32: p.q = p^T A p in its energy form, every term
+                    // non-negative (each east and south face once).  The sum
+                    // of the rounded products p_c q_c cancels to nothing on
+                    // ruptured films (weights 1e5 times the mass terms) and
+                    // lost its sign there, breaking the iteration down.
+                    h = ff_add_f(h, __fmul_rn(dm[u] * pc, pc));
+                    h = ff_add_f(h, __fmul_rn(ce[u] * dE, dE));
+                    if (hasS) h = ff_add_f(h, __fmul_rn(cs[u] * dS, dS));
+                }
             }
         }
     }
