@@ -188,7 +188,7 @@ std::shared_ptr<const Corridor> corridor_factors(int nT, double radius) {
 
 struct ArenaPlan {
     Layout L;
-    size_t tables, eta, gam, uth, uph, eta_adv, gam_adv, uth_adv, uph_adv;
+    size_t tables, rowtab, rottab, eta, gam, uth, uph, eta_adv, gam_adv, uth_adv, uph_adv;
     size_t bim[8];
     size_t fwd[2], bwd[2], bwdprev;
     size_t uair_init, vair_init, corr_u, corr_v, uair, vair;
@@ -205,6 +205,8 @@ ArenaPlan plan_arena(const SbGrid& g, int storage) {
     ArenaPlan a;
     const size_t N = (size_t)g.N, Nv = (size_t)g.Nv, F = sizeof(float);
     a.tables = a.L.take((size_t)(4 * g.nT + 2) * F);
+    a.rowtab = a.L.take((size_t)g.nT * sizeof(float4));
+    a.rottab = a.L.take((size_t)g.nP * sizeof(float2));
     const size_t S = scalar_bytes(storage);
     a.eta = a.L.take(N * S); a.gam = a.L.take(N * S);
     a.uth = a.L.take(Nv * F); a.uph = a.L.take(N * F);
@@ -213,8 +215,11 @@ ArenaPlan plan_arena(const SbGrid& g, int storage) {
     // init, delta, initL, deltaL of eta, then of gamma: the reference fields
     // in the stored type, the accumulators in FP32
     for (int k = 0; k < 8; ++k) a.bim[k] = a.L.take(N * ((k & 1) ? F : S));
-    for (int k = 0; k < 2; ++k) { a.fwd[k] = a.L.take(N * 8); a.bwd[k] = a.L.take(N * 8); }
-    a.bwdprev = a.L.take(N * 8);
+    for (int k = 0; k < 2; ++k) {
+        a.fwd[k] = a.L.take(N * sizeof(float4));
+        a.bwd[k] = a.L.take(N * sizeof(float4));
+    }
+    a.bwdprev = a.L.take(N * sizeof(float4));
     a.uair_init = a.L.take(N * F); a.vair_init = a.L.take(Nv * F);
     a.corr_u = a.L.take(N * F); a.corr_v = a.L.take(Nv * F);
     a.uair = a.L.take((N + 1) * F); a.vair = a.L.take((Nv + 1) * F);
@@ -288,7 +293,7 @@ float* fptr(sb_bubble* b, sb_field w) {
     }
 }
 
-float2* map_ptr(sb_bubble* b, sb_field w, int& comp) {
+float4* map_ptr(sb_bubble* b, sb_field w, int& comp) {
     comp = (w == SB_FWD_P || w == SB_BWD_P || w == SB_BWDPREV_P) ? 1 : 0;
     switch (w) {
         case SB_FWD_T: case SB_FWD_P: return b->f.fwd[b->cur];
@@ -296,6 +301,27 @@ float2* map_ptr(sb_bubble* b, sb_field w, int& comp) {
         case SB_BWDPREV_T: case SB_BWDPREV_P: return b->f.bwdprev;
         default: return nullptr;
     }
+}
+
+// A map entry of cell (i, j) (the mapped point's displacement from the cell
+// centre in the cell's frame, whose x axis lies at azimuth j h) and the
+// mapped point's absolute grid coordinates (theta / h, phi / h in [0, nPhi)),
+// in FP64 both ways.
+void map_entry_to_abs(int i, int j, int nT, float4 D, double* th, double* ph) {
+    const double h = kPi / nT, t0 = (i + 0.5) * h;
+    const double X = std::sin(t0) + D.x, Y = D.y, Z = std::cos(t0) + D.z;
+    *th = std::atan2(std::hypot(X, Y), Z) / h;
+    double p = j + std::atan2(Y, X) / h;
+    p = std::fmod(p, 2.0 * nT);
+    if (p < 0) p += 2.0 * nT;
+    *ph = p;
+}
+
+float4 map_entry_from_abs(int i, int j, int nT, double th, double ph) {
+    const double h = kPi / nT, t0 = (i + 0.5) * h;
+    const double t = th * h, dp = (ph - j) * h;
+    const double X = std::sin(t) * std::cos(dp), Y = std::sin(t) * std::sin(dp), Z = std::cos(t);
+    return make_float4((float)(X - std::sin(t0)), (float)Y, (float)(Z - std::cos(t0)), 0.0f);
 }
 
 // Writes the per-step scalars into the pinned slot and copies them to the
@@ -505,10 +531,10 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     f.gam_init = SCL(a.bim[4]); f.gam_delta = F32(a.bim[5]);
     f.gam_initL = SCL(a.bim[6]); f.gam_deltaL = F32(a.bim[7]);
     for (int k = 0; k < 2; ++k) {
-        f.fwd[k] = (float2*)(A + a.fwd[k]);
-        f.bwd[k] = (float2*)(A + a.bwd[k]);
+        f.fwd[k] = (float4*)(A + a.fwd[k]);
+        f.bwd[k] = (float4*)(A + a.bwd[k]);
     }
-    f.bwdprev = (float2*)(A + a.bwdprev);
+    f.bwdprev = (float4*)(A + a.bwdprev);
     f.uair_init = F32(a.uair_init); f.vair_init = F32(a.vair_init);
     f.corr_u = F32(a.corr_u); f.corr_v = F32(a.corr_v);
     f.uair = F32(a.uair); f.vair = F32(a.vair);
@@ -557,6 +583,28 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     g.cos_e = b->tables + 3 * g.nT + 1;
     e = cudaMemcpy(b->tables, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { int r = cuda_fail(e, "tables"); sb_destroy(b); return r; }
+    // characteristic-map geometry: row angles as (hi, lo) float pairs and
+    // the rotation by every column offset
+    {
+        std::vector<float4> row((size_t)g.nT);
+        for (int i = 0; i < g.nT; ++i) {
+            const double sv = std::sin((i + 0.5) * h), cv = std::cos((i + 0.5) * h);
+            const float sh = (float)sv, ch = (float)cv;
+            row[i] = make_float4(sh, (float)(sv - sh), ch, (float)(cv - ch));
+        }
+        std::vector<float2> rot((size_t)g.nP);
+        for (int k = 0; k < g.nP; ++k) {
+            const double d = (k - g.nT) * h, sh = std::sin(0.5 * d);
+            rot[k] = make_float2((float)std::sin(d), (float)(-2.0 * sh * sh));
+        }
+        g.rowtab = (const float4*)(A + a.rowtab);
+        g.rottab = (const float2*)(A + a.rottab);
+        e = cudaMemcpy((void*)g.rowtab, row.data(), row.size() * sizeof(float4), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy((void*)g.rottab, rot.data(), rot.size() * sizeof(float2),
+                           cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { int r = cuda_fail(e, "map tables"); sb_destroy(b); return r; }
+    }
 
     // static corridor factors
     {
@@ -672,27 +720,25 @@ int sb_upload_field(sb_bubble* b, sb_field which, const double* src, size_t n) {
     if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
     SB_CHECK(cudaSetDevice(b->device));
     int comp = 0;
-    float2* m = map_ptr(b, which, comp);
+    float4* m = map_ptr(b, which, comp);
     if (m) {
-        // absolute grid coordinates -> offsets from the cell centre
+        // absolute grid coordinates of one component -> displacements (the
+        // other component is kept: read, converted, replaced, written back)
         const int nT = b->g.nT, nP = b->g.nP;
-        std::vector<float2> tmp((size_t)b->g.N);
-        SB_CHECK(cudaMemcpyAsync(tmp.data(), m, tmp.size() * sizeof(float2), cudaMemcpyDeviceToHost,
+        std::vector<float4> tmp((size_t)b->g.N);
+        SB_CHECK(cudaMemcpyAsync(tmp.data(), m, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost,
                                  b->stream));
         SB_CHECK(cudaStreamSynchronize(b->stream));
         for (int i = 0; i < nT; ++i)
             for (int j = 0; j < nP; ++j) {
                 const size_t c = (size_t)i * nP + j;
-                if (comp == 0) {
-                    tmp[c].x = (float)(src[c] - (i + 0.5));
-                } else {
-                    double d = std::fmod(src[c] - j, (double)nP);
-                    if (d >= nT) d -= nP;
-                    if (d < -nT) d += nP;
-                    tmp[c].y = (float)d;
-                }
+                double th, ph;
+                map_entry_to_abs(i, j, nT, tmp[c], &th, &ph);
+                if (comp == 0) th = src[c];
+                else ph = src[c];
+                tmp[c] = map_entry_from_abs(i, j, nT, th, ph);
             }
-        SB_CHECK(cudaMemcpyAsync(m, tmp.data(), tmp.size() * sizeof(float2), cudaMemcpyHostToDevice,
+        SB_CHECK(cudaMemcpyAsync(m, tmp.data(), tmp.size() * sizeof(float4), cudaMemcpyHostToDevice,
                                  b->stream));
         SB_CHECK(cudaStreamSynchronize(b->stream));
         return SB_OK;
@@ -708,22 +754,19 @@ int sb_download_field(sb_bubble* b, sb_field which, double* dst, size_t n) {
     if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
     SB_CHECK(cudaSetDevice(b->device));
     int comp = 0;
-    float2* m = map_ptr(b, which, comp);
+    float4* m = map_ptr(b, which, comp);
     if (m) {
         const int nT = b->g.nT, nP = b->g.nP;
-        std::vector<float2> tmp((size_t)b->g.N);
-        SB_CHECK(cudaMemcpyAsync(tmp.data(), m, tmp.size() * sizeof(float2), cudaMemcpyDeviceToHost,
+        std::vector<float4> tmp((size_t)b->g.N);
+        SB_CHECK(cudaMemcpyAsync(tmp.data(), m, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost,
                                  b->stream));
         SB_CHECK(cudaStreamSynchronize(b->stream));
         for (int i = 0; i < nT; ++i)
             for (int j = 0; j < nP; ++j) {
                 const size_t c = (size_t)i * nP + j;
-                if (comp == 0) {
-                    dst[c] = (i + 0.5) + (double)tmp[c].x;
-                } else {
-                    double v = std::fmod(j + (double)tmp[c].y + nP, (double)nP);
-                    dst[c] = v;
-                }
+                double th, ph;
+                map_entry_to_abs(i, j, nT, tmp[c], &th, &ph);
+                dst[c] = comp == 0 ? th : ph;
             }
         return SB_OK;
     }

@@ -10,8 +10,14 @@
 //     (cos t0, 0, -sin t0), e_phi = (0, 1, 0); nearby points are carried as
 //     displacements d = P - C, converted to and from grid offsets with
 //     half-angle formulas that never subtract two O(1) quantities;
-//   * characteristic maps store, per cell, the offset (in grid units) of the
-//     mapped point from the cell centre.
+//   * characteristic maps store, per cell, the mapped point's displacement
+//     from the cell centre in the cell's own frame (a float4: x, y, z, 0).
+//     A lookup from another cell's frame rotates it about z by the column
+//     difference and adds the difference of the two centres, both from
+//     tables computed in FP64 (rottab: sin and cos - 1 of dc h; rowtab: sin
+//     and cos of the row angles as hi + lo pairs, so that the difference of
+//     two rows' values keeps full precision); writing a map entry is a
+//     store of the displacement the step computed in the cell's frame.
 // The arithmetic is the reference's (kernel/bubble.cu:116-606): geometric
 // pole reflection with vector sign flips, NaN-skipping bilinear lerp,
 // great-circle RK2 trace with parallel transport, spherical lerp of map
@@ -28,8 +34,8 @@
 #include "sb_types.h"
 
 // Inlining of the geometry helpers: the slerp and the map lookup are inlined
-// (measured faster); the two position / displacement conversions stay out of
-// line, which keeps the map kernels small in the instruction cache.
+// (measured faster); the position of a displacement (pos_from_disp) stays
+// out of line, which keeps the map kernels small in the instruction cache.
 #ifndef SB_GEOM_INLINE
 #define SB_GEOM_INLINE __forceinline__
 #endif
@@ -57,6 +63,7 @@ struct Frame {
     int bi, bj;
     float fi, fj;
     float s0, c0;
+    float s0lo, c0lo;  // cell frames: the low parts of s0, c0 (rowtab); else 0
 };
 
 // A sample position: raw theta/h = bi + ox, raw phi/h = bj + oy.
@@ -70,23 +77,6 @@ __device__ __forceinline__ float blerp(float from, float to, float a) {
     if (isnan(from)) return to;
     if (isnan(to)) return from;
     return (1.0f - a) * from + a * to;
-}
-
-// Displacement P - C, in the frame, of the point at grid offsets (dth, dph)
-// from the frame's base.
-__device__ SB_CONV_INLINE f3 disp_from_offsets(Frame F, float dth, float dph, float h) {
-    float sh, chh;
-    fsincos(0.5f * dth * h, &sh, &chh);
-    const float sm = F.s0 * chh + F.c0 * sh;  // sin(t0 + dt/2)
-    const float cm = F.c0 * chh - F.s0 * sh;  // cos(t0 + dt/2)
-    const float dS = 2.0f * cm * sh;          // sin t1 - sin t0
-    const float dC = -2.0f * sm * sh;         // cos t1 - cos t0
-    const float s1 = F.s0 + dS;
-    float sp, cp;
-    fsincos(0.5f * dph * h, &sp, &cp);
-    const float sinD = 2.0f * sp * cp;
-    const float cosDm1 = -2.0f * sp * sp;
-    return {dS + s1 * cosDm1, s1 * sinD, dC};
 }
 
 // Grid position of the point C + d.  Points past a pole come back with the
@@ -107,6 +97,31 @@ __device__ SB_CONV_INLINE Pos pos_from_disp(Frame F, f3 d, float invh, int nT) {
     } else {
         q.bj = F.bj + nT;
         q.oy = F.fj + fatan2(-Py, -Px) * invh;
+    }
+    return q;
+}
+
+// pos_from_disp for positions that only select and weight samples (the
+// departure points of field samples and of map lookups whose result is not
+// stored): the same formulas with the quotients taken by __fdividef, which
+// places the point within ~1e-6 of a cell.
+__device__ SB_CONV_INLINE Pos pos_from_disp_fast(Frame F, f3 d, float invh, int nT) {
+    const float Px = F.s0 + d.x, Py = d.y, Pz = F.c0 + d.z;
+    const float rho = sqrtf(Px * Px + Py * Py);
+    const float den = rho + F.s0;
+    const float rms0 =
+        den > 0.0f ? __fdividef(2.0f * F.s0 * d.x + d.x * d.x + d.y * d.y, den) : 0.0f;
+    const float sdt = rms0 * F.c0 - d.z * F.s0;
+    const float cdt = rho * F.s0 + Pz * F.c0;
+    Pos q;
+    q.bi = F.bi;
+    q.ox = F.fi + fatan2_fast(sdt, cdt) * invh;
+    if (Px >= 0.0f) {
+        q.bj = F.bj;
+        q.oy = F.fj + fatan2_fast(Py, Px) * invh;
+    } else {
+        q.bj = F.bj + nT;
+        q.oy = F.fj + fatan2_fast(-Py, -Px) * invh;
     }
     return q;
 }
@@ -325,56 +340,45 @@ __device__ __forceinline__ float sample_utheta(const SbGrid& g, const float* __r
     return flipped ? -r : r;
 }
 
+// Displacement, in the cell frame F, of the map point stored for cell
+// (r, c) (D: its displacement in its own frame).  With Delta = (c - F.bj) h
+// the rotation from the entry's frame to F's and C_r, C_F the two centres:
+// P - C_F = R(Delta) (C_r + D) - C_F, evaluated as sums of small terms
+// (each product of two precise factors) so that the result keeps ~1e-7 of
+// its own size next to the poles too.
+__device__ __forceinline__ f3 map_point(const SbGrid& g, const Frame& F, float4 D, int r, int c) {
+    const float4 R = __ldg(&g.rowtab[r]);
+    const int dc = ((c - F.bj + g.nT) & g.maskP) - g.nT;
+    const float2 t = __ldg(&g.rottab[dc + g.nT]);  // sin(Delta), cos(Delta) - 1
+    const float ds = (R.x - F.s0) + (R.y - F.s0lo);  // s_r - s_F
+    const float dz = (R.z - F.c0) + (R.w - F.c0lo);  // c_r - c_F
+    f3 P;
+    P.x = ds + D.x + t.y * R.x + t.y * D.x - t.x * D.y;
+    P.y = t.x * R.x + t.x * D.x + D.y + t.y * D.y;
+    P.z = dz + D.z;
+    return P;
+}
+
 // Characteristic-map lookup (sampleMapping, kernel/bubble.cu:539-606): the
 // four map points around q, slerped along phi on each row and then along
-// theta.  Map entries are float2 offsets from their own cell centre.  The
-// result is a displacement in frame F.
-// The lookup for a stencil already computed at the query point (the same
-// cell-centred stencil also serves scalar samples there).
-__device__ SB_GEOM_INLINE f3 map_at_stencil(const float2* __restrict__ map, Frame F,
-                                             const CStencil& s, int nT, float h) {
-    const int nP = 2 * nT, maskP = nP - 1;
-    const float baseI = (float)0.5f - F.fi;
-    auto point = [&](int r, int c) -> f3 {
-        const float2 m = map[r * nP + c];
-        const float dth = (float)(r - F.bi) + baseI + m.x;
-        int dj = c - F.bj;
-        dj = ((dj + nT) & maskP) - nT;  // wrap to [-nT, nT)
-        const float dph = (float)dj + (m.y - F.fj);
-        return disp_from_offsets(F, dth, dph, h);
-    };
-    const f3 ll = point(s.r0, s.c00), lr = point(s.r0, s.c01);
-    const f3 hl = point(s.r1, s.c10), hr = point(s.r1, s.c11);
+// theta.  The result is a displacement in the cell frame F.  The lookup for
+// a stencil already computed at the query point (the same cell-centred
+// stencil also serves scalar samples there).
+__device__ SB_GEOM_INLINE f3 map_at_stencil(const SbGrid& g, const float4* __restrict__ map,
+                                             const Frame& F, const CStencil& s) {
+    const int nP = g.nP;
+    const f3 ll = map_point(g, F, map[s.r0 * nP + s.c00], s.r0, s.c00);
+    const f3 lr = map_point(g, F, map[s.r0 * nP + s.c01], s.r0, s.c01);
+    const f3 hl = map_point(g, F, map[s.r1 * nP + s.c10], s.r1, s.c10);
+    const f3 hr = map_point(g, F, map[s.r1 * nP + s.c11], s.r1, s.c11);
     const f3 lo = slerp_disp(F.s0, F.c0, ll, lr, s.b);
     const f3 hi = slerp_disp(F.s0, F.c0, hl, hr, s.b);
     return slerp_disp(F.s0, F.c0, lo, hi, s.a);
 }
 
-__device__ SB_GEOM_INLINE f3 sample_map_impl(const float2* __restrict__ map, Frame F, Pos q,
-                                              int nT, float h, float invh) {
-    SbGrid g;
-    g.nT = nT;
-    g.nP = 2 * nT;
-    g.maskP = g.nP - 1;
-    g.h = h;
-    g.invh = invh;
-    return map_at_stencil(map, F, centred_stencil(g, q, 0.0f), nT, h);
-}
-
-__device__ __forceinline__ f3 sample_map(const SbGrid& g, const float2* __restrict__ map,
+__device__ __forceinline__ f3 sample_map(const SbGrid& g, const float4* __restrict__ map,
                                          const Frame& F, Pos q) {
-    return sample_map_impl(map, F, q, g.nT, g.h, g.invh);
-}
-
-// Offsets (grid units) of C + d from the frame base, for storing as a map
-// entry of a cell frame: phi offset wrapped to [-nT, nT).
-__device__ __forceinline__ float2 map_entry_from_disp(const SbGrid& g, const Frame& F, f3 d) {
-    const Pos q = pos_from_disp(F, d, g.invh, g.nT);
-    float dth = (float)(q.bi - F.bi) + (q.ox - F.fi);
-    float dph = (float)(q.bj - F.bj) + (q.oy - F.fj);
-    if (dph >= (float)g.nT) dph -= (float)g.nP;
-    if (dph < -(float)g.nT) dph += (float)g.nP;
-    return make_float2(dth, dph);
+    return map_at_stencil(g, map, F, centred_stencil(g, q, 0.0f));
 }
 
 // Velocity (u_theta, u_phi) at an arbitrary position.
@@ -414,6 +418,10 @@ struct Trace {
 // direction is first corrected with the velocity at the half step (the
 // scalar traces always; the velocity advection under RUNGE_KUTTA,
 // bubble.cu:689-730).
+// FAST: the half-step position that picks the mid-point velocity samples
+// comes from pos_from_disp_fast (the velocity advection); the map update
+// keeps the exact quotients.
+template <bool FAST = false>
 __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restrict__ uth,
                                           const float* __restrict__ uph, const Frame& F,
                                           float gt, float gp, float dt, bool rk2 = true) {
@@ -437,7 +445,8 @@ __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restri
         cdm1 = -2.0f * sh * sh;
         const f3 dmid = sd * u_ + cdm1 * w;
         const f3 midx = w + dmid;
-        const Pos qm = pos_from_disp(F, dmid, g.invh, g.nT);
+        const Pos qm = FAST ? pos_from_disp_fast(F, dmid, g.invh, g.nT)
+                            : pos_from_disp(F, dmid, g.invh, g.nT);
         float mt, mp;
         velocity_at(g, uth, uph, qm, mt, mp);
         f3 beth, beph;
@@ -538,7 +547,7 @@ __device__ __forceinline__ float gather(const float* __restrict__ f, const SSten
 // cell, so its nine map points are converted once (rows -1 and nTheta are
 // the across-pole reflections, as in the single lookup).  Results are
 // displacements in the cell's frame F.
-__device__ __forceinline__ void sample_map_multi5(const SbGrid& g, const float2* __restrict__ map,
+__device__ __forceinline__ void sample_map_multi5(const SbGrid& g, const float4* __restrict__ map,
                                                   const Frame& F, f3 out[5]) {
     const int nT = g.nT, nP = g.nP, i = F.bi, j = F.bj;
     f3 P[3][3];
@@ -550,12 +559,7 @@ __device__ __forceinline__ void sample_map_multi5(const SbGrid& g, const float2*
 #pragma unroll
         for (int dc = -1; dc <= 1; ++dc) {
             const int col = (j + dc + shift) & g.maskP;
-            const float2 m = map[row * nP + col];
-            int dj = col - j;
-            dj = ((dj + nT) & g.maskP) - nT;
-            const float dth = (float)(row - i) + m.x;
-            const float dph = (float)dj + m.y;
-            P[dr + 1][dc + 1] = disp_from_offsets(F, dth, dph, g.h);
+            P[dr + 1][dc + 1] = map_point(g, F, map[row * nP + col], row, col);
         }
     }
     // (theta, phi) = (-1/4, -1/4): rows i-1, i; cols j-1, j; fractions 3/4
@@ -573,7 +577,8 @@ __device__ __forceinline__ void sample_map_multi5(const SbGrid& g, const float2*
 __device__ __forceinline__ Frame cell_frame(const SbGrid& g, int i, int j) {
     Frame F;
     F.bi = i; F.bj = j; F.fi = 0.5f; F.fj = 0.0f;
-    F.s0 = g.sin_c[i]; F.c0 = g.cos_c[i];
+    const float4 R = __ldg(&g.rowtab[i]);
+    F.s0 = R.x; F.s0lo = R.y; F.c0 = R.z; F.c0lo = R.w;
     return F;
 }
 

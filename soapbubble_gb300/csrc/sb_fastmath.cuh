@@ -135,4 +135,28 @@ __device__ __forceinline__ float fatan2(float y, float x) {
     return slow_atan2(y, x);
 }
 
+// fatan2 with the fast paths' quotient taken by __fdividef (reciprocal
+// and product, at most 2 ulp from the rounded quotient): for positions that
+// only select and weight samples (not stored in a characteristic map),
+// where 2 ulp of an offset of a few cells is ~1e-6 of a cell.
+__device__ __forceinline__ float fatan2_fast(float y, float x) {
+    if (x > 0.0f && fabsf(y) <= 0.25f * x) {
+        const float t = __fdividef(y, x);
+        const float t2 = t * t;
+        if (t2 <= 0.00390625f) {
+            const float p = fmaf(t2, 2.0e-1f, -3.3333333333e-1f);  // -1/3 + t^2/5
+            return fmaf(p * t2, t, t);
+        }
+        float p = -6.6666666667e-2f;           // -1/15
+        p = fmaf(p, t2, 7.6923076923e-2f);     //  1/13
+        p = fmaf(p, t2, -9.0909090909e-2f);    // -1/11
+        p = fmaf(p, t2, 1.1111111111e-1f);     //  1/9
+        p = fmaf(p, t2, -1.4285714286e-1f);    // -1/7
+        p = fmaf(p, t2, 2.0e-1f);              //  1/5
+        p = fmaf(p, t2, -3.3333333333e-1f);    // -1/3
+        return fmaf(p * t2, t, t);
+    }
+    return slow_atan2(y, x);
+}
+
 }  // namespace sb

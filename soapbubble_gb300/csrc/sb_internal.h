@@ -53,7 +53,10 @@ struct SbFields {
     float *eta_adv, *gam_adv, *uth_adv, *uph_adv;  // after advection
     SbScalar *eta_init, *eta_initL, *gam_init, *gam_initL;
     float *eta_delta, *eta_deltaL, *gam_delta, *gam_deltaL;
-    float2 *fwd[2], *bwd[2], *bwdprev;             // map offsets (ping-pong)
+    // characteristic maps (ping-pong): per cell the mapped point's
+    // displacement from the cell centre in the cell's own frame (x, y, z, 0),
+    // see sb_device.cuh
+    float4 *fwd[2], *bwd[2], *bwdprev;
     float *uair_init, *vair_init, *corr_u, *corr_v;
     float *uair, *vair;                            // N+1, Nv+1 (last element 0)
     float *d_eta, *d_gam, *err_eta, *err_gam;  // per-step increments, re-initialisation errors

@@ -37,6 +37,7 @@ __device__ __forceinline__ Frame face_frame_uphi(const SbGrid& g, int i, int j) 
     Frame F;
     F.bi = i; F.bj = j; F.fi = 0.5f; F.fj = -0.5f;
     F.s0 = g.sin_c[i]; F.c0 = g.cos_c[i];
+    F.s0lo = 0.0f; F.c0lo = 0.0f;
     return F;
 }
 
@@ -44,6 +45,7 @@ __device__ __forceinline__ Frame face_frame_utheta(const SbGrid& g, int i, int j
     Frame F;
     F.bi = i + 1; F.bj = j; F.fi = 0.0f; F.fj = 0.0f;
     F.s0 = g.sin_e[i + 1]; F.c0 = g.cos_e[i + 1];
+    F.s0lo = 0.0f; F.c0lo = 0.0f;
     return F;
 }
 
@@ -79,13 +81,13 @@ __device__ __forceinline__ void advect_maps_cell(const SbGrid& g, const SbPhys& 
         // forward map: trace forward in time (negative step), sample the old map
         const Trace Tf = trace_gc(g, f.uth, f.uph, F, gt, gp, -dt);
         const f3 df = sample_map(g, f.fwd[cur], F, pos_of(F, Tf, g));
-        f.fwd[cur ^ 1][idx] = map_entry_from_disp(g, F, df);
+        f.fwd[cur ^ 1][idx] = make_float4(df.x, df.y, df.z, 0.0f);  // in the cell's own frame
 
         // backward map and gamma share the backward trace
         const Trace Tb = trace_gc(g, f.uth, f.uph, F, gt, gp, dt);
         const CStencil cb = centred_stencil(g, pos_of(F, Tb, g), 0.0f);
-        const f3 db = map_at_stencil(f.bwd[cur], F, cb, g.nT, g.h);
-        f.bwd[cur ^ 1][idx] = map_entry_from_disp(g, F, db);
+        const f3 db = map_at_stencil(g, f.bwd[cur], F, cb);
+        f.bwd[cur ^ 1][idx] = make_float4(db.x, db.y, db.z, 0.0f);
         f.gam_adv[idx] = gather_s<T>(f.gam, sstencil_of(g, cb), ph.base_gam);
     }
 
@@ -107,10 +109,10 @@ __device__ __forceinline__ float advect_velocity(const SbGrid& g, const float* _
     const f3 w = {F.s0, 0.0f, F.c0};
     // a zero or NaN speed stops the trace; the reference then writes that
     // speed (bubble.cu:689-692, 727-730)
-    const Trace T = trace_gc(g, uth, uph, F, gt, gp, dt, rk2);
+    const Trace T = trace_gc<true>(g, uth, uph, F, gt, gp, dt, rk2);
     if (!T.moved) return T.fail;
     const f3 P = w + T.d;
-    const Pos qp = pos_from_disp(F, T.d, g.invh, g.nT);
+    const Pos qp = pos_from_disp_fast(F, T.d, g.invh, g.nT);
     float pt, pp;
     velocity_at(g, uth, uph, qp, pt, pp);
     f3 beth, beph;
@@ -164,9 +166,9 @@ __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, c
     float attrib = 0.0f;
 #pragma unroll 1
     for (int k = 0; k < 5; ++k) {
-        const CStencil c1 = centred_stencil(g, pos_from_disp(F, d1s[k], g.invh, g.nT), 0.0f);
-        const f3 d2 = map_at_stencil(f.bwdprev, F, c1, g.nT, g.h);
-        const Pos q2 = pos_from_disp(F, d2, g.invh, g.nT);
+        const CStencil c1 = centred_stencil(g, pos_from_disp_fast(F, d1s[k], g.invh, g.nT), 0.0f);
+        const f3 d2 = map_at_stencil(g, f.bwdprev, F, c1);
+        const Pos q2 = pos_from_disp_fast(F, d2, g.invh, g.nT);
         const SStencil s1 = sstencil_of(g, c1);
         const SStencil s2 = scalar_stencil(g, q2);
         const float sDelta = gather(f.eta_delta, s1);
@@ -586,15 +588,15 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
                                            int idx) {
     const int i = idx >> g.logP, j = idx & g.maskP;
     const Frame F = cell_frame(g, i, j);
-    const float2* fwd = f.fwd[cur ^ 1];
-    const float2* bwd = f.bwd[cur ^ 1];
+    const float4* fwd = f.fwd[cur ^ 1];
+    const float4* bwd = f.bwd[cur ^ 1];
     float ed = f.eta_delta[idx], gd = f.gam_delta[idx];
     float th = 0.0f, gm = 0.0f;
     f3 ds[5];
     sample_map_multi5(g, fwd, F, ds);
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-        const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
+        const SStencil s = scalar_stencil(g, pos_from_disp_fast(F, ds[k], g.invh, g.nT));
         ed += kW5[k] * gather(f.d_eta, s);
         gd += kW5[k] * gather(f.d_gam, s);
         th += kW5[k] * gather_s<T>(f.eta, s, ph.base_eta);
@@ -605,10 +607,12 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
     f.err_eta[idx] = (th - ed - ld_s<T>(f.eta_init, idx, ph.base_eta)) * 0.5f;
     f.err_gam[idx] = (gm - gd - ld_s<T>(f.gam_init, idx, ph.base_gam)) * 0.5f;
     // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
-    float2 m = fwd[idx];
-    const float d1 = dist_from_disp(sample_map(g, bwd, F, frame_pos(F, m.x, m.y)), g.invh);
+    float4 m = fwd[idx];
+    const float d1 = dist_from_disp(
+        sample_map(g, bwd, F, pos_from_disp_fast(F, f3{m.x, m.y, m.z}, g.invh, g.nT)), g.invh);
     m = bwd[idx];
-    const float d2 = dist_from_disp(sample_map(g, fwd, F, frame_pos(F, m.x, m.y)), g.invh);
+    const float d2 = dist_from_disp(
+        sample_map(g, fwd, F, pos_from_disp_fast(F, f3{m.x, m.y, m.z}, g.invh, g.nT)), g.invh);
     const float dist = fmaxf(fabsf(d1), fabsf(d2));
     return isnan(dist) ? 0.0f : dist;
 }
@@ -728,14 +732,14 @@ __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbPhys& ph
                                                int idx) {
     const int i = idx >> g.logP, j = idx & g.maskP;
     const Frame F = cell_frame(g, i, j);
-    const float2* bwd = f.bwd[cur ^ 1];
+    const float4* bwd = f.bwd[cur ^ 1];
     const float be = ph.base_eta, bg = ph.base_gam;
     float th = ld_s<T>(f.eta, idx, be), gm = ld_s<T>(f.gam, idx, bg);
     f3 ds[5];
     sample_map_multi5(g, bwd, F, ds);
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-        const SStencil s = scalar_stencil(g, pos_from_disp(F, ds[k], g.invh, g.nT));
+        const SStencil s = scalar_stencil(g, pos_from_disp_fast(F, ds[k], g.invh, g.nT));
         th -= kW5[k] * gather(f.err_eta, s);
         gm -= kW5[k] * gather(f.err_gam, s);
     }
@@ -768,8 +772,8 @@ __device__ __forceinline__ void reinit_commit(const SbPhys& ph, const SbFields& 
     st_s<T>(f.gam_init, idx, gm, ph.base_gam);
     f.gam_delta[idx] = 0.0f;
     f.bwdprev[idx] = f.bwd[cur ^ 1][idx];
-    f.fwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
-    f.bwd[cur ^ 1][idx] = make_float2(0.0f, 0.0f);
+    f.fwd[cur ^ 1][idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    f.bwd[cur ^ 1][idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // reInitializeMapping (kernel/bubble.cu:2509-2564) for every bubble of the
@@ -847,7 +851,7 @@ __global__ void k_barrier_probe(SbBubbleDesc* d, int absent, unsigned limit) {
 __global__ void k_reset_maps(SbGrid g, SbFields f) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= g.N) return;
-    const float2 z = make_float2(0.0f, 0.0f);
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     f.fwd[0][idx] = z; f.fwd[1][idx] = z;
     f.bwd[0][idx] = z; f.bwd[1][idx] = z;
     f.bwdprev[idx] = z;

@@ -14,6 +14,11 @@ struct SbGrid {
     const float* cos_c;
     const float* sin_e;       // sin(i h), i <= nT (row edges; u_theta faces at i + 1)
     const float* cos_e;
+    // tables of the characteristic-map geometry (FP64 values rounded on the host):
+    const float4* rowtab;     // per row i < nT: sin and cos of (i + 0.5) h as (hi, lo) pairs:
+                              // (sin hi, sin lo, cos hi, cos lo)
+    const float2* rottab;     // per column offset dc in [-nT, nT) at index dc + nT:
+                              // (sin(dc h), cos(dc h) - 1)
 };
 
 // Scalars that change per step (kept in device memory so a captured graph
