@@ -43,26 +43,27 @@ NTHETA, DT, RECIPE, SEED = 512, 0.002, "c1", 20261203
 STEPS_PER_FRAME = 10
 L2_FLUSH_BYTES = 512 << 20
 
-# Algorithmic bytes per cell and launch (FP32 = 4 B, map entry = 8 B; every
-# array a kernel must read or write counted once; halo re-reads excluded).
+# Algorithmic bytes per cell and launch (every array a kernel must read or
+# write counted once; halo re-reads excluded)
+# (FP32 = 4 B, map entry = 16 B: a float4 displacement).
 ALG_BYTES_PER_CELL = {
-    "k_advect_maps": 72,  # u_th,u_ph,fwd,bwd,gamma,uair0,corr_u,vair0,corr_v -> fwd',bwd',gamma',uair,vair
-    "k_velocity": 16,     # u_th,u_ph -> u_th',u_ph'
-    "k_bimocq": 40,       # eta,bwd',bwdprev,init,delta,initLast,deltaLast -> eta'
-    "k_assemble": 44,     # eta',gamma',u_th',u_ph',uair,vair -> dmass,cE,cS,r0,b
-    "k_post": 56,         # gamma',x,dx,eta',u_th',u_ph',uair,vair -> gamma,dgamma,eta,deta,u_th,u_ph
-    "k_accum": 64,        # eta_delta,gamma_delta,fwd',bwd',deta,dgamma,eta,gamma,eta_init,gamma_init
-                          # -> eta_delta,gamma_delta,err_eta,err_gamma
+    "k_advect_maps": 104,  # u_th,u_ph,fwd,bwd,gamma,uair0,corr_u,vair0,corr_v -> fwd',bwd',gamma',uair,vair
+    "k_velocity": 16,      # u_th,u_ph -> u_th',u_ph'
+    "k_bimocq": 56,        # eta,bwd',bwdprev,init,delta,initLast,deltaLast -> eta'
+    "k_assemble": 44,      # eta',gamma',u_th',u_ph',uair,vair -> dmass,cE,cS,r0,b
+    "k_post": 64,          # gamma',x,dx,xff(8),eta',u_th',u_ph',uair,vair -> gamma,dgamma,eta,deta,u_th,u_ph
+    "k_accum": 80,         # eta_delta,gamma_delta,fwd',bwd',deta,dgamma,eta,gamma,eta_init,gamma_init
+                           # -> eta_delta,gamma_delta,err_eta,err_gamma
     "k_reinit": 0,        # no traffic unless re-initialising (about 1 step in 10)
 }
-# The implicit solve, per cell.  Fixed: set-up (r0, rhs, dmass, cE, cS ->
-# x (float-float), r, q, z or z1 = 40), the final true-residual check (x, r0,
+# The implicit solve, per cell.  Fixed: set-up (r0, rhs, dmass, cE, cS, the
+# previous increment dx -> x (float-float), r, q, z or z1 = 44), the final true-residual check (x, r0,
 # dmass, cE, cS -> r = 28) and the result (x, gamma_adv -> dx, gamma = 20).
 # Per CG iteration: q = A p (z, p, dmass, cE, cS -> p, q = 28) and the update
 # with the line solve (p, r, q, x -> x, r, z or z1 = 36).  With the Neumann
 # term, one more phase per iteration and one at the start (z1, cS, r -> z =
 # 16).  Keyed by the preconditioner a solve used (1: line, 2: Neumann).
-PCG_BYTES = {1: (88, 64), 2: (104, 80)}
+PCG_BYTES = {1: (92, 64), 2: (108, 80)}
 ROOFLINE_NOTES = {
     "k_solve": "latency-bound, not HBM-bound: the solve's vectors and factors stay in L2 and in "
                "shared memory across its iterations (DRAM traffic per launch is their first touch "

@@ -349,6 +349,18 @@ int set_step_params(sb_bubble* b, double t, double dt_s) {
     return write_step_params(b, t, dt_s, b->stream);
 }
 
+// The next solve starts from dx = 0: the state it would warm-start from has
+// been replaced (a field upload or initialiser).
+int invalidate_warm_start(sb_bubble* b, cudaStream_t s) {
+    SB_CHECK(cudaMemsetAsync(&b->f.stats->dx_valid, 0, sizeof(int), s));
+    return SB_OK;
+}
+
+// Fields that define the state a solve warm-starts from (not the wind).
+bool state_field(sb_field w) {
+    return !(w == SB_UAIR_INIT || w == SB_VAIR_INIT || w == SB_UAIR || w == SB_VAIR);
+}
+
 int reset_bimocq(sb_bubble* b) {
     const size_t N = (size_t)b->g.N * scalar_bytes(b->storage), N4 = (size_t)b->g.N * 4;
     SbFields& f = b->f;
@@ -361,7 +373,7 @@ int reset_bimocq(sb_bubble* b) {
     SB_CHECK(cudaMemsetAsync(f.gam_delta, 0, N4, b->stream));
     SB_CHECK(cudaMemsetAsync(f.gam_deltaL, 0, N4, b->stream));
     SB_CHECK(launch_reset_maps(b->g, b->f, b->stream));
-    return SB_OK;
+    return invalidate_warm_start(b, b->stream);
 }
 
 int upload_f32(sb_bubble* b, float* dst, const double* src, size_t n) {
@@ -719,6 +731,10 @@ int sb_upload_field(sb_bubble* b, sb_field which, const double* src, size_t n) {
     if (!b || !src) return fail(SB_ERR_INVALID, "null argument");
     if (n != sb_field_size(b, which)) return fail(SB_ERR_INVALID, "element count mismatch");
     SB_CHECK(cudaSetDevice(b->device));
+    if (state_field(which)) {
+        int r = invalidate_warm_start(b, b->stream);
+        if (r != SB_OK) return r;
+    }
     int comp = 0;
     float4* m = map_ptr(b, which, comp);
     if (m) {
@@ -972,6 +988,10 @@ int take_staged_uploads(sb_bubble* b, cudaStream_t s) {
         }
         SB_CHECK(cudaEventRecord(b->stage_ev[kUpTaken][w], s));
         b->up_pending[w] = false;
+        if (state_field(which)) {
+            int r = invalidate_warm_start(b, s);
+            if (r != SB_OK) return r;
+        }
     }
     return SB_OK;
 }
@@ -1097,6 +1117,10 @@ int sb_upload_field_f32(sb_bubble* b, sb_field which, const float* src, size_t n
                  : fptr(b, which);
     if (!d) return fail(SB_ERR_INVALID, "maps move through sb_upload_field");
     SB_CHECK(cudaSetDevice(b->device));
+    if (state_field(which)) {
+        int r = invalidate_warm_start(b, b->stream);
+        if (r != SB_OK) return r;
+    }
     SB_CHECK(cudaMemcpyAsync(d, src, n * sizeof(float), cudaMemcpyHostToDevice, b->stream));
     if (s && b->storage != kStoreF32) return store_from_staging(b, s, n);
     return SB_OK;

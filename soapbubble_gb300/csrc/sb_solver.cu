@@ -529,11 +529,20 @@ __device__ __forceinline__ const float* row_blob(const SbGrid& g, const SbFields
 // of a thread's columns first, which costs registers).  Dot-product terms
 // are accumulated in column order.
 
-// dx = 0, r = r0, p_old = 0; rv = r; adds |rhs|^2 to bb.
+// The initial iterate and residual, p_old = 0; rv = r; adds |rhs|^2 to bb.
+// The iterate starts from the previous step's increment dx when the state
+// has not been replaced since (stats->dx_valid, the same in every block
+// during a solve): the increment of gamma changes little from one step to
+// the next, so r = r0 - A dx_prev is much smaller than r0 and the solve
+// needs fewer iterations; it stops at the same relative residual of the
+// same system.  Otherwise it starts from dx = 0 (gamma_new = gamma_adv).
+// dx itself is only read here (the plain mode's iterate already holds it),
+// so the neighbours' values are those of the previous solve in every block.
 template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int i,
                                          float (&rv)[PER], ff& bb) {
-    const int nP = g.nP, row = i * nP;
+    const int nP = g.nP, nT = g.nT, row = i * nP;
+    const bool warm = f.stats->dx_valid != 0;
     ff h[2] = {ff_zero(), ff_zero()};
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
@@ -541,11 +550,22 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
         rv[k] = 0.0f;
         if (j < nP) {
             const int c = row + j;
-            rv[k] = f.r0[c];
+            float r = f.r0[c];
             const float rhs = f.rhs[c];
-            if (MIXED) f.xff[c] = make_float2(0.0f, 0.0f);
-            else f.dx[c] = 0.0f;
-            f.r[c] = rv[k];
+            if (warm) {
+                const float x0 = f.dx[c];
+                const int e = row + ((j + 1) & g.maskP), w = row + ((j - 1) & g.maskP);
+                float ax = f.dmass[c] * x0 + f.cE[c] * (x0 - f.dx[e]) + f.cE[w] * (x0 - f.dx[w]);
+                if (i < nT - 1) ax += f.cS[c] * (x0 - f.dx[c + nP]);
+                if (i > 0) ax += f.cS[c - nP] * (x0 - f.dx[c - nP]);
+                r -= ax;
+                if (MIXED) f.xff[c] = make_float2(x0, 0.0f);
+            } else {
+                if (MIXED) f.xff[c] = make_float2(0.0f, 0.0f);
+                else f.dx[c] = 0.0f;
+            }
+            rv[k] = r;
+            f.r[c] = r;
             f.q[c] = 0.0f;
             h[half_of<TB>(k)] = ff_add_prod(h[half_of<TB>(k)], rhs, rhs);
         }
@@ -604,19 +624,16 @@ __device__ __forceinline__ ff row_spmv(const SbGrid& g, const SbFields& f, int i
                 if (hasN) qf += cn[u] * (pc - (zn[u] + beta * pn[u]));
                 pnew[cc[u]] = pc;
                 qout[cc[u]] = qf;
+                // p.q = p^T A p in its energy form: dmass p^2 plus w (p_c -
+                // p_n)^2 over each east and south face once, every term
+                // non-negative.  The sum of the products p_c q_c of the FP32
+                // q = A p cancels to almost nothing on ruptured films
+                // (weights 1e5 times the mass terms) and could lose its
+                // sign there, which broke the iteration down.
                 ff& h = pq[half_of<TB>(k0 + u)];
-                if (MIXED) {
-                    h = ff_add_prod(h, pc, qf);  // exact products: p.q as the sum of p_c q_c
-                } else {
-                    // plain FP32: p.q = p^T A p in its energy form, every term
-                    // non-negative (each east and south face once).  The sum
-                    // of the rounded products p_c q_c cancels to nothing on
-                    // ruptured films (weights 1e5 times the mass terms) and
-                    // lost its sign there, breaking the iteration down.
-                    h = ff_add_f(h, __fmul_rn(dm[u] * pc, pc));
-                    h = ff_add_f(h, __fmul_rn(ce[u] * dE, dE));
-                    if (hasS) h = ff_add_f(h, __fmul_rn(cs[u] * dS, dS));
-                }
+                h = acc<MIXED>(h, dm[u] * pc, pc);
+                h = acc<MIXED>(h, ce[u] * dE, dE);
+                if (hasS) h = acc<MIXED>(h, cs[u] * dS, dS);
             }
         }
     }
@@ -1373,6 +1390,7 @@ k_solve(SbSolveSet S, SolverConfig cfg) {
         if (i0 >= i1) continue;
         stage_desc(S, b, &s_d);
         for (int i = i0; i < i1; ++i) row_final<MIXED, PER, TB>(s_d.g, s_d.f, i);
+        if (i0 == 0 && threadIdx.x == 0) s_d.f.stats->dx_valid = 1;
         __syncthreads();
     }
 }
@@ -1436,6 +1454,7 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
     if (!grid_barrier(S.bar, gen, G, &f.stats->wait_faults)) return;
     if (blockIdx.x == 0) acc_zero(S.acc, kSolveAccWords, threadIdx.x, blockDim.x);
     for (int i = blockIdx.x; i < nT; i += G) row_final<MIXED, PER, TB>(g, f, i);
+    if (blockIdx.x == 0 && threadIdx.x == 0) f.stats->dx_valid = 1;
 }
 
 template <bool MIXED>

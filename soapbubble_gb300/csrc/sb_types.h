@@ -66,6 +66,9 @@ struct SbDevStats {
     long long solver_nonconverged; // solves that missed their tolerance since the last reset
     double solver_resid_max;       // largest relative residual since the last reset
     long long steps_done;          // steps completed (map parity flips) since creation
+    int dx_valid;                  // 1: dx holds the last solve's increment of this state
+                                   // (the next solve starts from it); uploads clear it
+    int pad_;
 };
 
 }  // namespace sb

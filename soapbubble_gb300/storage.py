@@ -24,12 +24,12 @@ from .bubble import GpuBubble, bytes_required, make_params, stage_names
 # entry = 8 B, a stored field 4 or 2 B).  s = bytes of a stored element.
 def alg_bytes(s: int) -> dict:
     return {
-        "k_advect_maps": 68 + s,      # gamma sampled in the stored type
+        "k_advect_maps": 100 + s,     # gamma sampled in the stored type; maps 16 B
         "k_velocity": 16,
-        "k_bimocq": 28 + 3 * s,       # bwd', bwdprev, 2 deltas, eta_adv + eta, init, initL
+        "k_bimocq": 44 + 3 * s,       # bwd', bwdprev (16 B), 2 deltas, eta_adv + eta, init, initL
         "k_assemble": 44,
-        "k_post": 48 + 2 * s,         # eta, gamma written in the stored type
-        "k_accum": 48 + 4 * s,        # deltas, maps, changes, errors + eta, gamma, inits
+        "k_post": 56 + 2 * s,         # eta, gamma written in the stored type; xff read
+        "k_accum": 64 + 4 * s,        # deltas, maps (16 B), changes, errors + eta, gamma, inits
     }
 
 
