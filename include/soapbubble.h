@@ -375,6 +375,16 @@ int sb_batch_step_timed(sb_batch* batch, int n_steps, double t_frame, double dt,
  * receives the choice.  The tuning steps advance the members (3 steps). */
 int sb_batch_autotune(sb_batch* batch, double t_frame, double dt, int* tile_sizes);
 
+/* Takes member `member` (its index in sb_batch_create's list) out of the
+ * batch's work without rebuilding the batch: from the next step on every
+ * kernel of the batch leaves it untouched (its state can still be read, and
+ * the other members' results do not change).  The member must stay alive
+ * until the batch is destroyed; it takes part again in a batch created
+ * later.  Synchronises.  No counterpart in the reference; a serving loop
+ * retires finished requests this way and rebuilds its batch only when
+ * requests join. */
+int sb_batch_retire(sb_batch* batch, int member);
+
 int sb_batch_synchronize(sb_batch* batch);
 
 /* CUDA stream of the batch (cudaStream_t). */

@@ -115,6 +115,7 @@ def lib() -> C.CDLL:
     L.sb_batch_step_each.argtypes = [H, C.c_int, dp, C.c_double]
     L.sb_batch_autotune.argtypes = [H, C.c_double, C.c_double, ip]
     L.sb_batch_synchronize.argtypes = [H]
+    L.sb_batch_retire.argtypes = [H, C.c_int]
     L.sb_batch_stream.argtypes = [H]
     L.sb_batch_stream.restype = C.c_void_p
     L.sb_init_thickness_from_exr.argtypes = [H, C.c_char_p]
@@ -131,7 +132,7 @@ def lib() -> C.CDLL:
                  "sb_download_field_f32", "sb_synchronize", "sb_reset_stats",
                  "sb_selftest_grid_barrier", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
-                 "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
+                 "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize", "sb_batch_retire",
                  "sb_init_thickness_from_exr", "sb_init_airflow_from_exr", "sb_exr_load_resized",
                  "sb_write_velocity_exr", "sb_write_concentration_exr", "sb_stage_upload_f32",
                  "sb_stage_download_f32", "sb_wait_staged"):
@@ -154,6 +155,6 @@ EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
            "sb_run", "sb_write_exr_gray", "sb_mass_integrals_noalloc", "sb_bytes_required",
            "sb_stream", "sb_last_error", "sb_batch_create", "sb_batch_destroy", "sb_batch_step",
            "sb_batch_step_timed", "sb_batch_step_each", "sb_batch_autotune", "sb_batch_synchronize",
-           "sb_batch_stream", "sb_init_thickness_from_exr", "sb_init_airflow_from_exr",
+           "sb_batch_retire", "sb_batch_stream", "sb_init_thickness_from_exr", "sb_init_airflow_from_exr",
            "sb_exr_load_resized", "sb_write_velocity_exr", "sb_write_concentration_exr",
            "sb_stage_upload_f32", "sb_stage_download_f32", "sb_wait_staged"]

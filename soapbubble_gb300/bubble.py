@@ -269,6 +269,10 @@ class GpuBatch:
     def synchronize(self) -> None:
         check(lib().sb_batch_synchronize(self.h), "sb_batch_synchronize")
 
+    def retire(self, k: int) -> None:
+        """sb_batch_retire: member k leaves the batch's work (no rebuild)."""
+        check(lib().sb_batch_retire(self.h, k), "sb_batch_retire")
+
     def stream(self) -> int:
         return lib().sb_batch_stream(self.h)
 

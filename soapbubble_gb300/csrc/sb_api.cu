@@ -1550,8 +1550,11 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
     S.cnt = (int*)(A + o_cnt);
     S.acc = (unsigned long long*)(A + o_acc);
     S.bar = (unsigned*)(A + o_bar);
-    // members may have work queued on their own streams
+    // members may have work queued on their own streams; a member retired
+    // from an earlier batch takes part again
     for (sb_bubble* b : B->m) e = e == cudaSuccess ? cudaStreamSynchronize(b->stream) : e;
+    for (sb_bubble* b : B->m)
+        if (e == cudaSuccess) e = cudaMemset(&b->f.self->halted, 0, sizeof(int));
     if (e == cudaSuccess)
         e = cudaMemcpy((void*)P.descs, descs.data(), sizeof(SbBubbleDesc*) * n, cudaMemcpyHostToDevice);
     for (int s = 0; s < 3 && e == cudaSuccess; ++s)
@@ -1636,6 +1639,17 @@ int sb_batch_autotune(sb_batch* B, double t_frame, double dt, int* tile_sizes) {
         B->graph = nullptr;
     }
     return rc;
+}
+
+int sb_batch_retire(sb_batch* B, int member) {
+    if (!B) return fail(SB_ERR_INVALID, "null batch");
+    if (member < 0 || member >= (int)B->m.size()) return fail(SB_ERR_INVALID, "no such member");
+    SB_CHECK(cudaSetDevice(B->device));
+    static const int one = 1;
+    SB_CHECK(cudaMemcpyAsync(&B->m[member]->f.self->halted, &one, sizeof(int),
+                             cudaMemcpyHostToDevice, B->stream));
+    SB_CHECK(cudaStreamSynchronize(B->stream));
+    return SB_OK;
 }
 
 int sb_batch_synchronize(sb_batch* B) {

@@ -1092,7 +1092,8 @@ __device__ __forceinline__ unsigned active_prefix(const SbSolveSet& S, int p, un
         const int b = base + threadIdx.x;
         unsigned v = 0;
         if (b < S.nb) {
-            const bool act = p <= 0 || __ldcg(&S.done_at[b]) > p;
+            // a member retired from its batch (halted) takes no part
+            const bool act = (p <= 0 || __ldcg(&S.done_at[b]) > p) && !__ldcg(&S.descs[b]->halted);
             if (act) v = (unsigned)(S.roff[b + 1] - S.roff[b]) * row_weight(S.roff[b + 1] - S.roff[b]);
         }
         unsigned incl = v;

@@ -5,7 +5,9 @@ size, step count, coefficients and initial fields (the payload).  The loop
 admits waiting requests first come first served while their device memory
 fits the HBM budget, keeps every admitted bubble resident, and steps all
 resident bubbles together as one set (one launch per stage, one CUDA graph
-per step; the set is rebuilt when a request joins or leaves).  Each member
+per step; the set is rebuilt when requests join, and a finished request is
+retired from it without a rebuild: the kernels skip it until the next
+rebuild, when its bubble is freed).  Each member
 runs at its own frame time.  Admission happens at frame boundaries (every
 10 steps), so all members stay on the same frame grid; a thickness frame of
 every member is streamed to the host every 10 of its steps, and its final
@@ -152,6 +154,8 @@ class Server:
         waiting: List[Request] = []
         ready: List[Active] = []  # made while the GPU ran a frame, not yet in the set
         active: List[Active] = []
+        members: List[Active] = []   # the batch's members in its order (retired ones too)
+        retired: List[Active] = []   # finished, retired from the batch, freed at the next rebuild
         results: Dict[int, Result] = {}
         batch: Optional[GpuBatch] = None
         admitted_at: Dict[int, float] = {}
@@ -203,14 +207,19 @@ class Server:
                 if changed:
                     if batch is not None:
                         batch.close()
-                    batch = GpuBatch([a.bubble for a in active])
+                    for a in retired:
+                        a.bubble.close()
+                        self.resident_bytes -= bytes_required(params_of(a.req, device=self.device))
+                    retired.clear()
+                    members = list(active)
+                    batch = GpuBatch([a.bubble for a in members])
                     self.rebuilds += 1
                     changed = False
                     self.max_members = max(self.max_members, len(active))
                     self.max_resident = max(self.max_resident, self.resident_bytes)
                 n = min(STEPS_PER_FRAME - g_step % STEPS_PER_FRAME,
                         min(a.req.steps - a.done for a in active))
-                batch.step(n, [frame_time(a.done) for a in active], DT)
+                batch.step(n, [frame_time(a.done) for a in members], DT)
                 g_step += n
                 for a in active:
                     a.done += n
@@ -235,19 +244,24 @@ class Server:
                                (a.req.steps - 1) // STEPS_PER_FRAME,
                                eta if self.keep_eta else None)
                     results[a.req.rid] = r
-                    self.resident_bytes -= bytes_required(params_of(a.req, device=self.device))
                 if finished:
-                    if batch is not None:
+                    # retired from the batch in place; freed at the next rebuild
+                    for a in finished:
+                        batch.retire(next(k for k, m in enumerate(members) if m is a))
+                        retired.append(a)
+                    active = [a for a in active if a.done < a.req.steps]
+                    if not active:
                         batch.close()
                         batch = None
-                    for a in finished:
-                        a.bubble.close()
-                    active = [a for a in active if a.done < a.req.steps]
-                    changed = True
+                        for a in retired:
+                            a.bubble.close()
+                            self.resident_bytes -= bytes_required(params_of(a.req, device=self.device))
+                        retired.clear()
+                        members = []
         finally:
             if batch is not None:
                 batch.close()
-            for a in active + ready:
+            for a in active + ready + retired:
                 a.bubble.close()
         self.wall = now()
         self.cell_steps = cell_steps

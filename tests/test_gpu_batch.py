@@ -219,3 +219,31 @@ def test_wide_rows_batch_matches_members_stepped_alone(gpulib):
             assert ga.stats().solver_iters == gb.stats().solver_iters
     finally:
         _close(a + b)
+
+
+def test_retired_member_is_left_untouched(gpulib):
+    """sb_batch_retire: a member retired after 6 steps keeps its state while
+    the batch steps on, and the other members still match the same bubbles
+    stepped alone bit for bit (the retired member's rows leave the solve,
+    whose exact sums do not depend on which rows take part)."""
+    from soapbubble_gb300.bubble import GpuBatch
+    a, b = _twins(SMALL[:3], solver_tol=1e-6)
+    try:
+        with GpuBatch(a) as batch:
+            for k, (t, dt) in enumerate(_schedule(15, 0.005)):
+                if k == 6:
+                    batch.synchronize()
+                    kept = {n: a[1].download(n) for n in FIELDS}
+                    batch.retire(1)
+                batch.step(1, t, dt)
+                for i, g in enumerate(b):
+                    if i != 1 or k < 6:
+                        g.step(1, t, dt)
+            batch.synchronize()
+        for n in FIELDS:
+            np.testing.assert_array_equal(a[1].download(n), kept[n], err_msg=n)
+            for i in (0, 2):
+                np.testing.assert_array_equal(a[i].download(n), b[i].download(n), err_msg=n)
+        assert a[1].stats().steps == 6 and a[0].stats().steps == 15
+    finally:
+        _close(a + b)
