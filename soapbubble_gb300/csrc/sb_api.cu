@@ -1402,6 +1402,7 @@ const char* sb_last_error(void) { return g_err.c_str(); }
 
 struct sb_batch {
     std::vector<sb_bubble*> m;
+    std::vector<char> retired;  // members taken out by sb_batch_retire
     int device = 0;
     cudaStream_t stream = nullptr;
     char* arena = nullptr;
@@ -1434,9 +1435,12 @@ int batch_set_params(sb_batch* B, double t, double dt) {
     return batch_set_params_each(B, ts.data(), dt);
 }
 
+// The host mirrors (map parity, step and launch counts) of the members the
+// steps moved; a retired member's device state stays as it was.
 void batch_advance(sb_batch* B, int n) {
     B->steps += n;
-    for (sb_bubble* b : B->m) bubble_advance(b, n);
+    for (size_t k = 0; k < B->m.size(); ++k)
+        if (!B->retired[k]) bubble_advance(B->m[k], n);
 }
 
 }  // namespace
@@ -1483,6 +1487,7 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
             return fail(SB_ERR_INVALID, "batch members must share the viscous switch");
         }
         B->m.push_back(b);
+        B->retired.push_back(0);
         if (b->g.nP > P.maxNP) P.maxNP = b->g.nP;
     }
     // the row list of the solve: every member's theta rows, member by member
@@ -1649,6 +1654,7 @@ int sb_batch_retire(sb_batch* B, int member) {
     SB_CHECK(cudaMemcpyAsync(&B->m[member]->f.self->halted, &one, sizeof(int),
                              cudaMemcpyHostToDevice, B->stream));
     SB_CHECK(cudaStreamSynchronize(B->stream));
+    B->retired[member] = 1;
     return SB_OK;
 }
 
