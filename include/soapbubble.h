@@ -86,6 +86,10 @@ typedef struct {
     int solver_precond;       /* preconditioner of the implicit solve: 0 chooses per solve
                                  from the previous solve's iterations, 1 the exact phi-line
                                  blocks B alone, 2 B^-1 + B^-1 C B^-1 (C: the theta couplings) */
+    int solver_cold_start;    /* 1: every solve starts from a zero increment (gamma_new =
+                                 the advected gamma, as the reference's AmgX call starts from
+                                 gamma); 0: from the previous step's increment after a
+                                 converged solve of an unchanged state */
 } sb_params;
 
 enum { SB_STORE_FP32 = 0, SB_STORE_BF16 = 1 };

@@ -33,7 +33,7 @@ class SbParams(C.Structure):
         ("nu_scale", C.c_double), ("storage", C.c_int), ("plain_advection", C.c_int),
         ("single_step_velocity", C.c_int), ("viscous", C.c_int),
         ("write_velocity_frames", C.c_int), ("write_concentration_frames", C.c_int),
-        ("solver_precond", C.c_int),
+        ("solver_precond", C.c_int), ("solver_cold_start", C.c_int),
     ]
 
 

@@ -36,7 +36,7 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
                 device: int = 0, storage: int = 0, plain_advection: int = 0,
                 single_step_velocity: int = 0, viscous: int = 0,
                 write_velocity_frames: int = 0, write_concentration_frames: int = 0,
-                solver_precond: int = 0) -> SbParams:
+                solver_precond: int = 0, solver_cold_start: int = 0) -> SbParams:
     p = default_params()
     p.nTheta, p.dt, p.radius, p.H, p.Gamma_m, p.T = nTheta, dt, radius, H, Gamma_m, T
     p.blendCoeff = blendCoeff
@@ -52,6 +52,7 @@ def make_params(nTheta: int, dt: float, radius: float = 1.0, H: float = 1e-6,
     p.write_velocity_frames = write_velocity_frames
     p.write_concentration_frames = write_concentration_frames
     p.solver_precond = solver_precond  # 0 auto, 1 phi-line blocks, 2 with the Neumann term
+    p.solver_cold_start = solver_cold_start  # 1: every solve from a zero increment
     return p
 
 

@@ -507,6 +507,7 @@ int sb_create(const sb_params* p, sb_bubble** out) {
     b->solver.mode = p->solver_mode == 1 ? 0 : 1;
     b->solver.tol = p->solver_tol > 0 ? p->solver_tol : 1e-6;
     b->solver.max_iter = p->solver_max_iter > 0 ? p->solver_max_iter : 1000;
+    b->solver.warm = p->solver_cold_start ? 0 : 1;
     b->solver.precond = p->solver_precond == 1 ? kPrecLine
                         : p->solver_precond == 2 ? kPrecNeumann : kPrecAuto;
     b->force_reinit = p->force_reinit == 1 ? 0 : (p->force_reinit == 2 ? 1 : -1);
@@ -1474,7 +1475,7 @@ int sb_batch_create(sb_bubble* const* bubbles, int n, sb_batch** out) {
         }
         const SolverConfig& c = b->solver;
         if (c.mode != P.solver.mode || c.max_iter != P.solver.max_iter ||
-            c.tol != P.solver.tol || c.precond != P.solver.precond) {
+            c.tol != P.solver.tol || c.precond != P.solver.precond || c.warm != P.solver.warm) {
             delete B;
             return fail(SB_ERR_INVALID, "batch members must share one solver configuration");
         }

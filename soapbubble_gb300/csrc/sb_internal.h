@@ -103,6 +103,7 @@ struct SolverConfig {
     int max_iter;
     double tol;     // relative residual ||b - A x|| / ||b||
     int precond;    // kPrecLine, kPrecNeumann or kPrecAuto (sb_solver.cu)
+    int warm;       // 1: start from the previous increment when it is valid (row_init)
     int blob;       // bytes of a block's shared-memory factor blob (set at launch)
     float tol2f;    // target r.r / |b|^2 of the iterate (set at launch)
 };

@@ -530,19 +530,25 @@ __device__ __forceinline__ const float* row_blob(const SbGrid& g, const SbFields
 // are accumulated in column order.
 
 // The initial iterate and residual, p_old = 0; rv = r; adds |rhs|^2 to bb.
-// The iterate starts from the previous step's increment dx when the state
-// has not been replaced since (stats->dx_valid, the same in every block
-// during a solve): the increment of gamma changes little from one step to
-// the next, so r = r0 - A dx_prev is much smaller than r0 and the solve
-// needs fewer iterations; it stops at the same relative residual of the
-// same system.  Otherwise it starts from dx = 0 (gamma_new = gamma_adv).
-// dx itself is only read here (the plain mode's iterate already holds it),
-// so the neighbours' values are those of the previous solve in every block.
+// With warm starts on, the iterate starts from the previous step's
+// increment dx when the previous solve converged and the state has not
+// been replaced since (stats->dx_valid and solver_converged, the same in
+// every block during a solve): the increment of gamma changes little from
+// one step to the next, so r = r0 - A dx_prev is much smaller than r0 and
+// the solve needs fewer iterations; it stops at the same relative residual
+// of the same system.  A non-finite previous value starts from zero.
+// Otherwise the iterate starts from dx = 0 (gamma_new = gamma_adv).  dx
+// itself is only read here (the plain mode's iterate already holds it), so
+// the neighbours' values are those of the previous solve in every block.
 template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int i,
-                                         float (&rv)[PER], ff& bb) {
+                                         const SolverConfig& cfg, float (&rv)[PER], ff& bb) {
     const int nP = g.nP, nT = g.nT, row = i * nP;
-    const bool warm = f.stats->dx_valid != 0;
+    const bool warm = cfg.warm && f.stats->dx_valid != 0 && f.stats->solver_converged != 0;
+    auto prev = [&](int c) {
+        const float v = f.dx[c];
+        return isfinite(v) ? v : 0.0f;
+    };
     ff h[2] = {ff_zero(), ff_zero()};
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
@@ -553,13 +559,14 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
             float r = f.r0[c];
             const float rhs = f.rhs[c];
             if (warm) {
-                const float x0 = f.dx[c];
+                const float x0 = prev(c);
                 const int e = row + ((j + 1) & g.maskP), w = row + ((j - 1) & g.maskP);
-                float ax = f.dmass[c] * x0 + f.cE[c] * (x0 - f.dx[e]) + f.cE[w] * (x0 - f.dx[w]);
-                if (i < nT - 1) ax += f.cS[c] * (x0 - f.dx[c + nP]);
-                if (i > 0) ax += f.cS[c - nP] * (x0 - f.dx[c - nP]);
+                float ax = f.dmass[c] * x0 + f.cE[c] * (x0 - prev(e)) + f.cE[w] * (x0 - prev(w));
+                if (i < nT - 1) ax += f.cS[c] * (x0 - prev(c + nP));
+                if (i > 0) ax += f.cS[c - nP] * (x0 - prev(c - nP));
                 r -= ax;
                 if (MIXED) f.xff[c] = make_float2(x0, 0.0f);
+                else if (x0 != f.dx[c]) f.dx[c] = x0;  // only where it was not finite
             } else {
                 if (MIXED) f.xff[c] = make_float2(0.0f, 0.0f);
                 else f.dx[c] = 0.0f;
@@ -1224,7 +1231,7 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
     switch (kind) {
         case K_SETUP:
         case K_SETUP_L:
-            row_init<MIXED, PER, TB>(g, f, i, rv, c2);
+            row_init<MIXED, PER, TB>(g, f, i, cfg, rv, c2);
             precondition_row<PER, TB, true>(g, f, i, St, rv);
             break;
         case K_NEUMANN: {
