@@ -126,6 +126,39 @@ def test_bf16_run_stays_near_fp32(gpulib):
         b.close()
 
 
+def test_bf16_drift_over_the_c2_run_is_the_flows_sensitivity(gpulib):
+    """Config c2 (1024 x 2048, dt 0.001 s), 100 steps.  The c2 flow
+    amplifies any perturbation of its initial thickness about seventyfold
+    over 100 steps: an FP32 run started from the BF16-rounded initial
+    fields (4e-4 from the exact ones) ends 2.9e-2 from the FP32 run.  BF16
+    storage, which also rounds every step, ends 5.6e-2 away (measured on a
+    GB300).  The bound: the BF16 run stays within 3x the drift that the
+    initial rounding alone causes, and within 0.1 of the FP32 thickness."""
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    nT, dt = 1024, 0.001
+    f = synth.make_fields("c2", nT, 20261203)
+
+    def run(storage, eta, gamma):
+        gb = GpuBubble(make_params(nT, dt, solver_tol=1e-6, storage=storage))
+        try:
+            gb.upload_fields(eta, gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+            init = (gb.download("eta"), gb.download("gamma"))
+            for k in range(100):
+                gb.step(1, (k // 10) * 10 * dt, dt)
+            return gb.download("eta"), init
+        finally:
+            gb.close()
+
+    fp32, _ = run(0, f.eta, f.gamma)
+    bf16, (e0, g0) = run(1, f.eta, f.gamma)
+    fp32_rounded_start, _ = run(0, e0, g0)
+    d_bf16 = P.rel_err(bf16, fp32)
+    d_start = P.rel_err(fp32_rounded_start, fp32)
+    assert np.isfinite(bf16).all()
+    assert d_bf16 <= 3.0 * d_start and d_bf16 <= 0.1, (d_bf16, d_start)
+
+
 def test_bf16_batch_matches_members_stepped_alone(gpulib):
     from soapbubble_gb300.bubble import GpuBatch
     specs = [(32, "c0", 41), (64, "c0", 42), (16, "c0", 43)]
