@@ -100,7 +100,8 @@ typedef struct {
     double distortion;        /* max BIMOCQ distortion, grid units */
     int reinit;               /* maps re-initialised in the last step */
     int solver_iters;
-    double solver_rel_resid;  /* ||b - A x|| / ||b|| of the returned gamma */
+    double solver_rel_resid;  /* ||b - A x|| / ||b|| of the returned gamma (rows scaled by
+                                 the range guard of sb_download_system enter scaled) */
     int solver_converged;
     int broken_cells;         /* identity rows of the implicit system */
     long long steps;          /* steps taken by this handle */
@@ -182,6 +183,35 @@ int sb_download_field(sb_bubble* b, sb_field which, double* dst, size_t n);
 
 /* Element count of a field. */
 size_t sb_field_size(const sb_bubble* b, sb_field which);
+
+/* The implicit surfactant system of the most recent step, for inspection
+ * (the reference keeps its matrix inside AmgX: val/rhs of
+ * Bubble::concentrationLinearSystem, kernel/bubble.cu:1301-1473).  The
+ * library solves it for the increment dx = gamma_new - gamma_adv:
+ *   (A dx)_c = dmass_c dx_c + sum_n w_cn (dx_c - dx_n),  A dx = r0,
+ * whose dx is 0 in broken cells.  The reference's row c of an unbroken cell
+ * is then: diagonal sin(theta)/(dt gamma_adv) + sum over all four
+ * neighbours of w_cn, off-diagonal -w_cn; dmass_c holds the first term
+ * plus the weights towards broken neighbours, and the stored east/south
+ * weights are 0 across a broken cell.  A broken cell has dmass 1, no
+ * weights, r0 0 and gamma_adv gmax (the reference's identity row).  A cell
+ * left with almost no surfactant, whose term t = sin(theta) / (dt gamma_adv)
+ * exceeds 2^48, has its row and column scaled by s = 2^-k (2^45 < t s^2 <=
+ * 2^48; FP32 range guard, exact): its dmass, weights and r0 here are the
+ * scaled ones, its dx is not.  Each array has nTheta * nPhi elements,
+ * row-major. */
+typedef enum {
+    SB_SYS_ETA_ADV = 0,  /* advected thickness */
+    SB_SYS_GAMMA_ADV,    /* advected concentration (gmax in broken cells) */
+    SB_SYS_DMASS,        /* diagonal excess (sin(theta) / (dt gamma_adv) + broken couplings) */
+    SB_SYS_WEAST,        /* coupling weight to the east neighbour (0 if either is broken) */
+    SB_SYS_WSOUTH,       /* coupling weight to the south neighbour */
+    SB_SYS_R0,           /* r0 = b - A gamma_adv */
+    SB_SYS_RHS,          /* b */
+    SB_SYS_DX,           /* the solved increment, FP32-rounded */
+    SB_SYS_COUNT
+} sb_system_array;
+int sb_download_system(sb_bubble* b, sb_system_array which, double* dst, size_t n);
 
 /* Replaces Solver::stepForward(dt) (kernel/solver.cu:252-292) called
  * n_steps times with currentTimeGlobal = t_frame (s) and the dimensional

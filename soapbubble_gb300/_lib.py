@@ -20,6 +20,9 @@ FIELDS = ["eta", "gamma", "u_theta", "u_phi",
           "fwd_t", "fwd_p", "bwd_t", "bwd_p", "bwdprev_t", "bwdprev_p",
           "uair_init", "vair_init", "uair", "vair"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
+# sb_system_array: the implicit system of the most recent step
+SYSTEM = ["eta_adv", "gamma_adv", "dmass", "w_east", "w_south", "r0", "rhs", "dx"]
+SYSTEM_ID = {n: i for i, n in enumerate(SYSTEM)}
 
 
 class SbParams(C.Structure):
@@ -78,6 +81,7 @@ def lib() -> C.CDLL:
     L.sb_upload_field.argtypes = [H, C.c_int, dp, C.c_size_t]
     L.sb_download_field.argtypes = [H, C.c_int, dp, C.c_size_t]
     L.sb_field_size.argtypes = [H, C.c_int]
+    L.sb_download_system.argtypes = [H, C.c_int, dp, C.c_size_t]
     L.sb_field_size.restype = C.c_size_t
     L.sb_step.argtypes = [H, C.c_int, C.c_double, C.c_double]
     L.sb_step_timed.argtypes = [H, C.c_int, C.c_double, C.c_double, dp]
@@ -128,7 +132,7 @@ def lib() -> C.CDLL:
     L.sb_write_velocity_exr.argtypes = [H, C.c_char_p]
     L.sb_write_concentration_exr.argtypes = [H, C.c_char_p]
     for name in ("sb_create", "sb_destroy", "sb_upload_fields", "sb_upload_field",
-                 "sb_download_field", "sb_step", "sb_step_timed", "sb_autotune", "sb_upload_field_f32",
+                 "sb_download_field", "sb_download_system", "sb_step", "sb_step_timed", "sb_autotune", "sb_upload_field_f32",
                  "sb_download_field_f32", "sb_synchronize", "sb_reset_stats",
                  "sb_selftest_grid_barrier", "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr", "sb_run", "sb_batch_create",
                  "sb_batch_destroy", "sb_batch_step", "sb_batch_step_timed",
@@ -148,7 +152,7 @@ def check(code: int, what: str) -> None:
 
 # Every symbol include/soapbubble.h declares (checked by the CPU tests).
 EXPORTS = ["sb_default_params", "sb_create", "sb_destroy", "sb_upload_fields",
-           "sb_upload_field", "sb_download_field", "sb_field_size", "sb_step",
+           "sb_upload_field", "sb_download_field", "sb_field_size", "sb_download_system", "sb_step",
            "sb_step_timed", "sb_autotune", "sb_stage_count", "sb_stage_name", "sb_upload_field_f32",
            "sb_download_field_f32", "sb_synchronize", "sb_reset_stats", "sb_selftest_grid_barrier",
            "sb_get_stats", "sb_update_mass", "sb_write_thickness_exr",

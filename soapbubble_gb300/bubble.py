@@ -117,6 +117,14 @@ class GpuBubble:
         check(lib().sb_download_field(self.h, _lib.FIELD_ID[name], _dp(out), n), "sb_download_field")
         return out.reshape(self.shape(name))
 
+    def download_system(self, name: str) -> np.ndarray:
+        """One array of the last step's implicit system (sb_download_system):
+        eta_adv, gamma_adv, dmass, w_east, w_south, r0, rhs or dx."""
+        out = np.empty(self.nTheta * self.nPhi, dtype=np.float64)
+        check(lib().sb_download_system(self.h, _lib.SYSTEM_ID[name], _dp(out), out.size),
+              "sb_download_system")
+        return out.reshape(self.nTheta, self.nPhi)
+
     # -- stepping -----------------------------------------------------------
     def step(self, n: int = 1, t: float = 0.0, dt: Optional[float] = None) -> None:
         check(lib().sb_step(self.h, n, t, self.params.dt if dt is None else dt), "sb_step")

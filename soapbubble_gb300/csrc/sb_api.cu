@@ -801,6 +801,30 @@ int sb_download_field(sb_bubble* b, sb_field which, double* dst, size_t n) {
     return SB_OK;
 }
 
+int sb_download_system(sb_bubble* b, sb_system_array which, double* dst, size_t n) {
+    if (!b || !dst) return fail(SB_ERR_INVALID, "null argument");
+    if (n != (size_t)b->g.N) return fail(SB_ERR_INVALID, "element count mismatch");
+    const SbFields& f = b->f;
+    const float* d = nullptr;
+    switch (which) {
+        case SB_SYS_ETA_ADV: d = f.eta_adv; break;
+        case SB_SYS_GAMMA_ADV: d = f.gam_adv; break;
+        case SB_SYS_DMASS: d = f.dmass; break;
+        case SB_SYS_WEAST: d = f.cE; break;
+        case SB_SYS_WSOUTH: d = f.cS; break;
+        case SB_SYS_R0: d = f.r0; break;
+        case SB_SYS_RHS: d = f.rhs; break;
+        case SB_SYS_DX: d = f.dx; break;
+        default: return fail(SB_ERR_INVALID, "unknown system array");
+    }
+    SB_CHECK(cudaSetDevice(b->device));
+    std::vector<float> tmp(n);
+    SB_CHECK(cudaMemcpyAsync(tmp.data(), d, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+    SB_CHECK(cudaStreamSynchronize(b->stream));
+    for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i];
+    return SB_OK;
+}
+
 int sb_exr_load_resized(const char* path, const char* channel, int width, int height,
                         double* out) {
     if (!path || !channel || !out || width <= 0 || height <= 0)

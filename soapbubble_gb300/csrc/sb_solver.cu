@@ -50,6 +50,7 @@
 
 #include "sb_ff.cuh"
 #include "sb_internal.h"
+#include "sb_scale.cuh"
 #include "sb_sync.cuh"
 
 namespace sb {
@@ -545,9 +546,21 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
                                          const SolverConfig& cfg, float (&rv)[PER], ff& bb) {
     const int nP = g.nP, nT = g.nT, row = i * nP;
     const bool warm = cfg.warm && f.stats->dx_valid != 0 && f.stats->solver_converged != 0;
-    auto prev = [&](int c) {
-        const float v = f.dx[c];
-        return isfinite(v) ? v : 0.0f;
+    // The previous increment, bounded by |x0| <= min(gamma_adv, gmax - gamma_adv):
+    // 0 in a broken cell (gamma_adv = gmax, its row is dx = 0), and where
+    // advection brought a tiny concentration into the cell, its diagonal
+    // sin(theta) / (dt gamma_adv) times x0 stays below sin(theta) / dt
+    // (unbounded, 6e24 x 1e2 made a residual whose square overflows FP32).
+    // The bound depends on the cell alone, so every row that reads x0 of a
+    // neighbour sees the same value.
+    // The iterate of a scaled cell (sb_scale.cuh) is dx / s.
+    const float gmax = f.self->ph.gmax, invDt = f.step->invDt;
+    auto prev = [&](int c, int ic) {
+        const float v = f.dx[c], ga = f.gam_adv[c];
+        const float lim = fminf(ga, gmax - ga);
+        const float x0 = isfinite(v) ? fminf(fmaxf(v, -lim), lim) : 0.0f;
+        const int k = diag_scale_k(ga, g.sin_c[ic], invDt);
+        return k ? x0 * pow2_pos(k) : x0;
     };
     ff h[2] = {ff_zero(), ff_zero()};
 #pragma unroll
@@ -559,11 +572,11 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
             float r = f.r0[c];
             const float rhs = f.rhs[c];
             if (warm) {
-                const float x0 = prev(c);
+                const float x0 = prev(c, i);
                 const int e = row + ((j + 1) & g.maskP), w = row + ((j - 1) & g.maskP);
-                float ax = f.dmass[c] * x0 + f.cE[c] * (x0 - prev(e)) + f.cE[w] * (x0 - prev(w));
-                if (i < nT - 1) ax += f.cS[c] * (x0 - prev(c + nP));
-                if (i > 0) ax += f.cS[c - nP] * (x0 - prev(c - nP));
+                float ax = f.dmass[c] * x0 + f.cE[c] * (x0 - prev(e, i)) + f.cE[w] * (x0 - prev(w, i));
+                if (i < nT - 1) ax += f.cS[c] * (x0 - prev(c + nP, i + 1));
+                if (i > 0) ax += f.cS[c - nP] * (x0 - prev(c - nP, i - 1));
                 r -= ax;
                 if (MIXED) f.xff[c] = make_float2(x0, 0.0f);
                 else if (x0 != f.dx[c]) f.dx[c] = x0;  // only where it was not finite
@@ -725,14 +738,25 @@ __device__ __forceinline__ void row_load_r(const SbGrid& g, const SbFields& f, i
 template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_final(const SbGrid& g, const SbFields& f, int i) {
     const int nP = g.nP, row = i * nP;
+    const float invDt = f.step->invDt;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int j = col_of<TB>(k);
         if (j < nP) {
             const int c = row + j;
-            const float dx = MIXED ? ff_to_f(ld_ff(f.xff, c)) : f.dx[c];
+            float dx = MIXED ? ff_to_f(ld_ff(f.xff, c)) : f.dx[c];
+            const float ga = f.gam_adv[c];
+            const int ks = diag_scale_k(ga, g.sin_c[i], invDt);
+            if (ks) {  // a scaled cell's iterate is dx / s (sb_scale.cuh)
+                const float sc = pow2_neg(ks);
+                dx *= sc;
+                if (MIXED) {
+                    const float2 v = f.xff[c];
+                    f.xff[c] = make_float2(v.x * sc, v.y * sc);
+                }
+            }
             f.dx[c] = dx;
-            f.x[c] = f.gam_adv[c] + dx;
+            f.x[c] = ga + dx;
             if (!MIXED) f.xff[c] = make_float2(dx, 0.0f);
         }
     }

@@ -22,6 +22,7 @@
 
 #include "sb_device.cuh"
 #include "sb_internal.h"
+#include "sb_scale.cuh"
 #include "sb_sync.cuh"
 
 namespace sb {
@@ -338,7 +339,9 @@ __device__ __noinline__ float viscous_fu(const SbGrid& g, const SbPhys& ph, cons
 // maximum or no film) keeps gamma = gmax: its row is dx = 0 and the weight
 // of its couplings moves into the neighbours' dmass, which keeps A
 // symmetric positive definite with the same solution as the reference's
-// identity row.
+// identity row.  A cell with almost no surfactant (t = sin(theta) / (dt
+// gamma) > 2^48) enters with its row and column scaled by a power of two
+// (sb_scale.cuh).
 template <bool VISC>
 __device__ __forceinline__ void assemble_cell(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                           int idx) {
@@ -434,27 +437,50 @@ __device__ __forceinline__ void assemble_cell(const SbGrid& g, const SbPhys& ph,
     const bool bE = is_broken(gEr, etaE, gmax), bW = is_broken(gWr, etaW, gmax);
     const float gE = bE ? gmax : gEr, gW = bW ? gmax : gWr;
     bool bN = false, bS = false;
-    float gN = gamma, gS = gamma;
+    float gN = gamma, gS = gamma, gNr = gamma, gSr = gamma;
     if (i != 0) {
-        const float gr = f.gam_adv[idx - nP];
-        bN = is_broken(gr, etaN, gmax);
-        gN = bN ? gmax : gr;
+        gNr = f.gam_adv[idx - nP];
+        bN = is_broken(gNr, etaN, gmax);
+        gN = bN ? gmax : gNr;
     }
     if (i != nT - 1) {
-        const float gr = f.gam_adv[idx + nP];
-        bS = is_broken(gr, etaS, gmax);
-        gS = bS ? gmax : gr;
+        gSr = f.gam_adv[idx + nP];
+        bS = is_broken(gSr, etaS, gmax);
+        gS = bS ? gmax : gSr;
     }
     const float lap = wE * (gamma - gE) + wW * (gamma - gW) + wN * (gamma - gN) + wS * (gamma - gS);
-    float dmass = sinT * invDt / gamma;
-    if (bE) dmass += wE;
-    if (bW) dmass += wW;
-    if (bN) dmass += wN;
-    if (bS) dmass += wS;
+    float cE = bE ? 0.0f : wE, cS = bS ? 0.0f : wS;
+    float r0 = -sinThetaDiv - lap;
+    // rows and columns of cells with t > 2^48 are scaled by s = 2^-k
+    // (sb_scale.cuh): this cell's row, and its couplings to such neighbours
+    const int kc = diag_scale_k(gamma, sinT, invDt);
+    const int kE = bE ? 0 : diag_scale_k(gEr, sinT, invDt);
+    const int kW = bW ? 0 : diag_scale_k(gWr, sinT, invDt);
+    const int kN = (i == 0 || bN) ? 0 : diag_scale_k(gNr, g.sin_c[i - 1], invDt);
+    const int kS = (i == nT - 1 || bS) ? 0 : diag_scale_k(gSr, g.sin_c[i + 1], invDt);
+    float dmass = scaled_diag_term(gamma, sinT, invDt, kc);
+    if (!(kc | kE | kW | kN | kS)) {
+        if (bE) dmass += wE;
+        if (bW) dmass += wW;
+        if (bN) dmass += wN;
+        if (bS) dmass += wS;
+    } else {
+        // s_c A_cc s_c in excess form: t s_c^2 + s_c^2 (weights to broken
+        // neighbours) + sum over the other couplings of w s_c (s_c - s_n)
+        const float sc = pow2_neg(kc), sc2 = sc * sc;
+        const float sE = pow2_neg(kE), sW = pow2_neg(kW), sN = pow2_neg(kN), sS = pow2_neg(kS);
+        dmass += bE ? wE * sc2 : wE * sc * (sc - sE);
+        dmass += bW ? wW * sc2 : wW * sc * (sc - sW);
+        dmass += bN ? wN * sc2 : wN * sc * (sc - sN);
+        dmass += bS ? wS * sc2 : wS * sc * (sc - sS);
+        cE *= sc * sE;
+        cS *= sc * sS;
+        r0 *= sc;
+    }
     f.dmass[idx] = dmass;
-    f.cE[idx] = bE ? 0.0f : wE;
-    f.cS[idx] = bS ? 0.0f : wS;
-    f.r0[idx] = -sinThetaDiv - lap;
+    f.cE[idx] = cE;
+    f.cS[idx] = cS;
+    f.r0[idx] = r0;
     f.rhs[idx] = sinT * invDt - sinThetaDiv;
 }
 
