@@ -477,8 +477,10 @@ def run_ours(args):
             "solver_iters_mean": mean_iters, "solver_rel_resid_last": st.solver_rel_resid,
             "solver_nonconverged": int(st.solver_nonconverged),
             "solver_rel_resid_max": float(st.solver_rel_resid_max),
-            "window": f"steps {k0}..{k0 + args.steps - 1} of the 1000-step run (the film is "
-                      "still whole; c1_whole_run covers the rupture)",
+            "window": f"steps {k0}..{k0 + args.steps - 1} of the 1000-step run " + (
+                "(the film is still whole; c1_whole_run covers the rupture)"
+                if k0 + args.steps <= 330 else
+                "(the film opens near step 330: the window includes the ruptured phase)"),
             "c1_whole_run": whole,
             "c1_solver_modes": modes,
             "solver_alg_bytes_per_cell": alg["k_solve"],

@@ -752,7 +752,9 @@ __device__ __forceinline__ int nb_index(const SbGrid& g, int i, int j) {
 
 // correctCentered2: subtract the error pulled back through the backward map,
 // clamp to the 3x3 range of the uncorrected field, keep non-negative.  The
-// result goes to the *_adv buffers and is committed in the next phase.
+// result goes to the per-step increment buffers (read by k_accum, free from
+// here on; the *_adv buffers keep the step's implicit system) and is
+// committed in the next phase.
 template <class T>
 __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbPhys& ph, const SbFields& f, int cur,
                                                int idx) {
@@ -779,14 +781,14 @@ __device__ __forceinline__ void reinit_correct(const SbGrid& g, const SbPhys& ph
         }
     th = (th < emin) ? emin : (emax < th) ? emax : th;
     gm = (gm < gmin) ? gmin : (gmx < gm) ? gmx : gm;
-    f.eta_adv[idx] = fmaxf(0.0f, th);
-    f.gam_adv[idx] = fmaxf(0.0f, gm);
+    f.d_eta[idx] = fmaxf(0.0f, th);
+    f.d_gam[idx] = fmaxf(0.0f, gm);
 }
 
 // Commit the correction, rotate the BIMOCQ buffers and reset the maps.
 template <class T>
 __device__ __forceinline__ void reinit_commit(const SbPhys& ph, const SbFields& f, int cur, int idx) {
-    const float e = f.eta_adv[idx], gm = f.gam_adv[idx];
+    const float e = f.d_eta[idx], gm = f.d_gam[idx];
     st_s<T>(f.eta, idx, e, ph.base_eta);
     st_s<T>(f.gam, idx, gm, ph.base_gam);
     cp_s<T>(f.eta_initL, f.eta_init, idx);

@@ -22,7 +22,7 @@ import _parity as P
 pytestmark = pytest.mark.gpu
 
 
-def _pair(oracle, recipe, nT, dt, pre, t, seed, gamma_patch=None):
+def _pair(oracle, recipe, nT, dt, pre, t, seed, gamma_patch=None, force_reinit=0):
     from soapbubble_gb300 import synth
     from soapbubble_gb300.bubble import GpuBubble, make_params
     f = synth.make_fields(recipe, nT, seed)
@@ -33,7 +33,8 @@ def _pair(oracle, recipe, nT, dt, pre, t, seed, gamma_patch=None):
         ob.step()
     if gamma_patch is not None:
         gamma_patch(ob)
-    gb = GpuBubble(make_params(nT, dt, solver_tol=1e-10, solver_max_iter=4000))
+    gb = GpuBubble(make_params(nT, dt, solver_tol=1e-10, solver_max_iter=4000,
+                               force_reinit=force_reinit))
     P.sync_state(gb, ob)
     return gb, ob
 
@@ -91,14 +92,19 @@ def _check_system(S, val, rhs, gamma_adv, eta_adv):
     assert np.max(np.abs(S["r0"][u] - r0_ref[u])) <= 1e-5 * bmax
 
 
-@pytest.mark.parametrize("case", [("c0", 64, 0.005, 4, 1.0, 11), ("c1", 128, 0.002, 6, 0.02, 12)],
-                         ids=lambda c: f"{c[0]}-{c[1]}")
+@pytest.mark.parametrize("case", [("c0", 64, 0.005, 4, 1.0, 11, 0), ("c1", 128, 0.002, 6, 0.02, 12, 0),
+                                  ("c0", 64, 0.005, 2, 0.5, 13, 2)],
+                         ids=lambda c: f"{c[0]}-{c[1]}" + ("-reinit" if c[6] == 2 else ""))
 def test_assembled_system_is_the_references_matrix(oracle, gpulib, case):
-    recipe, nT, dt, pre, t, seed = case
-    gb, ob = _pair(oracle, recipe, nT, dt, pre, t, seed)
+    """The system stays readable after the step, a step that re-initialises
+    the maps included (force_reinit 2: every step)."""
+    recipe, nT, dt, pre, t, seed, force = case
+    gb, ob = _pair(oracle, recipe, nT, dt, pre, t, seed, force_reinit=force)
     try:
         val, rhs, gamma_adv, eta_adv = _oracle_system(ob)
         gb.step(1, t, dt)
+        if force == 2:
+            assert gb.stats().reinit == 1
         S = _gpu_system(gb)
         _check_system(S, val, rhs, gamma_adv, eta_adv)
         # the solved increment is the step's change of gamma where nothing clamps
