@@ -107,10 +107,12 @@ def test_assembled_system_is_the_references_matrix(oracle, gpulib, case):
             assert gb.stats().reinit == 1
         S = _gpu_system(gb)
         _check_system(S, val, rhs, gamma_adv, eta_adv)
-        # the solved increment is the step's change of gamma where nothing clamps
-        g_new = gb.download("gamma")
-        inner = (S["dmass"] != 1.0) & (g_new > 0) & (g_new < ob.p.gammaMax - 1e-6)
-        assert np.max(np.abs(S["gamma_adv"] + S["dx"] - g_new)[inner]) <= 1e-6 * np.max(g_new)
+        # the solved increment is the step's change of gamma where nothing
+        # clamps (a re-initialisation corrects gamma after the solve)
+        if not gb.stats().reinit:
+            g_new = gb.download("gamma")
+            inner = (S["dmass"] != 1.0) & (g_new > 0) & (g_new < ob.p.gammaMax - 1e-6)
+            assert np.max(np.abs(S["gamma_adv"] + S["dx"] - g_new)[inner]) <= 1e-6 * np.max(g_new)
     finally:
         gb.close()
 
