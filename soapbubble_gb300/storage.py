@@ -21,7 +21,7 @@ from . import cudart, synth
 from .bubble import GpuBubble, bytes_required, make_params, stage_names
 
 # Algorithmic bytes per cell and launch (every array once; FP32 = 4 B, map
-# entry = 8 B, a stored field 4 or 2 B).  s = bytes of a stored element.
+# entry = 16 B, a stored field 4 or 2 B).  s = bytes of a stored element.
 def alg_bytes(s: int) -> dict:
     return {
         "k_advect_maps": 100 + s,     # gamma sampled in the stored type; maps 16 B
