@@ -387,7 +387,9 @@ typedef struct sb_batch sb_batch;
 
 /* Builds the batch's tables (per-member descriptors, cell tiles of 64, 128
  * and 256 cells, solve-block ranges).  Synchronises the members' streams.
- * A bubble listed twice is rejected (SB_ERR_INVALID). */
+ * A bubble listed twice is rejected (SB_ERR_INVALID), and so is a batch
+ * over its limits: at most 1024 members, and the sum over members of
+ * nTheta (2 nTheta + 256) below 2^32 (the solver's 32-bit row tables). */
 int sb_batch_create(sb_bubble* const* members, int n, sb_batch** out);
 int sb_batch_destroy(sb_batch* batch);
 

@@ -224,6 +224,16 @@ class GpuBubble:
         return lib().sb_stream(self.h)
 
 
+# The limits sb_batch_create enforces: at most 1024 members, and the sum
+# over members of nTheta (2 nTheta + 256) below 2^32.
+BATCH_MAX_MEMBERS = 1024
+BATCH_MAX_WEIGHT = 1 << 32
+
+
+def batch_weight(nTheta: int) -> int:
+    return nTheta * (2 * nTheta + 256)
+
+
 class GpuBatch:
     """An ensemble of GpuBubbles stepped together (sb_batch_*): one kernel
     launch per stage for all members, one CUDA graph per step.  The members

@@ -391,15 +391,18 @@ __device__ __forceinline__ void velocity_at(const SbGrid& g, const float* __rest
 
 // Local basis at the point P (unnormalised), as the reference derives it from
 // (acos(Pz), atan2(Py, Px)) (kernel/bubble.cu:462-471).
+// Reciprocal square roots in place of square roots and quotients (within
+// 2 ulp: the basis weights velocity samples).
 __device__ __forceinline__ void basis_at(f3 P, f3& eth, f3& eph) {
-    const float rho = sqrtf(P.x * P.x + P.y * P.y);
-    const float r = sqrtf(rho * rho + P.z * P.z);
-    float cph = 1.0f, sph = 0.0f;
-    if (rho > 0.0f) {
-        cph = P.x / rho;
-        sph = P.y / rho;
+    const float rho2 = P.x * P.x + P.y * P.y;
+    const float ir = rsqrtf(rho2 + P.z * P.z);
+    float cph = 1.0f, sph = 0.0f, irho = 0.0f;
+    if (rho2 > 0.0f) {
+        irho = rsqrtf(rho2);
+        cph = P.x * irho;
+        sph = P.y * irho;
     }
-    const float ct = P.z / r, st = rho / r;
+    const float ct = P.z * ir, st = rho2 * irho * ir;
     eth = {ct * cph, ct * sph, -st};
     eph = {-sph, cph, 0.0f};
 }
@@ -433,9 +436,11 @@ __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restri
     const f3 eth = {F.c0, 0.0f, -F.s0};
     const f3 eph = {0.0f, 1.0f, 0.0f};
     f3 u = gt * eth + gp * eph;
-    float un = len3(u);
-    if (!(un > 0.0f)) { T.fail = un; return T; }
-    f3 u_ = (1.0f / un) * u;
+    float un2 = dot3(u, u);
+    if (!(un2 > 0.0f)) { T.fail = sqrtf(un2); return T; }
+    float iun = rsqrtf(un2);
+    float un = un2 * iun;
+    f3 u_ = iun * u;
     f3 v_ = cross3(w, u_);
     float dS, sd, sh, ch, cdm1;
     if (rk2) {
@@ -457,9 +462,11 @@ __device__ __forceinline__ Trace trace_gc(const SbGrid& g, const float* __restri
         const float mgt = dot3(mu, vCircleMid);
         const float mgp = dot3(mu, uCircleMid);
         u = mgp * u_ + mgt * v_;
-        un = len3(u);
-        if (!(un > 0.0f)) { T.fail = un; return T; }
-        u_ = (1.0f / un) * u;
+        un2 = dot3(u, u);
+        if (!(un2 > 0.0f)) { T.fail = sqrtf(un2); return T; }
+        iun = rsqrtf(un2);
+        un = un2 * iun;
+        u_ = iun * u;
         v_ = cross3(w, u_);
     }
     dS = -un * dt;

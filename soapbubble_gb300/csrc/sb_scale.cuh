@@ -5,7 +5,7 @@
 // grows without bound as advection empties the cell of surfactant (1e-37
 // leaves t near the FP32 maximum, a subnormal gamma puts it past it), and the
 // preconditioner's factors take quotients by it and products of two of them.
-// For t > 2^48 the cell's unknown becomes y = dx / s with s = 2^-k,
+// For t > 2^48 (tested as gamma < A 2^-48) the cell's unknown becomes y = dx / s with s = 2^-k,
 // 2^45 < t s^2 <= 2^48, and its row and column of the matrix are multiplied
 // by s: a symmetric scaling by powers of two, which FP32 applies exactly, so
 // the solution is the unscaled system's.  t itself is never formed: k comes
@@ -34,7 +34,7 @@ __device__ __forceinline__ int ilog2_pos(float x) {
 __device__ __forceinline__ int diag_scale_k(float gamma, float sinT, float invDt) {
     const float A = sinT * invDt;
     if (gamma == 0.0f) return kScaleZero;
-    if (!(A / gamma > 0x1p48f)) return 0;  // also NaN
+    if (!(gamma < A * 0x1p-48f)) return 0;  // t <= 2^48 (A 2^-48 is exact); also NaN
     const int e = ilog2_pos(A) - ilog2_pos(gamma);  // log2 t in (e - 1, e + 1), e >= 48
     return min(max((e - (kScaleLog2 - 2)) / 2, 1), 63);  // ceil((e - 47) / 2)
 }

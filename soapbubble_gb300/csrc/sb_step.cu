@@ -405,31 +405,31 @@ __device__ __forceinline__ void assemble_cell(const SbGrid& g, const SbPhys& ph,
     const float etaLeft = (etaW + eta) * 0.5f;
     const float etaRight = (etaE + eta) * 0.5f;
     const float etaDown = (etaS + eta) * 0.5f;
-    const float wN = (i == 0) ? 0.0f : s2 * sinN * MDt / (etaUp + CrDt);
-    const float wW = s2 * cscT * MDt / (etaLeft + CrDt);
-    const float wE = s2 * cscT * MDt / (etaRight + CrDt);
-    const float wS = (i == nT - 1) ? 0.0f : s2 * sinS * MDt / (etaDown + CrDt);
+    // Every face term of the reference's row divides by eta_face + Cr dt
+    // (written there as eta/(eta + Cr dt), 1/(eta/(Cr dt) + 1) and
+    // eta/(eta/dt + Cr)): one reciprocal per face serves all of them.
+    const float rN = 1.0f / (etaUp + CrDt), rW = 1.0f / (etaLeft + CrDt);
+    const float rE = 1.0f / (etaRight + CrDt), rS = 1.0f / (etaDown + CrDt);
+    const float wN = (i == 0) ? 0.0f : s2 * sinN * MDt * rN;
+    const float wW = s2 * cscT * MDt * rW;
+    const float wE = s2 * cscT * MDt * rE;
+    const float wS = (i == nT - 1) ? 0.0f : s2 * sinS * MDt * rS;
 
-    float sinThetaDiv = g.invh * (uE * etaRight / (etaRight + CrDt) - uW * etaLeft / (etaLeft + CrDt) +
-                                  (vS * sinS * etaDown / (etaDown + CrDt) -
-                                   vN * sinN * etaUp / (etaUp + CrDt)));
-    sinThetaDiv += g.invh * (uAirE / (etaRight / Cr * invDt + 1.0f) -
-                             uAirW / (etaLeft / Cr * invDt + 1.0f) +
-                             vAirS * sinS / (etaDown / Cr * invDt + 1.0f) -
-                             vAirN * sinN / (etaUp / Cr * invDt + 1.0f));
+    float sinThetaDiv = g.invh * (uE * etaRight * rE - uW * etaLeft * rW +
+                                  (vS * sinS * etaDown * rS - vN * sinN * etaUp * rN));
+    sinThetaDiv += g.invh * CrDt *
+                   (uAirE * rE - uAirW * rW + vAirS * sinS * rS - vAirN * sinN * rN);
     if (VISC) {
         // bubble.cu:1460-1466: the viscous forces, gravity inside fv
         const float fuW = viscous_fu(g, ph, f, i, j), fuE = viscous_fu(g, ph, f, i, jE);
         const float fvN = i != 0 ? viscous_fv(g, ph, f, i - 1, j) : 0.0f;
         const float fvS = i != nT - 1 ? viscous_fv(g, ph, f, i, j) : 0.0f;
-        sinThetaDiv += g.invh * (sinS * fvS * etaDown / (invDt * etaDown + Cr) -
-                                 sinN * fvN * etaUp / (invDt * etaUp + Cr) +
-                                 fuE * etaRight / (invDt * etaRight + Cr) -
-                                 fuW * etaLeft / (invDt * etaLeft + Cr));
+        sinThetaDiv += g.invh * dt *
+                       (sinS * fvS * etaDown * rS - sinN * fvN * etaUp * rN +
+                        fuE * etaRight * rE - fuW * etaLeft * rW);
     } else {
-        sinThetaDiv += ph.gs * g.invh *
-                       (sinS * sinS * etaDown / (invDt * etaDown + Cr) -
-                        sinN * sinN * etaUp / (invDt * etaUp + Cr));
+        sinThetaDiv += ph.gs * g.invh * dt *
+                       (sinS * sinS * etaDown * rS - sinN * sinN * etaUp * rN);
     }
 
     // neighbour gamma (a broken neighbour holds gmax) and broken flags
@@ -546,53 +546,51 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
     // launches its u_phi update with the u_theta layout (nTheta - 1 rows,
     // kernel/bubble.cu:2463-2474), so u_phi's last theta row keeps its value
     // from before the step: the state buffer is left as it is.
+    // The reference's update u = (u dt^-1 + f1 + f2 (+ f3)) / (dt^-1 + Cr / eta_f)
+    // with f1 = -M grad(gamma) / eta_f, f2 = Cr uair / eta_f is evaluated
+    // multiplied through by the face thickness eta_f = (eta_a + eta_b) / 2:
+    // one quotient per face.  A face without film (eta_f = 0, the
+    // reference's 1/eta_f infinite) gets a NaN velocity as there.
     if (!VISC || i < g.nT - 1) {
         const int w = i * nP + ((j - 1) & g.maskP);
-        const float etaW = f.eta_adv[w];
-        const float invEta = 2.0f / (etaW + e);
+        const float ef = 0.5f * (f.eta_adv[w] + e);
         const float u1 = f.uph_adv[idx];
-        if (isinf(invEta)) {
+        if (ef == 0.0f) {
             f.uph[idx] = __int_as_float(0x7fffffff);
         } else {
             const float cscT = 1.0f / g.sin_c[i];
             const float pGpx = g.invh * gnew_diff(f, idx, w, gmax) * cscT;
-            const float f1 = -M * invEta * pGpx;
             if (VISC) {
                 // applyforcevelphiKernel_viscous (bubble.cu:1987-2038): the
                 // mirrored wind mix and fu
                 const float uAir = 0.5f * (f.uair[idx] * f.step->mixA +
                                            f.uair[i * nP + (nP - j)] * f.step->mixB);
-                const float f6 = Cr * invEta * uAir;
-                f.uph[idx] = (u1 * invDt + f1 + f6 + viscous_fu(g, ph, f, i, j)) /
-                             (invDt + Cr * invEta);
+                f.uph[idx] = ((u1 * invDt + viscous_fu(g, ph, f, i, j)) * ef - M * pGpx + Cr * uAir) /
+                             (invDt * ef + Cr);
             } else {
-                const float f2 = Cr * invEta * f.uair[idx];
-                f.uph[idx] = (u1 * invDt + f1 + f2) / (invDt + Cr * invEta);
+                f.uph[idx] = (u1 * invDt * ef - M * pGpx + Cr * f.uair[idx]) / (invDt * ef + Cr);
             }
         }
     }
     // u_theta face between (i, j) and (i+1, j)
     if (i < g.nT - 1) {
         const int s = idx + nP;
-        const float etaS = f.eta_adv[s];
-        const float invEta = 2.0f / (e + etaS);
+        const float ef = 0.5f * (e + f.eta_adv[s]);
         const float v1 = f.uth_adv[idx];
-        if (isinf(invEta)) {
+        if (ef == 0.0f) {
             f.uth[idx] = __int_as_float(0x7fffffff);
         } else {
             const float pGpy = g.invh * gnew_diff(f, s, idx, gmax);
-            const float f1 = -M * invEta * pGpy;
             if (VISC) {
                 // applyforcevelthetaKernel_viscous (bubble.cu:1940-1983)
                 const float vAir = 0.5f * (f.vair[idx] * f.step->mixA -
                                            f.vair[i * nP + (nP - j)] * f.step->mixB);
-                const float f6 = Cr * invEta * vAir;
-                f.uth[idx] = (v1 * invDt + f1 + f6 + viscous_fv(g, ph, f, i, j)) /
-                             (invDt + Cr * invEta);
+                f.uth[idx] = ((v1 * invDt + viscous_fv(g, ph, f, i, j)) * ef - M * pGpy + Cr * vAir) /
+                             (invDt * ef + Cr);
             } else {
-                const float f2 = Cr * invEta * f.vair[idx];
                 const float f3v = ph.gs * g.sin_e[i + 1];
-                f.uth[idx] = (v1 * invDt + f1 + f2 + f3v) / (invDt + Cr * invEta);
+                f.uth[idx] = ((v1 * invDt + f3v) * ef - M * pGpy + Cr * f.vair[idx]) /
+                             (invDt * ef + Cr);
             }
         }
     }

@@ -34,7 +34,8 @@ from typing import Dict, List, Optional
 import numpy as np
 
 from . import synth
-from .bubble import GpuBatch, GpuBubble, bytes_required, make_params
+from .bubble import (BATCH_MAX_MEMBERS, BATCH_MAX_WEIGHT, GpuBatch, GpuBubble, batch_weight,
+                     bytes_required, make_params)
 
 STEPS_PER_FRAME = 10
 DT = synth.ENSEMBLE["dt"]
@@ -146,6 +147,7 @@ class Server:
         self.max_resident = 0
         self.max_members = 0
         self.rebuilds = 0
+        self.limit_waits = 0  # admissions deferred by the batch limits
 
     def run(self, requests: List[Request], payloads, clock_start: Optional[float] = None):
         """Serve `requests` (sorted by arrival).  `payloads` maps a request
@@ -177,6 +179,11 @@ class Server:
                 req = waiting[0]
                 need = bytes_required(params_of(req, device=self.device))
                 if self.resident_bytes + need > self.budget and (in_use or ready):
+                    break
+                # the batch's own limits (members, row tables): the request
+                # waits until finished members have left the set
+                if not fits_batch([a.req.nTheta for a in active + ready], req.nTheta):
+                    self.limit_waits += 1
                     break
                 waiting.pop(0)
                 f = payloads[req.rid]
@@ -268,6 +275,15 @@ class Server:
         return [results[r.rid] for r in requests]
 
 
+def fits_batch(member_nthetas: List[int], nTheta: int) -> bool:
+    """Whether one more bubble of nTheta rows keeps a set of bubbles with
+    member_nthetas within sb_batch_create's limits."""
+    if len(member_nthetas) + 1 > BATCH_MAX_MEMBERS:
+        return False
+    w = sum(batch_weight(n) for n in member_nthetas) + batch_weight(nTheta)
+    return w < BATCH_MAX_WEIGHT
+
+
 def prepare_payloads(requests: List[Request], threads: int = 0) -> Dict[int, object]:
     """Every request's payload (its initial fields), computed by a thread
     pool before the stream starts: a request arrives with its payload, so
@@ -307,6 +323,7 @@ def summarise(requests, results, server: Server, model=None) -> dict:
         "latency_p99_s": float(np.percentile(lat, 99)),
         "latency_mean_s": float(lat.mean()),
         "max_resident_members": server.max_members,
+        "admissions_deferred_by_batch_limits": server.limit_waits,
         "max_resident_gb": server.max_resident / 1e9,
         "budget_gb": server.budget / 1e9,
         "set_rebuilds": server.rebuilds,
