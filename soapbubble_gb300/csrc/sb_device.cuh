@@ -79,6 +79,22 @@ __device__ __forceinline__ float blerp(float from, float to, float a) {
     return (1.0f - a) * from + a * to;
 }
 
+// The same lerp without the NaN tests.  A bilinear sample is formed with it
+// first: a result that is not NaN means no sample was NaN, and then every
+// lerp took blerp's last line, so the result is bit for bit blerp's; a NaN
+// result is formed again with blerp (the reference's NaN skipping).
+__device__ __forceinline__ float lerp_raw(float from, float to, float a) {
+    return (1.0f - a) * from + a * to;
+}
+
+// Bilinear sample from four values (lerp_raw first, blerp for a NaN).
+__device__ __forceinline__ float bilerp(float f00, float f01, float f10, float f11, float a,
+                                        float b) {
+    const float r = lerp_raw(lerp_raw(f00, f01, b), lerp_raw(f10, f11, b), a);
+    if (!isnan(r)) return r;
+    return blerp(blerp(f00, f01, b), blerp(f10, f11, b), a);
+}
+
 // Grid position of the point C + d.  Points past a pole come back with the
 // base column shifted by nTheta (azimuth + pi) so the float offset stays small.
 __device__ SB_CONV_INLINE Pos pos_from_disp(Frame F, f3 d, float invh, int nT) {
@@ -281,13 +297,24 @@ __device__ __forceinline__ float sample_centred(const SbGrid& g, const float* __
                                                 Pos q, float colOff) {
     const CStencil s = centred_stencil(g, q, colOff);
     const int nP = g.nP;
-    float l = blerp(f[s.r0 * nP + s.c00], f[s.r0 * nP + s.c01], s.b);
-    float u = blerp(f[s.r1 * nP + s.c10], f[s.r1 * nP + s.c11], s.b);
+    const float f00 = f[s.r0 * nP + s.c00], f01 = f[s.r0 * nP + s.c01];
+    const float f10 = f[s.r1 * nP + s.c10], f11 = f[s.r1 * nP + s.c11];
+    float l = lerp_raw(f00, f01, s.b);
+    float u = lerp_raw(f10, f11, s.b);
     if (VEC) {
         if (s.v0) l = -l;
         if (s.v1) u = -u;
     }
-    float r = blerp(l, u, s.a);
+    float r = lerp_raw(l, u, s.a);
+    if (isnan(r)) {  // a NaN sample: the reference's NaN-skipping lerps
+        l = blerp(f00, f01, s.b);
+        u = blerp(f10, f11, s.b);
+        if (VEC) {
+            if (s.v0) l = -l;
+            if (s.v1) u = -u;
+        }
+        r = blerp(l, u, s.a);
+    }
     if (VEC && s.flipped) r = -r;
     return r;
 }
@@ -333,9 +360,8 @@ __device__ __forceinline__ float sample_utheta(const SbGrid& g, const float* __r
         const float u = -blerp(f[row + ((j0 + nT) & g.maskP)], f[row + ((j1 + nT) & g.maskP)], b);
         r = blerp(l, u, 0.5f * s);
     } else {
-        const float l = blerp(f[lo * nP + j0], f[lo * nP + j1], b);
-        const float u = blerp(f[(lo + 1) * nP + j0], f[(lo + 1) * nP + j1], b);
-        r = blerp(l, u, a);
+        r = bilerp(f[lo * nP + j0], f[lo * nP + j1], f[(lo + 1) * nP + j0], f[(lo + 1) * nP + j1],
+                   a, b);
     }
     return flipped ? -r : r;
 }
@@ -537,15 +563,12 @@ __device__ __forceinline__ void cp_s(SbScalar* dst, const SbScalar* src, int i) 
 
 template <class T>
 __device__ __forceinline__ float gather_s(const SbScalar* f, const SStencil& s, float base) {
-    const float l = blerp(ld_s<T>(f, s.i00, base), ld_s<T>(f, s.i01, base), s.b);
-    const float u = blerp(ld_s<T>(f, s.i10, base), ld_s<T>(f, s.i11, base), s.b);
-    return blerp(l, u, s.a);
+    return bilerp(ld_s<T>(f, s.i00, base), ld_s<T>(f, s.i01, base), ld_s<T>(f, s.i10, base),
+                  ld_s<T>(f, s.i11, base), s.a, s.b);
 }
 
 __device__ __forceinline__ float gather(const float* __restrict__ f, const SStencil& s) {
-    const float l = blerp(f[s.i00], f[s.i01], s.b);
-    const float u = blerp(f[s.i10], f[s.i11], s.b);
-    return blerp(l, u, s.a);
+    return bilerp(f[s.i00], f[s.i01], f[s.i10], f[s.i11], s.a, s.b);
 }
 
 // Map lookups at the five MULTISAMPLE points of a cell, c + (-1/4, -1/4),
