@@ -618,9 +618,12 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
     float th = 0.0f, gm = 0.0f;
     f3 ds[5];
     sample_map_multi5(g, fwd, F, ds);
+    CStencil c4;  // stencil of sample 4, the cell's own forward-map point
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-        const SStencil s = scalar_stencil(g, pos_from_disp_fast(F, ds[k], g.invh, g.nT));
+        const CStencil c = centred_stencil(g, pos_from_disp_fast(F, ds[k], g.invh, g.nT), 0.0f);
+        if (k == 4) c4 = c;
+        const SStencil s = sstencil_of(g, c);
         ed += kW5[k] * gather(f.d_eta, s);
         gd += kW5[k] * gather(f.d_gam, s);
         th += kW5[k] * gather_s<T>(f.eta, s, ph.base_eta);
@@ -630,11 +633,10 @@ __device__ __forceinline__ float accum_cell(const SbGrid& g, const SbPhys& ph, c
     f.gam_delta[idx] = gd;
     f.err_eta[idx] = (th - ed - ld_s<T>(f.eta_init, idx, ph.base_eta)) * 0.5f;
     f.err_gam[idx] = (gm - gd - ld_s<T>(f.gam_init, idx, ph.base_gam)) * 0.5f;
-    // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x)))
-    float4 m = fwd[idx];
-    const float d1 = dist_from_disp(
-        sample_map(g, bwd, F, pos_from_disp_fast(F, f3{m.x, m.y, m.z}, g.invh, g.nT)), g.invh);
-    m = bwd[idx];
+    // estimateDistortion: dist(x, bwd(fwd(x))) and dist(x, fwd(bwd(x))); fwd(x)
+    // is sample 4 above (the cell's own map entry), whose stencil is reused
+    const float d1 = dist_from_disp(map_at_stencil(g, bwd, F, c4), g.invh);
+    const float4 m = bwd[idx];
     const float d2 = dist_from_disp(
         sample_map(g, fwd, F, pos_from_disp_fast(F, f3{m.x, m.y, m.z}, g.invh, g.nT)), g.invh);
     const float dist = fmaxf(fabsf(d1), fabsf(d2));
