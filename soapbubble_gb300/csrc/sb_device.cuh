@@ -174,12 +174,22 @@ __device__ __noinline__ f3 slerp_disp_far(float s0, float c0, f3 dA, f3 dB, floa
 //                   + (p^3+6p^2+17p+17) u^3/20160,   p = a (1-a);
 // the truncation is below 1e-9 relative.  For chords up to 1/16 (u < 0.004)
 // the u^2 and u^3 terms change the coefficients by less than 1e-9 and are
-// dropped.  Farther points take the exact formula out of line.
+// dropped, and for chords up to 2^-6.5 (u < 1.3e-4) the u^2 term of k and
+// c2^2/12 in u too.  Farther points take the exact formula out of line.
 __device__ __forceinline__ f3 slerp_disp_inl(float s0, float c0, f3 dA, f3 dB, float a) {
     const f3 e = dB - dA;
     const float c2 = dot3(e, e);
     if (c2 > 0.0625f) return slerp_disp_far(s0, c0, dA, dB, a);
     const float b = 1.0f - a;
+    if (c2 <= 0x1p-13f) {
+        // chords up to 2^-6.5 (a grid step of 512 rows and finer): u = c2 and
+        // first order in u (the dropped terms are below 2e-10 absolute)
+        const float cB = a * fmaf(c2 * fmaf(-a, a, 1.0f), 1.0f / 6.0f, 1.0f);
+        const float cA = b * fmaf(c2 * fmaf(-b, b, 1.0f), 1.0f / 6.0f, 1.0f);
+        const float k = 0.5f * a * b * c2;
+        const f3 C = {s0, 0.0f, c0};
+        return cA * dA + cB * dB + k * C;
+    }
     if (c2 <= 0.00390625f) {
         const float u = c2 * fmaf(c2, 1.0f / 12.0f, 1.0f);
         const float a2 = a * a, b2 = b * b;
@@ -393,6 +403,28 @@ __device__ __forceinline__ f3 map_point(const SbGrid& g, const Frame& F, float4 
 __device__ SB_GEOM_INLINE f3 map_at_stencil(const SbGrid& g, const float4* __restrict__ map,
                                              const Frame& F, const CStencil& s) {
     const int nP = g.nP;
+    if (!(s.v0 | s.v1)) {
+        // Rows r0, r0 + 1 and columns c00, c00 + 1: the four points are
+        // formed in the frame of entry (r0, c00), where that entry needs no
+        // conversion, the next row adds the difference of the row centres and
+        // the next column is a rotation by one grid step (a uniform table
+        // entry); the interpolated point is converted to F once.
+        const float4 Dll = map[s.r0 * nP + s.c00], Dlr = map[s.r0 * nP + s.c01];
+        const float4 Dhl = map[s.r1 * nP + s.c10], Dhr = map[s.r1 * nP + s.c11];
+        const float4 R0 = __ldg(&g.rowtab[s.r0]), R1 = __ldg(&g.rowtab[s.r1]);
+        const float2 t = __ldg(&g.rottab[g.nT + 1]);  // sin h, cos h - 1
+        const float ds = (R1.x - R0.x) + (R1.y - R0.y), dz = (R1.z - R0.z) + (R1.w - R0.w);
+        const f3 ll = {Dll.x, Dll.y, Dll.z};
+        const f3 lr = {Dlr.x + t.y * R0.x + t.y * Dlr.x - t.x * Dlr.y,
+                       t.x * R0.x + t.x * Dlr.x + Dlr.y + t.y * Dlr.y, Dlr.z};
+        const f3 hl = {ds + Dhl.x, Dhl.y, dz + Dhl.z};
+        const f3 hr = {ds + Dhr.x + t.y * R1.x + t.y * Dhr.x - t.x * Dhr.y,
+                       t.x * R1.x + t.x * Dhr.x + Dhr.y + t.y * Dhr.y, dz + Dhr.z};
+        const f3 lo = slerp_disp(R0.x, R0.z, ll, lr, s.b);
+        const f3 hi = slerp_disp(R0.x, R0.z, hl, hr, s.b);
+        const f3 m = slerp_disp(R0.x, R0.z, lo, hi, s.a);
+        return map_point(g, F, make_float4(m.x, m.y, m.z, 0.0f), s.r0, s.c00);
+    }
     const f3 ll = map_point(g, F, map[s.r0 * nP + s.c00], s.r0, s.c00);
     const f3 lr = map_point(g, F, map[s.r0 * nP + s.c01], s.r0, s.c01);
     const f3 hl = map_point(g, F, map[s.r1 * nP + s.c10], s.r1, s.c10);

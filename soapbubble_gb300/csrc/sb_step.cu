@@ -165,7 +165,7 @@ __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, c
     f3 d1s[5];
     sample_map_multi5(g, f.bwd[cur ^ 1], F, d1s);
     float attrib = 0.0f;
-#pragma unroll 1
+#pragma unroll 2
     for (int k = 0; k < 5; ++k) {
         const CStencil c1 = centred_stencil(g, pos_from_disp_fast(F, d1s[k], g.invh, g.nT), 0.0f);
         const f3 d2 = map_at_stencil(g, f.bwdprev, F, c1);
@@ -692,13 +692,6 @@ __device__ __forceinline__ const SbBubbleDesc& stage_tile_desc(SbBubbleDesc* con
         SB_CELL_KERNEL_BODY(name##_cell)                                               \
     }
 
-#define SB_CELL_KERNEL_T(name)                                                         \
-    template <class T>                                                                 \
-    __global__ void __launch_bounds__(256) k_##name(SbBubbleDesc* const* __restrict__ descs, \
-                                                    const int2* __restrict__ tiles) {  \
-        SB_CELL_KERNEL_BODY(name##_cell<T>)                                            \
-    }
-
 // k_advect_maps is held to 48 registers per thread (five 256-thread blocks
 // per SM; a few spilled values): measured 61 -> 58 us on c1.
 template <class T>
@@ -707,7 +700,15 @@ __global__ void __launch_bounds__(256, 5) k_advect_maps(SbBubbleDesc* const* __r
     SB_CELL_KERNEL_BODY(advect_maps_cell<T>)
 }
 SB_CELL_KERNEL(velocity)
-SB_CELL_KERNEL_T(bimocq)
+// k_bimocq is held to 64 registers per thread with its five samples taken two
+// at a time (two independent map-lookup chains in flight per thread; a few
+// spilled values): measured 79.7 -> 75.9 us on c1 (either change alone, or
+// all five samples unrolled, is slower).
+template <class T>
+__global__ void __launch_bounds__(256, 4) k_bimocq(SbBubbleDesc* const* __restrict__ descs,
+                                                   const int2* __restrict__ tiles) {
+    SB_CELL_KERNEL_BODY(bimocq_cell<T>)
+}
 // k_assemble / k_post: the instantiations with VISC = true evaluate the
 // viscous forces (every bubble of a plan has the same switch).
 template <bool VISC>
