@@ -54,7 +54,7 @@ ALG_BYTES_PER_CELL = {
     "k_post": 64,          # gamma',x,dx,xff(8),eta',u_th',u_ph',uair,vair -> gamma,dgamma,eta,deta,u_th,u_ph
     "k_accum": 80,         # eta_delta,gamma_delta,fwd',bwd',deta,dgamma,eta,gamma,eta_init,gamma_init
                            # -> eta_delta,gamma_delta,err_eta,err_gamma
-    "k_reinit": 0,        # no traffic unless re-initialising (about 1 step in 10)
+    "k_reinit": 0,        # not counted: it corrects only on re-initialising steps (half the c1 run)
 }
 # The implicit solve, per cell.  Fixed: set-up (r0, rhs, dmass, cE, cS, the
 # previous increment dx -> x (float-float), r, q, z or z1 = 44), the final true-residual check (x, r0,
