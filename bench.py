@@ -188,7 +188,7 @@ def workload_config(extra=None):
                    "iterations",
          "solver_tol": 1e-6, "seed": SEED,
          "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); "
-               "state 121 MB per bubble"}
+               f"state {state_mb():.0f} MB per bubble"}
     if extra:
         c.update(extra)
     return c
