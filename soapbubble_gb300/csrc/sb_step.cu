@@ -596,6 +596,130 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
     }
 }
 
+// 128-bit accesses to four consecutive cells (the arena's arrays are
+// 256-byte aligned and four-cell groups never straddle a row).
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+__device__ __forceinline__ void ld4(const float2* p, float2 (&v)[4]) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+    v[0] = make_float2(a.x, a.y); v[1] = make_float2(a.z, a.w);
+    v[2] = make_float2(b.x, b.y); v[3] = make_float2(b.z, b.w);
+}
+__device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <class T>
+__device__ __forceinline__ void st4_s(SbScalar* p, int i, const float (&v)[4], float base) {
+    (void)base;
+    st4(reinterpret_cast<float*>(p) + i, v);
+}
+template <>
+__device__ __forceinline__ void st4_s<__nv_bfloat16>(SbScalar* p, int i, const float (&v)[4], float base) {
+    const __nv_bfloat162 a = __floats2bfloat162_rn(v[0] - base, v[1] - base);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(v[2] - base, v[3] - base);
+    *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p) + i) =
+        make_uint2(*reinterpret_cast<const unsigned*>(&a), *reinterpret_cast<const unsigned*>(&b));
+}
+
+// gnew_diff of two cells whose x, xff and gamma_adv are at hand.
+__device__ __forceinline__ float gnew_diff_v(float xa, float2 da, float ga, float xb, float2 db,
+                                             float gb, float gmax) {
+    const bool ca = gamma_clamped(xa, gmax), cb = gamma_clamped(xb, gmax);
+    if (!ca && !cb) return (ga - gb) + ((da.x - db.x) + (da.y - db.y));
+    return (ca ? gmax : xa) - (cb ? gmax : xb);
+}
+
+// post_cell (without the viscous forces) on the four cells idx .. idx + 3
+// of one row: every input and output moves in 128-bit accesses along phi
+// (the west neighbour of the first cell in scalar ones), and each cell
+// does post_cell's operations.
+template <class T>
+__device__ __forceinline__ void post_quad(const SbGrid& g, const SbPhys& ph, const SbFields& f,
+                                          int idx) {
+    const int i = idx >> g.logP, j = idx & g.maskP;
+    const int nP = g.nP;
+    const float invDt = f.step->invDt, evapDt = f.step->evapDt;
+    const float gmax = ph.gmax, M = ph.M, Cr = ph.Cr;
+    const bool hasS = i < g.nT - 1;
+    float gO[4], X[4], DX[4], E[4], U1[4], UA[4];
+    float2 XF[4];
+    ld4(f.gam_adv + idx, gO);
+    ld4(f.x + idx, X);
+    ld4(f.dx + idx, DX);
+    ld4(f.eta_adv + idx, E);
+    ld4(f.uph_adv + idx, U1);
+    ld4(f.uair + idx, UA);
+    ld4(f.xff + idx, XF);
+    const int w = i * nP + ((j - 1) & g.maskP);
+    const float gW = f.gam_adv[w], xW = f.x[w], eW = f.eta_adv[w];
+    const float2 xfW = f.xff[w];
+    float gS[4], XS[4], ES[4], V1[4], VA[4];
+    float2 XFS[4];
+    if (hasS) {
+        ld4(f.gam_adv + idx + nP, gS);
+        ld4(f.x + idx + nP, XS);
+        ld4(f.eta_adv + idx + nP, ES);
+        ld4(f.xff + idx + nP, XFS);
+        ld4(f.uth_adv + idx, V1);
+        ld4(f.vair + idx, VA);
+    }
+    const float cscT = 1.0f / g.sin_c[i];
+    const float f3v = hasS ? ph.gs * g.sin_e[i + 1] : 0.0f;
+    const float nan = __int_as_float(0x7fffffff);
+    float oG[4], oDG[4], oE[4], oDE[4], oU[4], oV[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float mdtdiv;  // -dt * div
+        if (gamma_clamped(X[k], gmax)) {
+            oG[k] = gmax;
+            oDG[k] = gmax - gO[k];
+            mdtdiv = -1.0f;
+        } else {
+            oG[k] = X[k];
+            oDG[k] = DX[k];
+            mdtdiv = (X[k] > 2.0f * gO[k]) ? 1.0f : DX[k] / gO[k];
+        }
+        const float e = E[k];
+        const float de = e * mdtdiv + evapDt;
+        if (e + de >= 0.0f) {
+            oE[k] = e + de;
+            oDE[k] = de;
+        } else {
+            oE[k] = 0.0f;
+            oDE[k] = -e;
+        }
+        // u_phi face between cells k - 1 and k (the face thickness form of
+        // post_cell)
+        const float ef = 0.5f * ((k ? E[k - 1] : eW) + e);
+        if (ef == 0.0f) {
+            oU[k] = nan;
+        } else {
+            const float dG = k ? gnew_diff_v(X[k], XF[k], gO[k], X[k - 1], XF[k - 1], gO[k - 1], gmax)
+                               : gnew_diff_v(X[k], XF[k], gO[k], xW, xfW, gW, gmax);
+            const float pGpx = g.invh * dG * cscT;
+            oU[k] = (U1[k] * invDt * ef - M * pGpx + Cr * UA[k]) / (invDt * ef + Cr);
+        }
+        if (hasS) {
+            const float es = 0.5f * (e + ES[k]);
+            if (es == 0.0f) {
+                oV[k] = nan;
+            } else {
+                const float pGpy =
+                    g.invh * gnew_diff_v(XS[k], XFS[k], gS[k], X[k], XF[k], gO[k], gmax);
+                oV[k] = ((V1[k] * invDt + f3v) * es - M * pGpy + Cr * VA[k]) / (invDt * es + Cr);
+            }
+        }
+    }
+    st4_s<T>(f.gam, idx, oG, ph.base_gam);
+    st4(f.d_gam + idx, oDG);
+    st4_s<T>(f.eta, idx, oE, ph.base_eta);
+    st4(f.d_eta + idx, oDE);
+    st4(f.uph + idx, oU);
+    if (hasS) st4(f.uth + idx, oV);
+}
+
 __device__ __forceinline__ float warp_max(float v) {
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
@@ -721,6 +845,19 @@ template <class T, bool VISC>
 __global__ void __launch_bounds__(256) k_post(SbBubbleDesc* const* __restrict__ descs,
                                               const int2* __restrict__ tiles) {
     SB_CELL_KERNEL_BODY(post_cell<T, VISC>)
+}
+
+// The non-viscous post-solve update, four cells per thread (a tile of n
+// cells runs in n / 4 threads).
+template <class T>
+__global__ void __launch_bounds__(64) k_post4(SbBubbleDesc* const* __restrict__ descs,
+                                              const int2* __restrict__ tiles) {
+    __shared__ __align__(16) SbBubbleDesc s_d;
+    const int2 t = tiles[blockIdx.x];
+    const SbBubbleDesc& d = stage_tile_desc(descs, t.x, &s_d);
+    if (d.halted) return;
+    const int idx = t.y + 4 * threadIdx.x;
+    if (idx < d.g.N) post_quad<T>(d.g, d.ph, d.f, idx);
 }
 
 // k_accum is held to 64 registers per thread (a few spilled values): the
@@ -977,8 +1114,8 @@ cudaError_t launch_plan_stage(const SbStepPlan& P, int stage, cudaStream_t s) {
                 if (bf) k_post<__nv_bfloat16, true><<<n, block, 0, s>>>(d, t);
                 else k_post<float, true><<<n, block, 0, s>>>(d, t);
             } else {
-                if (bf) k_post<__nv_bfloat16, false><<<n, block, 0, s>>>(d, t);
-                else k_post<float, false><<<n, block, 0, s>>>(d, t);
+                if (bf) k_post4<__nv_bfloat16><<<n, block / 4, 0, s>>>(d, t);
+                else k_post4<float><<<n, block / 4, 0, s>>>(d, t);
             }
             break;
         case STAGE_ACCUM:
