@@ -119,7 +119,17 @@ void derive_phys(const sb_params& p, SbPhys& ph) {
     ph.gs = (float)gs;
     ph.re = (float)(kNu / (U * p.radius));
     ph.viscous = p.viscous ? 1 : 0;
-    ph.gmax = (float)(kSigmaA / sigma_r / p.Gamma_m);
+    const double gmax = kSigmaA / sigma_r / p.Gamma_m;
+    ph.gmax = (float)gmax;
+    // The reference marks gamma > gmax - 1e-7 as at its maximum
+    // (kernel/bubble.cu:28, FP64).  Near gmax ~ 29 that band is below FP32's
+    // resolution (1.9e-6) and gmax - 1e-7 rounds to gmax itself, so a cell
+    // holding gmax would not count.  The threshold is the lower of
+    // gmax - 1e-7 and the float two steps below gmax: gmax and the float
+    // just below it (an interpolation of gmax values, rounded) are at the
+    // maximum, and a broken cell whose gamma is set to gmax stays broken
+    // for every reader.
+    ph.gthr = std::min((float)(gmax - 1e-7), std::nextafter(std::nextafter(ph.gmax, 0.0f), 0.0f));
     ph.blend = (float)p.blendCoeff;
     ph.evap = (float)(kEvaporation * p.radius / (p.H * U));
 }

@@ -30,7 +30,6 @@ namespace sb {
 namespace {
 
 constexpr int kBlock = 128;
-constexpr float kEps = 1e-7f;  // bubble.cu:28
 
 __constant__ float kW5[5] = {0.125f, 0.125f, 0.125f, 0.125f, 0.5f};
 
@@ -180,8 +179,10 @@ __device__ __forceinline__ void bimocq_cell(const SbGrid& g, const SbPhys& ph, c
     f.eta_adv[idx] = fmaxf(0.0f, attrib);
 }
 
-__device__ __forceinline__ bool is_broken(float gamma, float eta, float gmax) {
-    return gamma > gmax - kEps || eta == 0.0f;
+// A cell at its maximum concentration or without film (kernel/bubble.cu:
+// 1317; thr: SbPhys::gthr, the FP32 form of gmax - 1e-7).
+__device__ __forceinline__ bool is_broken(float gamma, float eta, float thr) {
+    return gamma > thr || eta == 0.0f;
 }
 
 // VISCOUS variant (include/header.cuh:98, off in the reference's build): the
@@ -436,18 +437,18 @@ __device__ __forceinline__ void assemble_compute(const SbGrid& g, const SbPhys& 
 
     // neighbour gamma (a broken neighbour holds gmax) and broken flags
     const float gEr = c.gEr, gWr = c.gWr;
-    const bool bE = is_broken(gEr, etaE, gmax), bW = is_broken(gWr, etaW, gmax);
+    const bool bE = is_broken(gEr, etaE, ph.gthr), bW = is_broken(gWr, etaW, ph.gthr);
     const float gE = bE ? gmax : gEr, gW = bW ? gmax : gWr;
     bool bN = false, bS = false;
     float gN = gamma, gS = gamma, gNr = gamma, gSr = gamma;
     if (i != 0) {
         gNr = c.gNr;
-        bN = is_broken(gNr, etaN, gmax);
+        bN = is_broken(gNr, etaN, ph.gthr);
         gN = bN ? gmax : gNr;
     }
     if (i != nT - 1) {
         gSr = c.gSr;
-        bS = is_broken(gSr, etaS, gmax);
+        bS = is_broken(gSr, etaS, ph.gthr);
         gS = bS ? gmax : gSr;
     }
     const float lap = wE * (gamma - gE) + wW * (gamma - gW) + wN * (gamma - gN) + wS * (gamma - gS);
@@ -509,7 +510,7 @@ __device__ __forceinline__ void assemble_cell(const SbGrid& g, const SbPhys& ph,
     AsmCell c;
     c.gamma = f.gam_adv[idx];
     c.eta = eta_a[idx];
-    if (is_broken(c.gamma, c.eta, gmax)) {
+    if (is_broken(c.gamma, c.eta, ph.gthr)) {
         assemble_broken(f, gmax, idx);
         atomicAdd(&f.stats->broken_cells, 1);
         return;
@@ -621,7 +622,7 @@ __device__ __forceinline__ void assemble_quad(const SbGrid& g, const SbPhys& ph,
         AsmCell c;
         c.gamma = G[k];
         c.eta = E[k];
-        if (is_broken(c.gamma, c.eta, gmax)) {
+        if (is_broken(c.gamma, c.eta, ph.gthr)) {
             oD[k] = 1.0f; oE[k] = 0.0f; oS[k] = 0.0f; oR[k] = 0.0f; oB[k] = gmax;
             f.gam_adv[idx + k] = gmax;
             ++broken;
@@ -665,9 +666,10 @@ __device__ __forceinline__ void assemble_quad(const SbGrid& g, const SbPhys& ph,
 // BIMOCQ accumulates.  Increments are carried directly (dx from the solve,
 // d_eta = -eta dt div + evap dt) instead of as differences of O(1) values.
 // Neighbouring new gamma values are clamped on the fly exactly as
-// divergenceKernel_fromGamma clamps them in place.
-__device__ __forceinline__ bool gamma_clamped(float gm, float gmax) {
-    return gm <= 0.0f || gm > gmax - kEps;
+// divergenceKernel_fromGamma clamps them in place (kernel/bubble.cu:1287;
+// thr as in is_broken).
+__device__ __forceinline__ bool gamma_clamped(float gm, float thr) {
+    return gm <= 0.0f || gm > thr;
 }
 
 // Difference gamma_new(a) - gamma_new(b) of two cells.  The increments
@@ -675,9 +677,9 @@ __device__ __forceinline__ bool gamma_clamped(float gm, float gmax) {
 // new gamma varies along phi by parts in 1e5 of the increment, and the
 // Marangoni force there (1/sin(theta) times that difference) would inherit
 // the increment's FP32 rounding (2e-4 of u_phi at the config.txt grid).
-__device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, float gmax) {
+__device__ __forceinline__ float gnew_diff(const SbFields& f, int a, int b, float gmax, float thr) {
     const float xa = f.x[a], xb = f.x[b];
-    const bool ca = gamma_clamped(xa, gmax), cb = gamma_clamped(xb, gmax);
+    const bool ca = gamma_clamped(xa, thr), cb = gamma_clamped(xb, thr);
     if (!ca && !cb) {
         const float2 da = f.xff[a], db = f.xff[b];
         return (f.gam_adv[a] - f.gam_adv[b]) + ((da.x - db.x) + (da.y - db.y));
@@ -696,7 +698,7 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
     const float gOld = f.gam_adv[idx];
     const float gNew = f.x[idx];
     float mdtdiv;  // -dt * div
-    if (gamma_clamped(gNew, gmax)) {
+    if (gamma_clamped(gNew, ph.gthr)) {
         st_s<T>(f.gam, idx, gmax, ph.base_gam);
         f.d_gam[idx] = gmax - gOld;
         mdtdiv = -1.0f;
@@ -735,7 +737,7 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
             f.uph[idx] = __int_as_float(0x7fffffff);
         } else {
             const float cscT = 1.0f / g.sin_c[i];
-            const float pGpx = g.invh * gnew_diff(f, idx, w, gmax) * cscT;
+            const float pGpx = g.invh * gnew_diff(f, idx, w, gmax, ph.gthr) * cscT;
             if (VISC) {
                 // applyforcevelphiKernel_viscous (bubble.cu:1987-2038): the
                 // mirrored wind mix and fu
@@ -756,7 +758,7 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
         if (ef == 0.0f) {
             f.uth[idx] = __int_as_float(0x7fffffff);
         } else {
-            const float pGpy = g.invh * gnew_diff(f, s, idx, gmax);
+            const float pGpy = g.invh * gnew_diff(f, s, idx, gmax, ph.gthr);
             if (VISC) {
                 // applyforcevelthetaKernel_viscous (bubble.cu:1940-1983)
                 const float vAir = 0.5f * (f.vair[idx] * f.step->mixA -
@@ -774,8 +776,8 @@ __device__ __forceinline__ void post_cell(const SbGrid& g, const SbPhys& ph, con
 
 // gnew_diff of two cells whose x, xff and gamma_adv are at hand.
 __device__ __forceinline__ float gnew_diff_v(float xa, float2 da, float ga, float xb, float2 db,
-                                             float gb, float gmax) {
-    const bool ca = gamma_clamped(xa, gmax), cb = gamma_clamped(xb, gmax);
+                                             float gb, float gmax, float thr) {
+    const bool ca = gamma_clamped(xa, thr), cb = gamma_clamped(xb, thr);
     if (!ca && !cb) return (ga - gb) + ((da.x - db.x) + (da.y - db.y));
     return (ca ? gmax : xa) - (cb ? gmax : xb);
 }
@@ -821,7 +823,7 @@ __device__ __forceinline__ void post_quad(const SbGrid& g, const SbPhys& ph, con
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         float mdtdiv;  // -dt * div
-        if (gamma_clamped(X[k], gmax)) {
+        if (gamma_clamped(X[k], ph.gthr)) {
             oG[k] = gmax;
             oDG[k] = gmax - gO[k];
             mdtdiv = -1.0f;
@@ -845,8 +847,8 @@ __device__ __forceinline__ void post_quad(const SbGrid& g, const SbPhys& ph, con
         if (ef == 0.0f) {
             oU[k] = nan;
         } else {
-            const float dG = k ? gnew_diff_v(X[k], XF[k], gO[k], X[k - 1], XF[k - 1], gO[k - 1], gmax)
-                               : gnew_diff_v(X[k], XF[k], gO[k], xW, xfW, gW, gmax);
+            const float dG = k ? gnew_diff_v(X[k], XF[k], gO[k], X[k - 1], XF[k - 1], gO[k - 1], gmax, ph.gthr)
+                               : gnew_diff_v(X[k], XF[k], gO[k], xW, xfW, gW, gmax, ph.gthr);
             const float pGpx = g.invh * dG * cscT;
             oU[k] = (U1[k] * invDt * ef - M * pGpx + Cr * UA[k]) / (invDt * ef + Cr);
         }
@@ -856,7 +858,7 @@ __device__ __forceinline__ void post_quad(const SbGrid& g, const SbPhys& ph, con
                 oV[k] = nan;
             } else {
                 const float pGpy =
-                    g.invh * gnew_diff_v(XS[k], XFS[k], gS[k], X[k], XF[k], gO[k], gmax);
+                    g.invh * gnew_diff_v(XS[k], XFS[k], gS[k], X[k], XF[k], gO[k], gmax, ph.gthr);
                 oV[k] = ((V1[k] * invDt + f3v) * es - M * pGpy + Cr * VA[k]) / (invDt * es + Cr);
             }
         }

@@ -40,6 +40,7 @@ enum { kStoreF32 = 0, kStoreBF16 = 1 };
 // Constant physical coefficients of one bubble.
 struct SbPhys {
     float M, Cr, gs, gmax, blend, evap;
+    float gthr;       // gamma above gthr is at its maximum gmax (the cell is broken)
     float base_eta, base_gam;  // BF16 storage: offsets of the eta and gamma fields (else 0)
     int plain_adv;    // 1: thickness advected like gamma, no characteristic maps (BIMOCQ off)
     int single_step;  // 1: velocity traced in one step (RUNGE_KUTTA off)

@@ -21,11 +21,19 @@ MAPS = [("fwd_t", "fwd_p"), ("bwd_t", "bwd_p"), ("bwdprev_t", "bwdprev_p")]
 
 def sync_state(gb, ob) -> None:
     """Upload the oracle state to the GPU, then copy the GPU's (FP32-rounded)
-    state back into the oracle, so that both start from identical values."""
+    state back into the oracle, so that both start from identical values.
+    A concentration at the FP32 gmax is the clamp value (a broken cell's):
+    it goes back to the oracle as its FP64 gmax, which the reference's test
+    gamma > gmax - 1e-7 marks as at the maximum (the FP32 gmax lies below
+    that band)."""
     for gname, oname in FIELD_MAP.items():
         gb.upload(gname, ob.a[oname])
+    gmax32 = np.float32(ob.p.gammaMax)
     for gname, oname in FIELD_MAP.items():
-        ob.a[oname][...] = gb.download(gname).reshape(ob.a[oname].shape)
+        v = gb.download(gname).reshape(ob.a[oname].shape)
+        if gname in ("gamma", "gamma_init", "gamma_init_last"):
+            v = np.where(v == gmax32, ob.p.gammaMax, v)
+        ob.a[oname][...] = v
 
 
 def rel_err(gpu: np.ndarray, ref: np.ndarray, floor: float = 1e-30) -> float:

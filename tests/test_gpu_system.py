@@ -154,3 +154,62 @@ def test_tiny_surfactant_keeps_the_solve_in_range(oracle, gpulib):
             np.testing.assert_allclose(a[small], b[small], rtol=1e-3, atol=0)
     finally:
         gb.close()
+
+
+def test_cells_at_the_fp32_gmax_are_broken(gpulib):
+    """The reference marks gamma > gmax - 1e-7 as at the maximum
+    (kernel/bubble.cu:1317).  At gmax ~ 29 that band is below FP32's
+    resolution and gmax - 1e-7 rounds to gmax itself, so a threshold taken
+    literally in FP32 would leave cells holding gmax (every clamped cell)
+    unbroken, and a broken cell that the assembly sets to gmax would look
+    unbroken to a neighbour reading it afterwards.  Cells whose advected
+    concentration is the FP32 gmax must get the identity row."""
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    nT = 64
+    f = synth.make_fields("c0", nT, 31)
+    gb = GpuBubble(make_params(nT, 0.005))
+    try:
+        gb.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+        gmax32 = float(np.float32(29.347029))  # the default parameters' gmax in FP32
+        g = gb.download("gamma")
+        g[20:30, 40:60] = gmax32
+        gb.upload("gamma", g)
+        gb.step(1, 0.0, 0.005)
+        S = _gpu_system(gb)
+        inner = (slice(22, 28), slice(42, 58))  # stencils inside the patch
+        assert np.all(S["dmass"][inner] == 1.0) and not S["w_east"][inner].any()
+        assert np.all(S["r0"][inner] == 0.0)
+        assert gb.stats().broken_cells >= 6 * 16
+    finally:
+        gb.close()
+
+
+def test_twin_bubbles_stay_identical_through_the_rupture(gpulib):
+    """Two bubbles from the same fields, stepped on their own streams so that
+    their kernels overlap, through the film's rupture (broken cells from
+    about step 300 at this grid): bit-identical fields at the end.  A read
+    of a value that another thread of the same kernel writes would make the
+    twins differ."""
+    from soapbubble_gb300 import synth
+    from soapbubble_gb300.bubble import GpuBubble, make_params
+    nT, dt = 128, 0.002
+    f = synth.make_fields("c1", nT, 20261203)
+    a = GpuBubble(make_params(nT, dt, solver_tol=1e-6))
+    b = GpuBubble(make_params(nT, dt, solver_tol=1e-6))
+    try:
+        for gb in (a, b):
+            gb.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
+        broken = 0
+        for k in range(0, 600, 10):
+            t = k * dt
+            a.step(10, t, dt)
+            b.step(10, t, dt)
+            if k % 100 == 90:
+                broken = max(broken, a.stats().broken_cells)
+        assert broken > 0  # the run went through the rupture
+        for name in ("eta", "gamma", "u_theta", "u_phi", "eta_delta", "gamma_delta", "fwd_t", "bwd_t"):
+            np.testing.assert_array_equal(a.download(name), b.download(name), err_msg=name)
+    finally:
+        a.close()
+        b.close()
