@@ -538,9 +538,7 @@ __device__ __forceinline__ const float* row_blob(const SbGrid& g, const SbFields
 // one step to the next, so r = r0 - A dx_prev is much smaller than r0 and
 // the solve needs fewer iterations; it stops at the same relative residual
 // of the same system.  A non-finite previous value starts from zero.
-// Otherwise the iterate starts from dx = 0 (gamma_new = gamma_adv).  dx
-// itself is only read here (the plain mode's iterate already holds it), so
-// the neighbours' values are those of the previous solve in every block.
+// Otherwise the iterate starts from dx = 0 (gamma_new = gamma_adv).
 template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int i,
                                          const SolverConfig& cfg, float (&rv)[PER], ff& bb) {
@@ -555,8 +553,13 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
     // neighbour sees the same value.
     // The iterate of a scaled cell (sb_scale.cuh) is dx / s.
     const float gmax = f.self->ph.gmax, invDt = f.step->invDt;
+    // The previous increment is read where this phase does not write it:
+    // f.dx in mixed mode (the iterate is xff), xff's leading part in plain
+    // mode (whose iterate is dx; the last pass of every solve leaves
+    // xff = (dx, 0)), so that a row reads its neighbours' values of the
+    // previous solve whatever the order in which the rows are set up.
     auto prev = [&](int c, int ic) {
-        const float v = f.dx[c], ga = f.gam_adv[c];
+        const float v = MIXED ? f.dx[c] : f.xff[c].x, ga = f.gam_adv[c];
         const float lim = fminf(ga, gmax - ga);
         const float x0 = isfinite(v) ? fminf(fmaxf(v, -lim), lim) : 0.0f;
         const int k = diag_scale_k(ga, g.sin_c[ic], invDt);
@@ -579,7 +582,7 @@ __device__ __forceinline__ void row_init(const SbGrid& g, const SbFields& f, int
                 if (i > 0) ax += f.cS[c - nP] * (x0 - prev(c - nP, i - 1));
                 r -= ax;
                 if (MIXED) f.xff[c] = make_float2(x0, 0.0f);
-                else if (x0 != f.dx[c]) f.dx[c] = x0;  // only where it was not finite
+                else f.dx[c] = x0;
             } else {
                 if (MIXED) f.xff[c] = make_float2(0.0f, 0.0f);
                 else f.dx[c] = 0.0f;

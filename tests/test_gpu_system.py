@@ -185,18 +185,20 @@ def test_cells_at_the_fp32_gmax_are_broken(gpulib):
         gb.close()
 
 
-def test_twin_bubbles_stay_identical_through_the_rupture(gpulib):
+@pytest.mark.parametrize("mode", [0, 1], ids=["mixed", "plain"])
+def test_twin_bubbles_stay_identical_through_the_rupture(gpulib, mode):
     """Two bubbles from the same fields, stepped on their own streams so that
     their kernels overlap, through the film's rupture (broken cells from
-    about step 300 at this grid): bit-identical fields at the end.  A read
-    of a value that another thread of the same kernel writes would make the
+    about step 300 at this grid): bit-identical fields at the end, with the
+    mixed-precision and the plain FP32 solve (both warm-started).  A read of
+    a value that another thread of the same kernel writes would make the
     twins differ."""
     from soapbubble_gb300 import synth
     from soapbubble_gb300.bubble import GpuBubble, make_params
     nT, dt = 128, 0.002
     f = synth.make_fields("c1", nT, 20261203)
-    a = GpuBubble(make_params(nT, dt, solver_tol=1e-6))
-    b = GpuBubble(make_params(nT, dt, solver_tol=1e-6))
+    a = GpuBubble(make_params(nT, dt, solver_tol=1e-6, solver_mode=mode))
+    b = GpuBubble(make_params(nT, dt, solver_tol=1e-6, solver_mode=mode))
     try:
         for gb in (a, b):
             gb.upload_fields(f.eta, f.gamma, f.uth, f.uph, f.uair_init, f.vair_init)
