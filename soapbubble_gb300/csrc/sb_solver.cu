@@ -275,7 +275,8 @@ __device__ __forceinline__ ff fold_halves(const ff (&h)[2]) {
 // unless the block still holds them), with the same arithmetic.
 template <int PER, int TB, bool BUILD>
 __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields& f, int i,
-                                                 Stage& S, const float (&rv)[PER]) {
+                                                 Stage& S, const float (&rv)[PER],
+                                                 bool store = true) {
     const int nP = g.nP, nT = g.nT, mask = g.maskP;
     const int row = i * nP;
     constexpr int H = PER >= 2 ? PER / 2 : 1;  // items per thread of the n/2-item steps
@@ -505,11 +506,13 @@ __device__ __forceinline__ void precondition_row(const SbGrid& g, const SbFields
     __syncthreads();
     if (BUILD) {
         // the row's factors to its global slot, for fetches by any block in
-        // later phases; the blob is the block's resident copy
+        // later phases (not when every block keeps its one row for the whole
+        // solve: no fetch happens then); the blob is the block's resident copy
         float* const dst = f.pcr + (size_t)i * (B.bytes / 4);
         const float4* src = reinterpret_cast<const float4*>(S.blob);
-        for (int k = threadIdx.x; k < B.bytes / 16; k += TB)
-            reinterpret_cast<float4*>(dst)[k] = src[k];
+        if (store)
+            for (int k = threadIdx.x; k < B.bytes / 16; k += TB)
+                reinterpret_cast<float4*>(dst)[k] = src[k];
         S.resident = dst;
         // generic writes of both copies before later bulk copies from the
         // global slot and into the blob
@@ -1251,7 +1254,7 @@ template <bool MIXED, int PER, int TB>
 __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
                                           const SolverConfig& cfg, int i, int kind,
                                           float beta, ff alpha, float* pA, const float* pB,
-                                          Stage& St) {
+                                          Stage& St, bool own_row = false) {
     (void)cfg;
     ff a = ff_zero(), b2 = ff_zero(), c2 = ff_zero();
     float rv[PER];
@@ -1259,7 +1262,7 @@ __device__ __forceinline__ void row_phase(const SbGrid& g, const SbFields& f,
         case K_SETUP:
         case K_SETUP_L:
             row_init<MIXED, PER, TB>(g, f, i, cfg, rv, c2);
-            precondition_row<PER, TB, true>(g, f, i, St, rv);
+            precondition_row<PER, TB, true>(g, f, i, St, rv, !own_row);
             break;
         case K_NEUMANN: {
             stage_fetch(St, row_blob(g, f, i), factor_blob(g.nP).bytes);
@@ -1477,7 +1480,7 @@ k_solve_one(SbGrid g, SbFields f, SbSolveSet S, SolverConfig cfg) {
         float* pA = (it & 1) ? f.q : f.p;  // p_new of iteration it
         float* pB = (it & 1) ? f.p : f.q;  // p_old
         for (int i = blockIdx.x; i < nT; i += G) {
-            row_phase<MIXED, PER, TB>(g, f, cfg, i, kind, beta, alpha, pA, pB, St);
+            row_phase<MIXED, PER, TB>(g, f, cfg, i, kind, beta, alpha, pA, pB, St, G >= nT);
             if (vals) reduce_row<TB>(S, 0, p, vals, reinterpret_cast<ff*>(St.work + g.nP));
         }
         if (!grid_barrier(S.bar, gen, G, &f.stats->wait_faults)) {
