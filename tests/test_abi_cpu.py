@@ -115,5 +115,7 @@ def test_null_handles_and_members_are_rejected(gpulib):
     assert L.sb_run(None, None, 1) == SB_ERR_INVALID
     assert L.sb_wait_staged(None) == SB_ERR_INVALID
     assert L.sb_batch_step(None, 1, 0.0, 0.005) == SB_ERR_INVALID
+    buf = (C.c_double * 4)()
+    assert L.sb_download_system(None, 0, buf, 4) == SB_ERR_INVALID
     L.sb_default_params(None)  # ignored, no crash
     assert L.sb_bytes_required(None) == 0
